@@ -1,0 +1,220 @@
+"""Generate golden vectors from the compiled reference vegas (vegas 6.4.1).
+
+Run in the development container, where the reference sources exist:
+
+    python oracle/build_ref.py          # compiles src/vegas/_vegas.pyx out of tree
+    python tests/golden/make_golden.py  # writes tests/golden/*.npz
+
+The fixtures let the oracle (and, through it, the CUDA path) be pinned on a
+machine without the reference.  Every integrator trace is recorded in
+"injected-sample" mode: ``ran_array_generator`` hands the reference uniforms
+u = k / 2**24 (k drawn from a seeded numpy generator, stored as uint32), and
+the integrand wrapper records the exact f values the reference consumed.
+
+Per iteration a trace stores the state the reference ended with (grid, sigf,
+sum_sigf) plus the iteration's mean, var, last_neval and neval_hcube_range;
+the state before iteration k is the state after iteration k-1 (the initial
+state is the freshly constructed integrator's).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+import build_ref  # noqa: E402
+
+U_SCALE = 2.0 ** -24
+
+
+class Recorder(object):
+    """ran_array_generator that records its draws as uint32 k (u = k/2^24)."""
+
+    def __init__(self, seed):
+        self.rng = np.random.default_rng(seed)
+        self.draws = []
+
+    def __call__(self, size):
+        k = self.rng.integers(0, 2 ** 24, size=size, dtype=np.uint32)
+        self.draws.append(k)
+        return k.astype(np.float64) * U_SCALE
+
+    def take(self):
+        out = np.concatenate(self.draws, axis=0) if self.draws else np.zeros((0, 0), np.uint32)
+        self.draws = []
+        return out
+
+
+def valid_grid(m):
+    ninc = np.asarray(m.ninc)
+    K = int(ninc.max())
+    g = np.full((len(ninc), K + 1), np.nan)
+    for d in range(len(ninc)):
+        g[d, :ninc[d] + 1] = np.asarray(m.grid)[d, :ninc[d] + 1]
+    return g
+
+
+def trace(v, limits, fcn_np, nitn, neval, seed, **kargs):
+    """Run the reference integrator nitn times (nitn=1 each) recording everything."""
+    rec = Recorder(seed)
+    integ = v.Integrator(limits, neval=neval, ran_array_generator=rec, **kargs)
+    fvals = []
+
+    @v.lbatchintegrand
+    def f(x):
+        fx = fcn_np(np.asarray(x))
+        if np.asarray(x).shape[0] > 1:     # skip the one-point probe call (pyx:3080)
+            fvals.append(np.array(fx, dtype=np.float64))
+        return fx
+
+    out = dict(
+        nstrat=np.asarray(integ.nstrat, np.int64),
+        ninc=np.asarray(integ.map.ninc, np.int64),
+        grid_init=valid_grid(integ.map),
+        sigf_init=np.array(integ.sigf, float),
+        sum_sigf_init=np.array(integ.sum_sigf),
+        min_neval_hcube=np.array(integ.min_neval_hcube),
+        max_neval_hcube=np.array(integ.max_neval_hcube),
+        neval=np.array(integ.neval),
+        neval_frac=np.array(integ.neval_frac),
+        nitn=np.array(nitn),
+    )
+    for k in range(nitn):
+        fvals.clear()
+        r = integ(f, nitn=1)
+        u = rec.take()
+        fx = np.concatenate(fvals)
+        assert fx.shape[0] == u.shape[0], (fx.shape, u.shape)
+        res = r.itn_results[-1]
+        out['u%d' % k] = u.astype(np.uint32)
+        out['f%d' % k] = fx
+        out['mean%d' % k] = np.array(res.mean)
+        # sdev exactly as the reference formed it: var ** 0.5 (pyx:3144)
+        out['sdev%d' % k] = np.array(list(res.internaldata[1].values())[0])
+        out['sigf%d' % k] = np.array(integ.sigf, float)
+        out['sum_sigf%d' % k] = np.array(integ.sum_sigf)
+        out['grid%d' % k] = valid_grid(integ.map)
+        out['last_neval%d' % k] = np.array(integ.last_neval)
+        out['range%d' % k] = np.array(integ.neval_hcube_range, np.int64)
+    return out
+
+
+def gauss4(x):
+    return (100 / np.pi) ** 2 * np.exp(-100 * np.sum((x - 0.5) ** 2, axis=1))
+
+
+def ridge(x, M=1000, s=0.01):
+    dim = x.shape[1]
+    c = (np.arange(M) + 0.5) / M
+    acc = np.zeros(x.shape[0])
+    for j in range(M):
+        r2 = np.zeros(x.shape[0])
+        for d in range(dim):
+            r2 += (x[:, d] - c[j]) * (x[:, d] - c[j])
+        acc += np.exp(-r2 / (2 * s * s))
+    return (2 * np.pi * s * s) ** (-0.5 * dim) * acc / M
+
+
+def const7(x):
+    return 7 * np.ones(x.shape[0], float)
+
+
+def adapt_cases(v):
+    """Direct AdaptiveMap cases: map edges, training skips, adapt variants."""
+    rng = np.random.default_rng(7)
+    cases = {}
+    # map incl. y == 0 and y == 1 (iy == ninc branch, pyx:354-359)
+    m = v.AdaptiveMap([[0, 0.3, 1.0], [-2, -1.5, 0, 6]], ninc=[5, 7])
+    y = np.concatenate([rng.random((64, 2)), [[0., 0.], [1., 1.], [0.2, 1.0], [1.0, 0.5]]])
+    x = np.empty_like(y)
+    jac = np.empty(len(y))
+    m.map(y, x, jac)
+    cases['map_grid'] = valid_grid(m)
+    cases['map_ninc'] = np.asarray(m.ninc, np.int64)
+    cases['map_y'] = y
+    cases['map_x'] = x
+    cases['map_jac'] = jac
+    # training with y in {0, 1} skipped (pyx:460) then adapt variants
+    idx = 0
+    for ninc, alpha, new_ninc, train in [
+            ([6, 6], 0.5, None, True), ([10, 7], 1.5, None, True), ([8, 8], -2.0, None, True),
+            ([9, 12], 0.0, [5, 20], True), ([20, 20], 0.7, [4, 9], True),
+            ([5, 9], 0.5, None, False), ([1, 4], 0.5, None, True), ([2, 3], 2.0, [3, 3], True)]:
+        m = v.AdaptiveMap([[0, 1], [-1, 2]], ninc=ninc)
+        g0 = valid_grid(m)
+        y = rng.random((200, 2))
+        y[:5, 0] = 0.0
+        y[5:10, 1] = 1.0
+        f = np.exp(-10 * (y[:, 0] - 0.3) ** 2) * (1 + y[:, 1] ** 3)
+        f[::17] = 0.0
+        if train:
+            m.add_training_data(y, f)
+            sum_f = np.array(m.sum_f)
+            n_f = np.array(m.n_f)
+        else:
+            sum_f = n_f = np.zeros((2, max(ninc)))
+        m.adapt(alpha=alpha, ninc=new_ninc)
+        p = 'adapt%d_' % idx
+        cases[p + 'grid_in'] = g0
+        cases[p + 'ninc_in'] = np.array(ninc, np.int64)
+        cases[p + 'y'] = y
+        cases[p + 'f'] = f
+        cases[p + 'train'] = np.array(train)
+        cases[p + 'sum_f'] = sum_f
+        cases[p + 'n_f'] = n_f
+        cases[p + 'alpha'] = np.array(alpha)
+        cases[p + 'new_ninc'] = np.array(new_ninc if new_ninc is not None else ninc, np.int64)
+        cases[p + 'grid_out'] = valid_grid(m)
+        idx += 1
+    cases['n_adapt'] = np.array(idx)
+    return cases
+
+
+def alloc_cases(v):
+    """Allocation from a given sigf, incl. the max_neval_hcube clamp."""
+    rng = np.random.default_rng(11)
+    out = {}
+    for k, (dim, neval, mx) in enumerate([(3, 2000, 50000), (2, 5000, 40), (4, 30000, 200)]):
+        integ = v.Integrator(dim * [[0, 1]], neval=neval, max_neval_hcube=mx,
+                             ran_array_generator=np.random.default_rng(k).random)
+        H = integ.nhcube
+        sigf = rng.random(H) ** 4
+        sigf[rng.random(H) < 0.1] = 0.0
+        sigf[0] = 50.0
+        integ.set(sigf=sigf)
+        hc = np.concatenate([np.asarray(b[-1]) for b in integ.random_batch(yield_hcube=True)])
+        out['alloc%d_sigf' % k] = np.asarray(integ.sigf, float)
+        out['alloc%d_sum_sigf' % k] = np.array(integ.sum_sigf)
+        out['alloc%d_neval_h' % k] = np.bincount(hc, minlength=H).astype(np.int64)
+        out['alloc%d_range' % k] = np.asarray(integ.neval_hcube_range, np.int64)
+        out['alloc%d_params' % k] = np.array([integ.neval, integ.neval_frac, integ.min_neval_hcube,
+                                              integ.max_neval_hcube, H], float)
+    out['n_alloc'] = np.array(3)
+    return out
+
+
+def main():
+    build_ref.build()
+    v = build_ref.import_reference()
+    np.savez_compressed(os.path.join(HERE, 'ref_gauss4_injected.npz'),
+                        **trace(v, 4 * [[0, 1]], gauss4, nitn=3, neval=10000, seed=1,
+                                alpha=0.5, beta=0.75))
+    np.savez_compressed(os.path.join(HERE, 'ref_ridge_injected.npz'),
+                        **trace(v, 4 * [[0, 1]], ridge, nitn=3, neval=8000, seed=2,
+                                alpha=0.5, beta=0.75))
+    np.savez_compressed(os.path.join(HERE, 'ref_const_injected.npz'),
+                        **trace(v, [[0, 1]], const7, nitn=3, neval=100, seed=3, alpha=0.0))
+    np.savez_compressed(os.path.join(HERE, 'ref_beta0_injected.npz'),
+                        **trace(v, [[0, np.pi], [-np.pi / 2, np.pi / 2]],
+                                lambda x: (np.sin(x[:, 0]) ** 2 + np.cos(x[:, 1]) ** 2) / np.pi ** 2,
+                                nitn=2, neval=3000, seed=4, beta=0.0))
+    np.savez_compressed(os.path.join(HERE, 'ref_map_adapt.npz'), **adapt_cases(v), **alloc_cases(v))
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith('.npz'):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == '__main__':
+    main()
