@@ -1,0 +1,319 @@
+"""Benchmark: vegas+ on the ridge integrand (dim 4, M=1000 Gaussians of width
+0.01 on the diagonal), neval = 1e6 evaluations per iteration, FP32 sampling /
+map / evaluation with FP64 sums -- the vegas+ ridge workload.
+
+A step is one full vegas+ iteration: allocation of evaluations to the
+123462 hypercubes, Philox sampling + map + fused integrand evaluation +
+per-hypercube two-pass reduction + training histogram, and the grid adapt.
+
+Arms
+  (default)          this library on the GPU(s); one JSON line on rank 0.
+  --impl reference   the reference algorithm on the host cores: the CPU
+                     restatement in oracle/ (the reference's Cython cannot be
+                     built on the GPU host), all host threads, same workload.
+
+JSON keys follow the benchmark contract: value = evaluations/s with inputs
+resident in HBM (device loop, CUDA events on the launching stream); e2e = the
+same through the public API (Integrator.__call__ per step, host buffers for
+the integrand parameters and the result); roofline of the dominant kernel;
+cpu_baseline; clocks sampled during the timed region.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'time to 1e-4 rel. error & evals/s: flow-vegas+ vs plain vegas+, 1 GB300'
+WORKLOAD = 'vegas+ ridge: dim=4, M=1000 Gaussians s=0.01 on the diagonal, neval=1e6/itn, ' \
+           'ninc=1000 (actual [988,988,988,990]), nstrat [19,19,19,18], alpha=0.5, beta=0.75'
+NEVAL = 1000000
+DIM = 4
+RIDGE_M, RIDGE_S = 1000, 0.01
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-tta', action='store_true')
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler(object):
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            p = [q.strip() for q in ln.split(',')]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None,
+                'sm_max_mhz': max(smax) if smax else None, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    import vegas_gb300 as vg
+    from vegas_gb300 import _native as N
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        dist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    L = N.load()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    f = vg.Ridge(M=RIDGE_M, s=RIDGE_S)
+    exact = f.exact(DIM)
+    # -------- device loop (inputs resident; value, roofline)
+    integ = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=1234 + 7919 * rank, device=dev)
+    it, ncap = integ._struct()
+    it.stream_id = rank
+    stream = N.stream_ptr(dev)
+    params = N.dbl_array(f.params(DIM))
+    integ._put_sum_sigf()
+    l2_flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(itn, ev=None):
+        N.check(L.vg_allocate(ctypes.byref(it), stream))
+        if ev is not None:
+            ev[0].record()
+        N.check(L.vg_fused_iteration(ctypes.byref(it), itn, None, f.kind, params, 2, stream))
+        if ev is not None:
+            ev[1].record()
+        N.check(L.vg_end_iteration(ctypes.byref(it), stream))
+
+    itn = 1
+    for _ in range(args.warmup):
+        step(itn)
+        itn += 1
+    barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    neval_tot = 0
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    for k in range(args.steps):
+        l2_flush.fill_(float(k))          # evict L2 between timed iterations
+        e0, e1, e2, e3 = evs[k]
+        e0.record()
+        step(itn, (e1, e2))
+        e3.record()
+        itn += 1
+    barrier()
+    clk = clocks.stop()
+    step_ms = [evs[k][0].elapsed_time(evs[k][3]) for k in range(args.steps)]
+    kern_ms = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
+    st = integ._read_stats()
+    neval_step = int(st.neval)
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = world * neval_step * args.steps / t_total
+    # -------- roofline of the fused kernel: SFU-bound (one ex2 per Gaussian term)
+    kern_s = statistics.median(kern_ms) / 1e3
+    ex2_per_launch = neval_step * RIDGE_M
+    achieved = ex2_per_launch / kern_s / 1e9
+    peak = measure_ex2_peak(L, dev)
+    # -------- e2e through the public API
+    integ2 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=99 + rank, device=dev)
+    for _ in range(args.warmup):
+        integ2(f, nitn=1)
+    barrier()
+    t0 = time.perf_counter()
+    ne2 = 0
+    for _ in range(args.steps):
+        r = integ2(f, nitn=1)
+        ne2 += integ2.last_neval
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = world * ne2 / t_e2e
+    # -------- time to 1e-4 relative error (plain vegas+, public API, fresh map)
+    tta = None
+    if not args.no_tta:
+        integ3 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=4242 + rank, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r3 = integ3(f, nitn=200, rtol=1e-4)
+        torch.cuda.synchronize()
+        tta = {'seconds': time.perf_counter() - t0, 'iterations': r3.nitn,
+               'result': str(r3), 'rel_err': r3.sdev / abs(r3.mean),
+               'exact': exact, 'pull': (r3.mean - exact) / r3.sdev,
+               'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}
+    if world > 1:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    out = {
+        'metric': METRIC, 'value': value, 'unit': 'evals/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * t_total / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (sample/map/eval), f64 (sums)',
+        'data': 'synthetic (analytic integrand, Philox4x32-10 sampling)',
+        'config': {'workload': WORKLOAD, 'neval_per_step': neval_step, 'l2_flush': True,
+                   'parallelism': 'replicas' if world > 1 else 'single'},
+        'e2e': {'value': e2e, 'unit': 'evals/s', 'h2d_bytes_per_step': 16 + 80,
+                'd2h_bytes_per_step': 80},
+        'gpu_launches': 6 * args.steps,
+        'roofline': {'bound': 'sfu', 'achieved': achieved, 'peak': peak, 'unit': 'Gex2/s',
+                     'frac': achieved / peak, 'traffic': None,
+                     'kernel': 'tile_kernel<float, FUSED, RIDGE> (+finalize)',
+                     'algorithmic': '1 ex2 per Gaussian term: neval*M = %d per launch'
+                                    % ex2_per_launch},
+        'clocks': clk,
+        'time_to_1e-4': tta,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        out['cpu_baseline'] = cpu_baseline(iters=2)
+    print(json.dumps(out))
+
+
+def measure_ex2_peak(L, dev):
+    """MUFU ex2 throughput of this GPU (G ex2/s), measured by a probe kernel."""
+    import torch
+    from vegas_gb300 import _native as N
+    nthreads = 152 * 2048 * 4
+    iters = 4096
+    out = torch.empty(nthreads, dtype=torch.float32, device=dev)
+    s = N.stream_ptr(dev)
+    for _ in range(2):
+        N.check(L.vg_probe_mufu_ex2(N.ptr(out), nthreads, iters, s))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    N.check(L.vg_probe_mufu_ex2(N.ptr(out), nthreads, iters, s))
+    e1.record()
+    torch.cuda.synchronize()
+    return nthreads * iters * 8 / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline(iters=2, kind='port'):
+    """Oracle restatement of the reference on all host cores, same workload."""
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    cores = os.cpu_count() or 1
+    st = O.State(DIM * [[0, 1]], NEVAL)
+    t0 = time.perf_counter()
+    ne = 0
+    for k in range(iters):
+        out = st.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=5, itn=k + 1, nthreads=cores)
+        ne += out['neval']
+    dt = time.perf_counter() - t0
+    return {'value': ne / dt, 'unit': 'evals/s', 'cores': cores, 'kind': kind,
+            'sample': '%d full iterations of the workload (neval=1e6 each), FP64, %d threads'
+                      % (iters, cores)}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    cores = os.cpu_count() or 1
+    st = O.State(DIM * [[0, 1]], NEVAL)
+    itn = 1
+    for _ in range(args.warmup):
+        st.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=5, itn=itn, nthreads=cores)
+        itn += 1
+    t0 = time.perf_counter()
+    ne = 0
+    for _ in range(args.steps):
+        out = st.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=5, itn=itn, nthreads=cores)
+        ne += out['neval']
+        itn += 1
+    dt = time.perf_counter() - t0
+    v = ne / dt
+    print(json.dumps({
+        'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'evals/s', 'n_gpus': 0,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic', 'config': {'workload': WORKLOAD, 'neval_per_step': NEVAL},
+        'cpu_baseline': {'value': v, 'unit': 'evals/s', 'cores': cores, 'kind': 'port',
+                         'sample': 'each step one full iteration (neval=1e6), %d threads' % cores},
+        'e2e': {'value': v, 'unit': 'evals/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,205 @@
+/*
+ * vegas_gb300.h -- C ABI of the GB300 vegas+ hot path (libvegas_gb300.so).
+ *
+ * Conventions
+ *   - Every entry point returns an int status (VG_OK = 0).  On failure a
+ *     message is available from vg_last_error() (thread-local).
+ *   - Pointers documented "device" point to GPU memory owned by the caller;
+ *     the library never allocates device memory.  Scratch space is passed in
+ *     as a workspace whose size comes from vg_workspace_bytes().
+ *   - `stream` is a cudaStream_t passed as void*.  All device work is
+ *     enqueued on it; nothing synchronises except where stated.
+ *   - No torch types appear here: the Python package binds these symbols
+ *     with ctypes; other hosts (C, C++, Fortran via ISO_C_BINDING) can bind
+ *     them the same way.
+ *
+ * Each entry point names the reference code it replaces: src/vegas/_vegas.pyx
+ * of gplepage/vegas 6.4.1 ("pyx:line").
+ */
+#ifndef VEGAS_GB300_H
+#define VEGAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VG_MAX_DIM 64
+
+/* status codes; the Python layer maps them onto the reference's exceptions */
+#define VG_OK 0
+#define VG_ERR_VALUE 1       /* ValueError       (e.g. pyx:1319-1345)             */
+#define VG_ERR_MEMORY 2      /* MemoryError      (pyx:1355-1356, 1440-1441)       */
+#define VG_ERR_CUDA 3        /* CUDA runtime failure                                */
+#define VG_ERR_NAN 4         /* "integrand evaluates to nan" ValueError, pyx:2133  */
+#define VG_ERR_UNSUPPORTED 5 /* configuration outside what the kernels handle     */
+#define VG_ERR_TIMEOUT 6     /* a bounded device-side wait gave up                 */
+
+/* arithmetic of sampling / map / evaluation; sums are always FP64 */
+#define VG_F32 0
+#define VG_F64 1
+
+/* built-in integrands evaluated inside the fused kernel */
+#define VG_F_GAUSS 0   /* params {a, c, norm}: norm*exp(-a*sum_d (x_d-c)^2)                 */
+#define VG_F_RIDGE 1   /* params {M, s}: (1/M) sum_j N_dim(x; c_j(1..1), s), c_j=(j+.5)/M     */
+#define VG_F_LORENTZ 2 /* params {c[dim], w[dim]}: prod_d (w_d/pi)/((x_d-c_d)^2 + w_d^2)     */
+#define VG_F_MIXTURE 3 /* params {K, sigma, c[K*dim]}: (1/K) sum_k N_dim(x; c_k, sigma)      */
+#define VG_F_LATTICE 4 /* params {a, lambda}: exp(-sum_i (x_{i+1}-x_i)^2/2a + a(x_i^2/2+l x_i^4)) */
+#define VG_F_CONST 5   /* params {value}                                                     */
+
+/*
+ * Device-resident per-iteration scalars.  `sum_sigf` carries the vegas+
+ * stratification normaliser between iterations (Integrator.sum_sigf,
+ * pyx:2209-2215); the rest is written by each iteration.
+ */
+typedef struct vg_stats {
+    double sum_sigf;       /* in: used by the allocation; out: new value        */
+    double mean;           /* iteration estimate (component 0)                  */
+    double var;            /* its variance                                      */
+    double neval_sigf;     /* neval_frac*neval/sum_sigf used by the allocation  */
+    int64_t neval;         /* evaluations in the iteration (last_neval)         */
+    int64_t range_lo;      /* neval_hcube_range                                 */
+    int64_t range_hi;
+    int64_t ntiles;        /* tiles of the iteration                            */
+    int32_t nan_seen;      /* integrand returned NaN                            */
+    int32_t sigf_reset;    /* sum_sigf was 0: sigf set to 1 (pyx:2210-2215)     */
+    int32_t status;        /* device-side status (VG_ERR_*)                     */
+    int32_t pad;
+} vg_stats;
+
+/*
+ * One integrator (or one of many in a batch): geometry, adaptive map, vegas+
+ * stratification state, training histogram and scratch.  All pointers are
+ * device pointers except where noted.  Mirrors the state the reference keeps
+ * in Integrator/AdaptiveMap (pyx:834-1446, _vegas.pxd:21-70).
+ */
+typedef struct vg_integrator {
+    int32_t dim;
+    int32_t precision;             /* VG_F32 or VG_F64                          */
+    int64_t nhcube;                /* prod(nstrat)                              */
+    int64_t nstrat[VG_MAX_DIM];    /* host values                               */
+    int64_t ninc[VG_MAX_DIM];      /* host values                               */
+    double *grid;                  /* [dim, ldg] x-space nodes                  */
+    double *inc;                   /* [dim, ldi] increments                     */
+    int64_t ldg, ldi;
+    double *sigf;                  /* [nhcube] damped per-hypercube sdev        */
+    double *sum_f;                 /* [dim, ldi] training sums (fdv2)           */
+    uint64_t *n_f;                 /* [dim, ldi] training counts                */
+    vg_stats *stats;               /* device scalars                            */
+    void *work;                    /* workspace, vg_workspace_bytes() bytes     */
+    size_t work_bytes;
+    int64_t neval;
+    double neval_frac;
+    int64_t min_neval_hcube;
+    int64_t max_neval_hcube;
+    double alpha;
+    double beta;
+    int32_t adapt;                 /* Integrator.adapt                          */
+    int32_t adapt_to_errors;       /* must be 0 for now                         */
+    uint64_t seed;                 /* Philox key                                */
+    uint32_t stream_id;            /* Philox counter word: integral id          */
+    int32_t tile;                  /* samples per tile (0 = default)            */
+} vg_integrator;
+
+/* ---------------------------------------------------------------- library */
+const char *vg_last_error(void);
+int vg_version(void);
+/* sizeof(vg_integrator) for which=0, sizeof(vg_stats) for which=1 (binding check) */
+size_t vg_struct_size(int which);
+
+/* --------------------------------------------------------------- host-side */
+/*
+ * Stratification and grid sizes, Integrator.set pyx:1335-1407.
+ * mode 0: strata from neval (pyx:1346-1366); mode 1: explicit nstrat (sets
+ * *neval when neval_given==0, pyx:1335-1345); mode 2: keep nstrat_in.
+ * Returns VG_ERR_VALUE / VG_ERR_MEMORY as the reference raises.
+ */
+int vg_set_strata(int dim, int mode, int64_t *neval, int neval_given, const int64_t *nstrat_in,
+                  double neval_frac, double beta, int adapt_to_errors, int uniform_nstrat,
+                  double max_mem, int minimize_mem, int64_t maxinc_axis, int64_t *nstrat_out,
+                  int64_t *ninc_out, int64_t *min_neval_hcube_out);
+
+/* Upper bound on the evaluations of one iteration (capacity of x / f buffers). */
+int64_t vg_neval_cap(const vg_integrator *it);
+
+/* Workspace for an iteration of at most neval_cap evaluations (bytes);
+ * neval_cap <= 0 uses vg_neval_cap(it). */
+size_t vg_workspace_bytes(const vg_integrator *it, int64_t neval_cap);
+
+/* -------------------------------------------------------- AdaptiveMap ops */
+/* AdaptiveMap.make_uniform, pyx:205-241. xl/xu/ninc are host arrays. */
+int vg_make_uniform(int dim, const int64_t *ninc, const double *xl, const double *xu,
+                    double *grid, int64_t ldg, double *inc, int64_t ldi, void *stream);
+
+/*
+ * AdaptiveMap.adapt, pyx:467-594 (smoothing, damping, regrid to new_ninc).
+ * old_ninc/new_ninc are host arrays; sum_f/n_f may be NULL (no training
+ * data).  The new grid must not alias the old one.
+ */
+int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
+             const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
+             const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
+             int64_t ldg_new, int64_t ldi_new, void *stream);
+
+/* AdaptiveMap.map, pyx:310-360: y[n,dim] -> x[n,dim], jac[n] (dtype VG_F32/VG_F64). */
+int vg_map(int dim, const int64_t *ninc, const double *grid, const double *inc, int64_t ldg,
+           int64_t ldi, int64_t n, const void *y, void *x, void *jac, int dtype, void *stream);
+
+/* AdaptiveMap.add_training_data, pyx:421-464 (accumulates into sum_f / n_f). */
+int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, int64_t n, const void *y,
+                         const void *f, int dtype, double *sum_f, uint64_t *n_f, void *stream);
+
+/* ------------------------------------------------------ Integrator ops */
+/*
+ * Allocation of evaluations to hypercubes, Integrator._random_batch
+ * pyx:1692-1710 (whole iteration at once): per-hypercube counts from sigf,
+ * offsets, neval_hcube_range and the tile schedule.  Writes it->stats.
+ */
+int vg_allocate(const vg_integrator *it, void *stream);
+
+/*
+ * Integration points of the current allocation, pyx:1731-1752: x[n,dim]
+ * (precision dtype), optional y[n,dim], wgt[n] (FP64) and hcube[n].  u is an
+ * optional injected [n,dim] FP64 array of uniforms (ran_array_generator,
+ * pyx:1676-1680); NULL draws Philox4x32-10 keyed by (seed, itn, sample).
+ * n_cap is the capacity of the output arrays (>= stats->neval).
+ */
+int vg_sample(const vg_integrator *it, uint32_t itn, const double *u, void *x, void *y,
+              double *wgt, int64_t *hcube, int64_t n_cap, void *stream);
+
+/*
+ * Per-hypercube two-pass reduction of the integrand values f[n] (dtype),
+ * pyx:2136-2193, with the training histogram (pyx:2173, 2196-2197), the new
+ * sigf and the iteration mean/var/sum_sigf (written to it->stats).
+ */
+int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u, const void *f, int f_dtype,
+              void *stream);
+
+/*
+ * Fused iteration for a built-in integrand: sampling, map, evaluation,
+ * reduction and training histogram in one persistent kernel (the whole
+ * body of Integrator.__call__'s batch loop, pyx:2096-2197).  params are host
+ * doubles.  Call vg_allocate first.
+ */
+int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, int kind,
+                       const double *params, int nparams, void *stream);
+
+/*
+ * End of iteration, pyx:2209-2217: adapt the map from the training
+ * histogram (when alpha > 0 and adapt) and clear the histogram.  Uses the
+ * workspace for the new grid.
+ */
+int vg_end_iteration(const vg_integrator *it, void *stream);
+
+/* ------------------------------------------------------------- probes */
+/* Throughput probes used for roofline denominators (see bench.py). */
+int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);
+int vg_probe_fp64_fma(double *out, int64_t nthreads, int iters, void *stream);
+int vg_probe_fp32_fma(float *out, int64_t nthreads, int iters, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VEGAS_GB300_H */

@@ -1,0 +1,234 @@
+"""GPU parity tests: CUDA kernels (through the C ABI) against the oracle and
+the reference's golden traces.
+
+Tolerances (FP64 paths): points (y, hypercube ids, allocation) bit-exact;
+x, weights <= 1e-15 relative; per-iteration mean / sdev, sigf, sum_sigf,
+training histogram and adapted grid <= 1e-12 relative.  FP32 paths: final
+integrals within 3 combined standard deviations of the exact value.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import vegas_gb300 as vg
+from vegas_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+RTOL = 1e-12
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name)))
+
+
+def rel(a, b):
+    a = np.asarray(a, float)
+    b = np.asarray(b, float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))) if a.size else 0.0
+
+
+def set_state(I, grid, sigf, sum_sigf):
+    g = torch.from_numpy(np.nan_to_num(grid)).to(I.device)
+    I.map._grid.copy_(g)
+    I.map._inc.copy_(torch.diff(g, dim=1))
+    I._sigf.copy_(torch.from_numpy(np.asarray(sigf, float)).to(I.device))
+    I.sum_sigf = float(sum_sigf)
+
+
+def replay_on_gpu(tr, alpha=0.5, beta=0.75):
+    dim = len(tr['nstrat'])
+    I = vg.Integrator(dim * [[0, 1]], neval=int(tr['neval']), precision='fp64', seed=1,
+                      alpha=alpha, beta=beta)
+    assert list(I.nstrat) == list(tr['nstrat'])
+    assert list(I.map.ninc) == list(tr['ninc'])
+    assert I.min_neval_hcube == int(tr['min_neval_hcube'])
+    H = I.nhcube
+    grid = tr['grid_init']
+    sigf = tr['sigf_init'] if len(tr['sigf_init']) else np.ones(H)
+    sum_sigf = float(tr['sum_sigf_init'])
+    L = N.load()
+    stream = N.stream_ptr(I.device)
+    for k in range(int(tr['nitn'])):
+        set_state(I, grid, sigf, sum_sigf)
+        it, ncap = I._struct()
+        I._allocate(it)
+        st = I._read_stats()
+        assert st.neval == int(tr['last_neval%d' % k])
+        assert [st.range_lo, st.range_hi] == list(tr['range%d' % k])
+        # allocation: bit-exact against the oracle from the same sigf
+        nsf = float(tr['neval_frac']) * int(tr['neval']) / sum_sigf if sum_sigf > 0 else 0.0
+        nh_o, _, _ = O.alloc(sigf, nsf, beta > 0 and H > 1, I.min_neval_hcube,
+                             I.max_neval_hcube, int(int(tr['neval']) / H))
+        assert np.array_equal(I._neval_h_host(), nh_o)
+        # points with the reference's injected uniforms
+        u_np = tr['u%d' % k].astype(np.float64) * 2.0 ** -24
+        u = torch.from_numpy(u_np).to(I.device)
+        x, y, w, hc = I._points(it, ncap, 1, u, want_y=True, want_hc=True)
+        n = st.neval
+        g0 = np.nan_to_num(grid)
+        yo, xo, wo, hco = O.points(tr['nstrat'], g0, np.diff(g0, axis=1), tr['ninc'], nh_o, u=u_np)
+        assert np.array_equal(y[:n].cpu().numpy(), yo)
+        assert np.array_equal(hc[:n].cpu().numpy(), hco)
+        assert rel(x[:n].cpu().numpy(), xo) <= 1e-15
+        assert rel(w[:n].cpu().numpy(), wo) <= 1e-15
+        # reduction of the reference's own integrand values
+        f = torch.zeros(ncap, dtype=torch.float64, device=I.device)
+        f[:n] = torch.from_numpy(tr['f%d' % k]).to(I.device)
+        I.map.sum_f.zero_()
+        I.map.n_f.zero_()
+        N.check(L.vg_reduce(ctypes.byref(it), 1, N.ptr(u), N.ptr(f), N.VG_F64, stream))
+        st = I._read_stats()
+        assert st.status == 0 and not st.nan_seen
+        assert rel(st.mean, tr['mean%d' % k]) <= RTOL
+        assert rel(st.var ** 0.5, tr['sdev%d' % k]) <= RTOL
+        new_sigf = I.sigf
+        assert rel(new_sigf, tr['sigf%d' % k]) <= RTOL
+        assert rel(st.sum_sigf, tr['sum_sigf%d' % k]) <= RTOL
+        # training histogram against the oracle on the same fdv2
+        _, _, _, _, fdv2 = O.reduce(nh_o, wo, tr['f%d' % k], beta=beta, sigf=sigf)
+        sf_o, nf_o = O.add_training_data(tr['ninc'], I.map.inc_tensor.shape[1], yo, fdv2)
+        sf = I.map.sum_f.cpu().numpy()
+        nf = I.map.n_f.cpu().numpy()
+        assert np.array_equal(nf.astype(float) + O.TINY, nf_o)
+        assert rel(sf[sf_o > 0], sf_o[sf_o > 0]) <= RTOL
+        # adapt on the device
+        N.check(L.vg_end_iteration(ctypes.byref(it), stream))
+        gnew = I.map.grid
+        want = tr['grid%d' % k]
+        ok = ~np.isnan(want)
+        assert np.max(np.abs(gnew[ok] - want[ok])) <= RTOL * np.max(np.abs(want[ok]))
+        grid, sigf, sum_sigf = want, tr['sigf%d' % k], float(tr['sum_sigf%d' % k])
+
+
+def test_replay_gauss4_reference_trace():
+    replay_on_gpu(load('ref_gauss4_injected.npz'))
+
+
+def test_replay_ridge_reference_trace():
+    replay_on_gpu(load('ref_ridge_injected.npz'))
+
+
+def test_map_kernel_edges_golden():
+    c = load('ref_map_adapt.npz')
+    g = np.nan_to_num(c['map_grid'])
+    m = vg.AdaptiveMap([list(g[d, :c['map_ninc'][d] + 1]) for d in range(2)])
+    y = torch.from_numpy(c['map_y']).cuda()
+    x = torch.empty_like(y)
+    jac = torch.empty(y.shape[0], dtype=torch.float64, device='cuda')
+    m.map(y, x, jac)
+    assert np.array_equal(x.cpu().numpy(), c['map_x'])
+    assert np.array_equal(jac.cpu().numpy(), c['map_jac'])
+
+
+def test_adapt_kernel_golden():
+    c = load('ref_map_adapt.npz')
+    for k in range(int(c['n_adapt'])):
+        p = 'adapt%d_' % k
+        ninc = c[p + 'ninc_in']
+        g = np.nan_to_num(c[p + 'grid_in'])
+        m = vg.AdaptiveMap([list(g[d, :ninc[d] + 1]) for d in range(len(ninc))])
+        if bool(c[p + 'train']):
+            m.add_training_data(c[p + 'y'], c[p + 'f'])
+            sf, nf = m.training_data()
+            assert rel(sf[c[p + 'sum_f'] > 0], c[p + 'sum_f'][c[p + 'sum_f'] > 0]) <= RTOL
+            assert np.array_equal(nf, c[p + 'n_f'])
+        m.adapt(alpha=float(c[p + 'alpha']), ninc=c[p + 'new_ninc'])
+        want = c[p + 'grid_out']
+        ok = ~np.isnan(want)
+        got = m.grid
+        assert np.max(np.abs(got[ok] - want[ok])) <= RTOL * np.max(np.abs(want[ok])), k
+
+
+def test_fused_fp64_matches_oracle_philox():
+    """Fused FP64 iterations (Philox draws) == oracle on the same draws."""
+    for kind_cls, params in ((vg.Gaussian(a=100.0, c=0.5, dim=4), None),
+                             (vg.Ridge(M=50, s=0.05), None)):
+        seed = 99
+        I = vg.Integrator(4 * [[0, 1]], neval=6000, precision='fp64', seed=seed)
+        st = O.State(4 * [[0, 1]], 6000)
+        for itn in range(1, 4):
+            r = I(kind_cls, nitn=1)
+            out = st.iterate(kind_cls.kind, kind_cls.params(4), seed=seed, stream=0, itn=itn)
+            assert I.last_neval == out['neval']
+            assert rel(r.itn_results[0].mean, out['mean']) <= RTOL
+            assert rel(r.itn_results[0].var, out['var']) <= 1e-10
+            assert rel(I.sigf, st.sigf) <= 1e-10
+            g = I.map.grid
+            for d in range(4):
+                K = st.ninc[d]
+                assert np.max(np.abs(g[d, :K + 1] - st.grid[d, :K + 1])) <= 1e-12
+
+
+def test_dropin_matches_fused_fp64():
+    """lbatch torch integrand path == fused built-in path (same draws)."""
+    f = vg.Ridge(M=40, s=0.05)
+    I1 = vg.Integrator(4 * [[0, 1]], neval=5000, precision='fp64', seed=7)
+    I2 = vg.Integrator(4 * [[0, 1]], neval=5000, precision='fp64', seed=7)
+
+    @vg.lbatchintegrand
+    def g(x):
+        return f(x)
+
+    r1 = I1(f, nitn=3)
+    r2 = I2(g, nitn=3)
+    for a, b in zip(r1.itn_results, r2.itn_results):
+        assert rel(a.mean, b.mean) <= 1e-10
+        assert rel(a.var, b.var) <= 1e-8
+
+
+def test_fp32_gauss_config1_statistics():
+    f = vg.Gaussian(a=100.0, c=0.5, dim=4)
+    I = vg.Integrator(4 * [[0, 1]], seed=2024)
+    I(f, nitn=10, neval=1e4, alpha=0.5, beta=0.75)
+    r = I(f, nitn=10, neval=1e4)
+    exact = f.exact(4)
+    assert abs(r.mean - exact) < 3 * r.sdev, (r, exact)
+    assert r.sdev / exact < 5e-3
+
+
+def test_fp32_ridge_config2_statistics():
+    f = vg.Ridge(M=1000, s=0.01)
+    I = vg.Integrator(4 * [[0, 1]], seed=77)
+    I(f, nitn=10, neval=1e6)
+    r = I(f, nitn=10, neval=1e6)
+    exact = f.exact(4)
+    assert abs(r.mean - exact) < 3 * r.sdev, (r, exact)
+    assert r.dof == 9
+
+
+def test_nan_integrand_raises():
+    @vg.lbatchintegrand
+    def bad(x):
+        out = torch.ones(x.shape[0], dtype=x.dtype, device=x.device)
+        out[0] = float('nan')
+        return out
+
+    I = vg.Integrator(2 * [[0, 1]], seed=1)
+    with pytest.raises(ValueError):
+        I(bad, nitn=1, neval=1000)
+
+
+def test_integrand_exception_propagates():
+    @vg.lbatchintegrand
+    def bad(x):
+        return 1 / 0.
+
+    I = vg.Integrator(2 * [[0, 1]], seed=1)
+    with pytest.raises(ZeroDivisionError):
+        I(bad, nitn=1, neval=100)
+
+
+def test_constant_integrand_epsilon_guard():
+    # test_vegas.py:1272-1296: sdev ratios exactly 1 and 2 from the EPSILON guard
+    I = vg.Integrator([(0, 1)], neval=100, alpha=0, seed=3, precision='fp64')
+    res = I(vg.Constant(7.0), nitn=4)
+    np.testing.assert_almost_equal(res.itn_results[0].sdev / res.itn_results[1].sdev, 1.0, 7)
+    np.testing.assert_almost_equal(res.itn_results[0].sdev / res.sdev, 2.0, 7)
+    np.testing.assert_almost_equal(res.mean, 7.0, 7)
+    res = I(vg.Constant(0.0), nitn=4)
+    assert res.mean == 0.0

@@ -1,0 +1,156 @@
+// vg_common.cuh -- device helpers shared by the vegas+ kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vg_internal.h"
+
+#define VG_TINY 1e-257                       // _vegas.pyx:34
+#define VG_EPSILON (2.220446049250313e-16 * 1e4)  // _vegas.pyx:36
+
+// ---------------------------------------------------------------- Philox
+// Philox4x32-10 (Salmon et al., SC'11).  Counter layout shared with the
+// oracle: (sample_lo, sample_hi, iteration, stream<<8 | group).
+struct VgU4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ VgU4 vg_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                          uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return VgU4{c0, c1, c2, c3};
+}
+
+// Uniforms for sample i, axes [0, dim): FP64 (53 bits, two words per axis,
+// group d>>1 | 0x80) and FP32 (24 bits, one word per axis, group d>>2).
+template <typename T>
+struct VgUniform;
+
+template <>
+struct VgUniform<double> {
+    static __device__ __forceinline__ void draw(uint64_t seed, uint32_t stream, uint32_t itn,
+                                                uint64_t i, int dim, double *u)
+    {
+        for (int g = 0; 2 * g < dim; g++) {
+            VgU4 r = vg_philox((uint32_t)i, (uint32_t)(i >> 32), itn,
+                               (stream << 8) | 0x80u | (uint32_t)g, (uint32_t)seed,
+                               (uint32_t)(seed >> 32));
+            uint64_t m0 = ((uint64_t)r.x << 21) | (uint64_t)(r.y >> 11);
+            u[2 * g] = (double)m0 * (1.0 / 9007199254740992.0);
+            if (2 * g + 1 < dim) {
+                uint64_t m1 = ((uint64_t)r.z << 21) | (uint64_t)(r.w >> 11);
+                u[2 * g + 1] = (double)m1 * (1.0 / 9007199254740992.0);
+            }
+        }
+    }
+};
+
+template <>
+struct VgUniform<float> {
+    static __device__ __forceinline__ void draw(uint64_t seed, uint32_t stream, uint32_t itn,
+                                                uint64_t i, int dim, float *u)
+    {
+        for (int g = 0; 4 * g < dim; g++) {
+            VgU4 r = vg_philox((uint32_t)i, (uint32_t)(i >> 32), itn, (stream << 8) | (uint32_t)g,
+                               (uint32_t)seed, (uint32_t)(seed >> 32));
+            const float s = 1.0f / 16777216.0f;
+            u[4 * g] = (float)(r.x >> 8) * s;
+            if (4 * g + 1 < dim) u[4 * g + 1] = (float)(r.y >> 8) * s;
+            if (4 * g + 2 < dim) u[4 * g + 2] = (float)(r.z >> 8) * s;
+            if (4 * g + 3 < dim) u[4 * g + 3] = (float)(r.w >> 8) * s;
+        }
+    }
+};
+
+// ------------------------------------------------------- compensated sum
+// Neumaier summation in FP64 for the per-iteration totals.
+struct VgKSum {
+    double s, c;
+    __device__ __forceinline__ void add(double v)
+    {
+        double t = s + v;
+        if (fabs(s) >= fabs(v)) c += (s - t) + v;
+        else c += (v - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ void merge(const VgKSum &o)
+    {
+        add(o.s);
+        c += o.c;
+    }
+    __device__ __forceinline__ double value() const { return s + c; }
+};
+
+__device__ __forceinline__ VgKSum vg_ksum_shfl_down(VgKSum v, int off)
+{
+    VgKSum o;
+    o.s = __shfl_down_sync(0xffffffffu, v.s, off);
+    o.c = __shfl_down_sync(0xffffffffu, v.c, off);
+    return o;
+}
+
+// Fixed-order block reduction of a compensated sum (deterministic).  All
+// threads of the block must call it; result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ VgKSum vg_block_ksum(VgKSum v, VgKSum *smem /* NT/32 */)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        VgKSum o = vg_ksum_shfl_down(v, off);
+        v.merge(o);
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) smem[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < NT / 32) ? smem[lane] : VgKSum{0.0, 0.0};
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            VgKSum o = vg_ksum_shfl_down(v, off);
+            v.merge(o);
+        }
+    }
+    __syncthreads();
+    return v;
+}
+
+#define VG_CUDA_CHECK(expr)                                                                  \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return vg_fail(VG_ERR_CUDA, "%s: %s (%s:%d)", #expr, cudaGetErrorString(_e),    \
+                           __FILE__, __LINE__);                                              \
+    } while (0)
+
+#define VG_LAUNCH_CHECK()                                                                    \
+    do {                                                                                     \
+        cudaError_t _e = cudaGetLastError();                                                 \
+        if (_e != cudaSuccess)                                                               \
+            return vg_fail(VG_ERR_CUDA, "kernel launch: %s (%s:%d)", cudaGetErrorString(_e), \
+                           __FILE__, __LINE__);                                              \
+    } while (0)
+
+static inline int vg_num_sms()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}

@@ -1,0 +1,578 @@
+"""vegas+ Integrator on the GPU.
+
+Python face of the reference's ``vegas.Integrator`` (src/vegas/_vegas.pyx:
+834-2230): the same constructor, ``defaults``, ``set`` semantics, ``__call__``
+(fcn, save, saveall, **kargs), ``random_batch``/``random``/``sample``,
+``settings`` and pickling.  Everything numeric runs in libvegas_gb300.so:
+
+* built-in integrands (vegas_gb300.integrands) run fused: one allocation and
+  one persistent kernel per iteration, no host round trip except reading the
+  80-byte iteration record;
+* lbatch integrands receive CUDA tensors ``x[n, dim]`` (FP32 by default, FP64
+  with ``precision='fp64'``) in batches of ``min_neval_batch`` points and
+  return ``f[n]``; the reduction then runs on the device.
+
+Extra settings beyond the reference's: ``precision`` ('fp32' | 'fp64'),
+``seed`` (Philox key), ``device``.
+"""
+import ctypes
+import math
+import os
+import pickle
+import sys
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import _gvar as gv
+from .adaptive_map import AdaptiveMap, _device
+from .integrands import BuiltinIntegrand
+from .ravg import RAvg, RAvgArray
+
+HUGE = 10 ** (sys.float_info.max_10_exp - 50)  # _vegas.pyx:35
+
+# attribute types of the reference's typed Integrator fields (_vegas.pxd:35-62)
+_INT = ('neval', 'min_neval_batch', 'maxinc_axis', 'max_neval_hcube', 'nitn', 'nproc')
+_FLOAT = ('neval_frac', 'max_mem', 'alpha', 'rtol', 'atol', 'beta')
+_BOOL = ('gpu_pad', 'adapt', 'correlate_integrals', 'minimize_mem', 'adapt_to_errors',
+         'sync_ran', 'mpi', 'uniform_nstrat', 'uses_jac')
+
+
+class Integrator(object):
+    r"""Adaptive multidimensional Monte Carlo integration (vegas+), on a GPU.
+
+    ``Integrator(map, **kargs)`` where ``map`` is a list of ``[xl, xu]``
+    limits, an :class:`AdaptiveMap` or another Integrator (whose map, sigf
+    and strata are copied, pyx:1149-1162).
+    """
+
+    defaults = dict(
+        map=None,
+        neval=1000,
+        maxinc_axis=1000,
+        min_neval_batch=100000,
+        max_neval_hcube=50000,
+        gpu_pad=False,
+        neval_frac=0.75,
+        max_mem=1e9,
+        nitn=10,
+        alpha=0.5,
+        beta=0.75,
+        adapt=True,
+        correlate_integrals=True,
+        minimize_mem=False,
+        adapt_to_errors=False,
+        uniform_nstrat=False,
+        rtol=0,
+        atol=0,
+        analyzer=None,
+        ran_array_generator=None,
+        sync_ran=True,
+        mpi=False,
+        uses_jac=False,
+        nproc=1,
+        precision='fp32',
+        seed=None,
+    )
+
+    def __init__(self, map, **kargs):
+        self.neval_hcube_range = None
+        self.last_neval = 0
+        self._itn = 0
+        self._work = None
+        self._stats = None
+        self._sigf = None
+        self.sum_sigf = HUGE
+        self.nhcube = 1
+        self.min_neval_hcube = 2
+        self.device = _device(kargs.pop('device', None))
+        for k, v in Integrator.defaults.items():
+            if k != 'map':
+                setattr(self, k, v)
+        if isinstance(map, Integrator):
+            self._set_map(map)
+            args = {k: getattr(map, k) for k in Integrator.defaults if k != 'map'}
+            self._sigf = map._sigf.clone() if map._sigf is not None else None
+            self.sum_sigf = float(self._sigf.sum()) if self._sigf is not None else HUGE
+            self.nstrat = np.array(map.nstrat)
+            if 'nstrat' not in kargs:
+                kargs['nstrat'] = map.nstrat
+                if 'neval' not in kargs:
+                    kargs['neval'] = map.neval
+        else:
+            args = {k: v for k, v in Integrator.defaults.items() if k != 'map'}
+            self._set_map(map)
+            self.nstrat = np.zeros(self.map.dim, np.int64)
+        args.update(kargs)
+        if 'nstrat' in kargs and 'neval' not in kargs and 'neval' in args:
+            del args['neval']
+        if 'neval' in kargs and 'nstrat' not in kargs and 'nstrat' in args:
+            del args['nstrat']
+        if args.get('seed') is None:
+            args['seed'] = int.from_bytes(os.urandom(8), 'little') >> 1
+        self.set(args)
+
+    # ---------------------------------------------------------------- state
+    def _set_map(self, map):
+        if isinstance(map, AdaptiveMap):
+            self.map = AdaptiveMap(map, device=self.device)
+        elif isinstance(map, Integrator):
+            self.map = AdaptiveMap(map.map, device=self.device)
+        else:
+            if hasattr(map, 'keys'):
+                raise NotImplementedError('dictionary integration regions are not supported yet')
+            lim = np.array(map, dtype=float)
+            if lim.ndim < 2 or lim.shape[-1] != 2:
+                raise ValueError('integration limits must be [[xl, xu], ...]')
+            self.map = AdaptiveMap(lim.reshape(-1, 2), device=self.device)
+        self.xsample = np.array([0.5 * (a + b) for a, b in self.map.region()])
+
+    @property
+    def dim(self):
+        return self.map.dim
+
+    @property
+    def sigf(self):
+        return np.zeros(0) if self._sigf is None else self._sigf.cpu().numpy()
+
+    def __reduce__(self):
+        odict = {k: getattr(self, k) for k in Integrator.defaults if k != 'map'}
+        odict['nstrat'] = np.asarray(self.nstrat)
+        odict['sigf'] = self.sigf
+        return (Integrator, (self.map,), odict)
+
+    def __setstate__(self, odict):
+        self.set(odict)
+
+    def set(self, ka={}, **kargs):
+        """Reset parameters; returns the old values (pyx:1256-1446)."""
+        if kargs:
+            kargs.update(ka)
+        else:
+            kargs = dict(ka)
+        old_val = dict()
+        nstrat = None
+        for k in kargs:
+            if k == 'map':
+                old_val['map'] = self.map
+                self._set_map(kargs['map'])
+            elif k == 'nstrat':
+                if kargs['nstrat'] is None:
+                    continue
+                old_val['nstrat'] = self.nstrat
+                nstrat = np.array(kargs['nstrat'], dtype=np.int64)
+            elif k == 'sigf':
+                old_val['sigf'] = self.sigf
+                s = np.fabs(np.asarray(kargs['sigf'], float))
+                self._sigf = torch.from_numpy(s.copy()).to(self.device)
+                self.sum_sigf = float(np.sum(s))
+            elif k in Integrator.defaults:
+                old_val[k] = getattr(self, k, None)
+                v = kargs[k]
+                if k in _INT and v is not None:
+                    v = int(v)
+                elif k in _FLOAT and v is not None:
+                    v = float(v)
+                elif k in _BOOL and v is not None:
+                    v = bool(v)
+                setattr(self, k, v)
+            elif k not in ['nhcube_batch', 'max_nhcube']:
+                raise AttributeError('no parameter named "%s"' % str(k))
+        if self.precision not in ('fp32', 'fp64'):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        if self.adapt_to_errors:
+            raise NotImplementedError('adapt_to_errors=True is not supported yet')
+        # sanity checks (pyx:1319-1330)
+        if nstrat is not None:
+            if len(nstrat) != self.map.dim:
+                raise ValueError('nstrat[d] has wrong length: %d not %d' % (len(nstrat), self.map.dim))
+            if np.any(nstrat < 1):
+                raise ValueError('bad nstrat: ' + str(nstrat))
+        if self.neval_frac < 0 or self.neval_frac >= 1:
+            raise ValueError('neval_frac = {} but require 0 <= neval_frac < 1'.format(self.neval_frac))
+        if 'neval' in old_val and self.neval < 2:
+            raise ValueError('neval>2 required, not ' + str(self.neval))
+        dim = self.map.dim
+        # strata and increments (pyx:1333-1407), host logic in the C ABI
+        if nstrat is not None:
+            mode = 1
+        elif 'neval' in old_val or 'neval_frac' in old_val:
+            mode = 0
+        else:
+            mode = 2
+        nstrat_in = nstrat if nstrat is not None else np.asarray(self.nstrat, np.int64)
+        sz = strata(dim, mode, self.neval, 'neval' in old_val, nstrat_in, self.neval_frac,
+                    self.beta, self.adapt_to_errors, self.uniform_nstrat, self.max_mem,
+                    self.minimize_mem, self.maxinc_axis)
+        if mode == 1 and 'neval' not in old_val:
+            old_val['neval'] = self.neval
+        self.neval = sz['neval']
+        nstrat = sz['nstrat']
+        ninc = sz['ninc']
+        mnh = sz['min_neval_hcube']
+        if not np.array_equal(self.map.ninc, ninc):
+            self.map.adapt(ninc=ninc)
+        if not np.array_equal(np.asarray(self.nstrat), nstrat):
+            if 'sigf' not in old_val:
+                old_val['sigf'] = self.sigf
+                self._sigf = None
+                self.sum_sigf = HUGE
+            self.nstrat = nstrat
+        self.nhcube = int(np.prod(self.nstrat))
+        self.min_neval_hcube = int(mnh)
+        if self.beta >= 0 and self.nhcube > 1 and (self._sigf is None or
+                                                   self._sigf.numel() != self.nhcube):
+            self._sigf = torch.ones(self.nhcube, dtype=torch.float64, device=self.device)
+            self.sum_sigf = float(self.nhcube)
+        if self._sigf is None:
+            self._sigf = torch.ones(max(self.nhcube, 1), dtype=torch.float64, device=self.device)
+        workspace = self.min_neval_batch + self.max_neval_hcube
+        if workspace > self.neval:
+            workspace = self.neval + 1
+        if (3 * dim + 3) * workspace + (0 if self.minimize_mem else self.nhcube) > self.max_mem:
+            raise MemoryError('work arrays larger than max_mem; reduce min_neval_batch or '
+                              'max_neval_hcube (or increase max_mem)')
+        self._work = None   # re-derive device workspace lazily
+        return old_val
+
+    # ----------------------------------------------------- device plumbing
+    def _struct(self):
+        it = N.VgIntegrator()
+        it.dim = self.dim
+        it.precision = N.VG_F64 if self.precision == 'fp64' else N.VG_F32
+        it.nhcube = self.nhcube
+        for d in range(self.dim):
+            it.nstrat[d] = int(self.nstrat[d])
+            it.ninc[d] = int(self.map._ninc[d])
+        g, inc = self.map.grid_tensor, self.map.inc_tensor
+        it.grid = g.data_ptr()
+        it.inc = inc.data_ptr()
+        it.ldg = g.shape[1]
+        it.ldi = inc.shape[1]
+        it.sigf = self._sigf.data_ptr()
+        it.neval = self.neval
+        it.neval_frac = self.neval_frac
+        it.min_neval_hcube = self.min_neval_hcube
+        it.max_neval_hcube = self.max_neval_hcube
+        it.alpha = self.alpha
+        it.beta = self.beta
+        it.adapt = int(self.adapt)
+        it.adapt_to_errors = int(self.adapt_to_errors)
+        it.seed = int(self.seed) & ((1 << 64) - 1)
+        it.stream_id = 0
+        it.tile = 0
+        L = N.load()
+        ncap = L.vg_neval_cap(ctypes.byref(it))
+        need = L.vg_workspace_bytes(ctypes.byref(it), 0)
+        if self._work is None or self._work.numel() < need:
+            self._work = torch.empty(need, dtype=torch.uint8, device=self.device)
+        if self._stats is None:
+            self._stats = torch.zeros(ctypes.sizeof(N.VgStats), dtype=torch.uint8, device=self.device)
+        if self.map.sum_f is None or self.map.sum_f.shape != inc.shape:
+            self.map.sum_f = torch.zeros(inc.shape, dtype=torch.float64, device=self.device)
+            self.map.n_f = torch.zeros(inc.shape, dtype=torch.int64, device=self.device)
+        it.sum_f = self.map.sum_f.data_ptr()
+        it.n_f = self.map.n_f.data_ptr()
+        it.stats = self._stats.data_ptr()
+        it.work = self._work.data_ptr()
+        it.work_bytes = self._work.numel()
+        return it, int(ncap)
+
+    def _put_sum_sigf(self):
+        st = N.VgStats()
+        st.sum_sigf = self.sum_sigf
+        self._stats.copy_(torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8))
+
+    def _read_stats(self):
+        b = self._stats.cpu().numpy().tobytes()
+        return N.VgStats.from_buffer_copy(b)
+
+    def _allocate(self, it):
+        self._put_sum_sigf()
+        L = N.load()
+        N.check(L.vg_allocate(ctypes.byref(it), N.stream_ptr(self.device)))
+
+    # ------------------------------------------------------------- sampling
+    def _points(self, it, ncap, itn, u, want_y=False, want_hc=False):
+        L = N.load()
+        dt = torch.float64 if self.precision == 'fp64' else torch.float32
+        x = torch.empty((ncap, self.dim), dtype=dt, device=self.device)
+        y = torch.empty((ncap, self.dim), dtype=dt, device=self.device) if want_y else None
+        w = torch.empty(ncap, dtype=torch.float64, device=self.device)
+        hc = torch.empty(ncap, dtype=torch.int64, device=self.device) if want_hc else None
+        N.check(L.vg_sample(ctypes.byref(it), itn, N.ptr(u), N.ptr(x), N.ptr(y), N.ptr(w),
+                            N.ptr(hc), ncap, N.stream_ptr(self.device)))
+        return x, y, w, hc
+
+    def _draw_u(self, n):
+        """Injected uniforms [n, dim] (FP64, device) from ran_array_generator,
+        requested in the reference's batch sizes (pyx:1692-1732)."""
+        gen = self.ran_array_generator
+        parts = []
+        nh = self._neval_h_host()
+        csum = np.cumsum(nh)
+        start, base = 0, 0
+        H = len(nh)
+        while start < H:
+            # first hypercube where the batch reaches min_neval_batch
+            target = base + self.min_neval_batch
+            end = int(np.searchsorted(csum, target, side='left'))
+            end = min(end, H - 1)
+            nb = int(csum[end] - base)
+            parts.append(np.asarray(gen((nb, self.dim)), dtype=np.float64).reshape(nb, self.dim))
+            base = int(csum[end])
+            start = end + 1
+        u = np.concatenate(parts, axis=0)
+        assert u.shape[0] == n
+        return torch.from_numpy(np.ascontiguousarray(u)).to(self.device)
+
+    def _neval_h_host(self):
+        # neval_h lives at the start of the workspace (int32 per hypercube)
+        return self._work[:4 * self.nhcube].view(torch.int32).cpu().numpy().astype(np.int64)
+
+    def random_batch(self, yield_hcube=False, yield_y=False):
+        """Batches of integration points and weights of one iteration
+        (pyx:1601-1634): yields (x, [y,] wgt, [hcube]) as CUDA tensors."""
+        it, ncap = self._struct()
+        self._allocate(it)
+        st = self._read_stats()
+        n = int(st.neval)
+        self.last_neval = n
+        self.neval_hcube_range = np.array([st.range_lo, st.range_hi])
+        u = self._draw_u(n) if self.ran_array_generator is not None else None
+        self._itn += 1
+        x, y, w, hc = self._points(it, ncap, self._itn & 0xffffffff, u, yield_y, yield_hcube)
+        nb = max(1, int(self.min_neval_batch))
+        for lo in range(0, n, nb):
+            hi = min(n, lo + nb)
+            ans = (x[lo:hi],)
+            if yield_y:
+                ans += (y[lo:hi],)
+            ans += (w[lo:hi],)
+            if yield_hcube:
+                ans += (hc[lo:hi],)
+            yield ans
+
+    random_vec = random_batch
+
+    def random(self, yield_hcube=False, yield_y=False):
+        """Point-by-point version of random_batch (pyx:1770-1814)."""
+        for b in self.random_batch(yield_hcube=yield_hcube, yield_y=yield_y):
+            for i in range(b[0].shape[0]):
+                yield tuple(t[i] for t in b)
+
+    def sample(self, nbatch=None, mode='rbatch'):
+        """Random sample (wgt, x) with sum(wgt*f(x)) estimating the integral (pyx:1816-1863)."""
+        neval = self.last_neval if self.last_neval > 0 else self.neval
+        nbatch = neval if nbatch is None else int(nbatch)
+        nit = nbatch // neval
+        if nit * neval < nbatch:
+            nit += 1
+        xs, ws = [], []
+        for _ in range(nit):
+            for x, w in self.random_batch():
+                xs.append(x)
+                ws.append(w)
+        x = torch.cat(xs, dim=0)
+        w = torch.cat(ws) / nit
+        if mode == 'rbatch':
+            x = x.t()
+        return w, x
+
+    # ------------------------------------------------------------ integrate
+    def _classify(self, fcn):
+        if isinstance(fcn, BuiltinIntegrand):
+            return 'builtin'
+        ft = getattr(fcn, 'fcntype', 'scalar')
+        if ft == 'lbatch':
+            return 'lbatch'
+        if ft == 'rbatch':
+            return 'rbatch'
+        return 'scalar'
+
+    def _eval_batch(self, fcn, kind, x):
+        if kind == 'lbatch':
+            f = fcn(x)
+        elif kind == 'rbatch':
+            f = fcn(x.t())
+        else:
+            xc = x.cpu().numpy()
+            f = np.array([fcn(xi) for xi in xc], dtype=float)
+        if not isinstance(f, torch.Tensor):
+            f = torch.as_tensor(np.asarray(f, dtype=float), device=self.device)
+        f = f.to(self.device)
+        if f.dim() > 1:
+            if f[0].numel() != 1:
+                raise NotImplementedError('array-valued integrands are not supported yet')
+            f = f.reshape(f.shape[0])
+        return f
+
+    def __call__(self, fcn, save=None, saveall=None, **kargs):
+        """Integrate ``fcn``; returns an :class:`RAvg` (pyx:1912-2230)."""
+        if kargs:
+            self.set(kargs)
+        if isinstance(fcn, type):
+            raise ValueError('integrand given is a class, not an object -- need to initialize?')
+        kind = self._classify(fcn)
+        result = RAvg(weighted=self.adapt)
+        L = N.load()
+        stream = N.stream_ptr(self.device)
+        dt = torch.float64 if self.precision == 'fp64' else torch.float32
+        for itn in range(self.nitn):
+            if self.analyzer is not None:
+                self.analyzer.begin(itn, self)
+            it, ncap = self._struct()
+            self._allocate(it)
+            self._itn += 1
+            itn_word = self._itn & 0xffffffff
+            u = None
+            if kind == 'builtin' and self.ran_array_generator is None:
+                p = fcn.params(self.dim)
+                N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, None, int(fcn.kind),
+                                             N.dbl_array(p), len(p), stream))
+            else:
+                st = self._read_stats()
+                n = int(st.neval)
+                if self.ran_array_generator is not None:
+                    u = self._draw_u(n)
+                if kind == 'builtin':
+                    p = fcn.params(self.dim)
+                    N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, N.ptr(u),
+                                                 int(fcn.kind), N.dbl_array(p), len(p), stream))
+                else:
+                    x, _, _, _ = self._points(it, ncap, itn_word, u)
+                    f = torch.empty(ncap, dtype=dt, device=self.device)
+                    nb = max(1, int(self.min_neval_batch))
+                    for lo in range(0, n, nb):
+                        hi = min(n, lo + nb)
+                        fb = self._eval_batch(fcn, kind, x[lo:hi])
+                        if fb.shape[0] != hi - lo:
+                            raise ValueError('integrand returned %d values for %d points'
+                                             % (fb.shape[0], hi - lo))
+                        f[lo:hi] = fb.to(dt)
+                    if bool(torch.isnan(f[:n]).any()):
+                        raise ValueError('integrand evaluates to nan')
+                    N.check(L.vg_reduce(ctypes.byref(it), itn_word, N.ptr(u), N.ptr(f),
+                                        N.VG_F64 if dt == torch.float64 else N.VG_F32, stream))
+            # adapt the map on the device before reading the iteration record
+            N.check(L.vg_end_iteration(ctypes.byref(it), stream))
+            st = self._read_stats()
+            if st.status == N.VG_ERR_MEMORY:
+                raise MemoryError('iteration exceeded its evaluation capacity')
+            elif st.status != 0:
+                raise N.VegasError('device status %d' % st.status)
+            if st.nan_seen:
+                raise ValueError('integrand evaluates to nan')
+            self.last_neval = int(st.neval)
+            self.neval_hcube_range = np.array([st.range_lo, st.range_hi])
+            if self.beta > 0 and self.adapt and self.nhcube > 1:
+                self.sum_sigf = float(st.sum_sigf)
+            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            result.sum_neval += self.last_neval
+            if self.analyzer is not None:
+                self.analyzer.end(result.itn_results[-1], result)
+            if save is not None:
+                _save(save, result)
+            if saveall is not None:
+                _save(saveall, (result, self))
+            if result.converged(self.rtol, self.atol):
+                break
+        return result
+
+    # --------------------------------------------------------------- report
+    def settings(self, ngrid=0):
+        """Text summary of the settings (pyx:1448-1590)."""
+        nhcube = int(np.prod(self.nstrat))
+        neval = nhcube * self.min_neval_hcube if self.beta <= 0 else self.neval
+        ans = 'Integrator Settings:\n'
+        if self.beta > 0 and not self.adapt_to_errors:
+            ans += '    %.6g (approx) integrand evaluations in each of %d iterations\n' % (
+                self.neval, self.nitn)
+        else:
+            ans += '    %.6g integrand evaluations in each of %d iterations\n' % (neval, self.nitn)
+        ans += '    number of: strata/axis = %s\n' % np.array2string(
+            np.asarray(self.nstrat), max_line_width=80, prefix=29 * ' ')
+        ans += '               increments/axis = %s\n' % np.array2string(
+            np.asarray(self.map.ninc), max_line_width=80, prefix=33 * ' ')
+        ans += '               h-cubes = %.6g  processors = %d\n' % (nhcube, self.nproc)
+        max_neval_hcube = max(self.max_neval_hcube, self.min_neval_hcube)
+        ans += '               evaluations/batch >= %.2g\n' % (float(self.min_neval_batch),)
+        ans += '               %d <= evaluations/h-cube <= %.2g\n' % (
+            int(self.min_neval_hcube), float(max_neval_hcube))
+        ans += '    minimize_mem = %s  adapt_to_errors = %s  adapt = %s\n' % (
+            str(self.minimize_mem), str(self.adapt_to_errors), str(self.adapt))
+        ans += '    accuracy: relative = %g  absolute = %g\n' % (self.rtol, self.atol)
+        if not self.adapt:
+            ans += '    damping: alpha = %g  beta= %g\n\n' % (0., 0.)
+        else:
+            ans += '    damping: alpha = %g  beta= %g\n\n' % (self.alpha, self.beta)
+        limits = ['({:.5}, {:.5})'.format(*l) for l in self.map.region()]
+        entries = [(str(a), lim) for a, lim in enumerate(limits)]
+        w1 = max(len('axis'), max(len(e[0]) for e in entries))
+        w2 = max(len('integration limits'), max(len(e[1]) for e in entries))
+        lines = ['{:>{w1}}    {:>{w2}}'.format('axis', 'integration limits', w1=w1, w2=w2)]
+        lines.append(len(lines[0]) * '-')
+        for a, lim in entries:
+            lines.append('{:>{w1}}    {:>{w2}}'.format(a, lim, w1=w1, w2=w2))
+        ans += '    ' + '\n    '.join(lines) + '\n'
+        if ngrid > 0:
+            ans += '\n' + self.map.settings(ngrid=ngrid)
+        return ans
+
+
+def strata(dim, mode, neval, neval_given, nstrat, neval_frac=0.75, beta=0.75,
+           adapt_to_errors=False, uniform_nstrat=False, max_mem=1e9, minimize_mem=False,
+           maxinc_axis=1000):
+    """Strata, increments and min_neval_hcube of Integrator.set (pyx:1333-1407).
+
+    mode 0: from neval; 1: explicit nstrat; 2: keep nstrat.  Host logic in
+    the C ABI (vg_set_strata), which reproduces the reference's complex-power
+    rounding of the strata count."""
+    neval = ctypes.c_int64(int(neval))
+    ns_out = (ctypes.c_int64 * dim)()
+    ninc_out = (ctypes.c_int64 * dim)()
+    mnh = ctypes.c_int64(0)
+    nstrat_in = N.i64_array(nstrat if nstrat is not None else np.zeros(dim, np.int64))
+    L = N.load()
+    N.check(L.vg_set_strata(dim, mode, ctypes.byref(neval), 1 if neval_given else 0, nstrat_in,
+                            float(neval_frac), float(beta), int(adapt_to_errors),
+                            int(uniform_nstrat), float(max_mem), int(minimize_mem),
+                            int(maxinc_axis), ns_out, ninc_out, ctypes.byref(mnh)))
+    return dict(neval=int(neval.value), nstrat=np.array(list(ns_out), np.int64),
+                ninc=np.array(list(ninc_out), np.int64), min_neval_hcube=int(mnh.value))
+
+
+def _save(dest, obj):
+    if isinstance(dest, str):
+        with open(dest, 'wb') as f:
+            pickle.dump(obj, f)
+    else:
+        pickle.dump(obj, dest)
+
+
+class reporter(object):
+    """Analyzer printing a report after each iteration (pyx:2232-2269)."""
+
+    def __init__(self, ngrid=0):
+        self.ngrid = ngrid
+        self.clock = time.perf_counter
+
+    def begin(self, itn, integrator):
+        self.integrator = integrator
+        self.itn = itn
+        self.t0 = self.clock()
+        if itn == 0:
+            print(integrator.settings())
+        sys.stdout.flush()
+
+    def end(self, itn_ans, ans):
+        print("    itn %2d: %s\n all itn's: %s" % (self.itn + 1, itn_ans, ans))
+        print('    neval = %s  neval/h-cube = %s\n    chi2/dof = %.2f  Q = %.2f  time = %.2f' % (
+            format(self.integrator.last_neval, '.6g'), tuple(self.integrator.neval_hcube_range),
+            ans.chi2 / ans.dof if ans.dof > 0 else 0, ans.Q if ans.dof > 0 else 1.,
+            self.clock() - self.t0))
+        print(self.integrator.map.settings(ngrid=self.ngrid))
+        print('')
+        sys.stdout.flush()
