@@ -47,6 +47,8 @@ def parse():
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-tta', action='store_true')
+    ap.add_argument('--device-loop-only', action='store_true',
+                    help='run only the device-resident iteration loop (for profilers)')
     return ap.parse_args()
 
 
@@ -168,6 +170,8 @@ def gpu_arm(args):
         itn += 1
     barrier()
     clk = clocks.stop()
+    if args.device_loop_only:
+        return
     step_ms = [evs[k][0].elapsed_time(evs[k][3]) for k in range(args.steps)]
     kern_ms = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
     st = integ._read_stats()
@@ -206,7 +210,7 @@ def gpu_arm(args):
         integ3 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=4242 + rank, device=dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r3 = integ3(f, nitn=200, rtol=1e-4)
+        r3 = integ3(f, nitn=5000, rtol=1e-4)
         torch.cuda.synchronize()
         tta = {'seconds': time.perf_counter() - t0, 'iterations': r3.nitn,
                'result': str(r3), 'rel_err': r3.sdev / abs(r3.mean),

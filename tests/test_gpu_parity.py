@@ -145,23 +145,36 @@ def test_adapt_kernel_golden():
 
 
 def test_fused_fp64_matches_oracle_philox():
-    """Fused FP64 iterations (Philox draws) == oracle on the same draws."""
-    for kind_cls, params in ((vg.Gaussian(a=100.0, c=0.5, dim=4), None),
-                             (vg.Ridge(M=50, s=0.05), None)):
+    """Fused FP64 iterations (Philox draws) == oracle on the same draws.
+
+    Each iteration starts the GPU from the oracle's state (grid, sigf,
+    sum_sigf), so single-iteration outputs are compared at 1e-12; a second
+    loop lets both run freely and checks the looser agreement that results
+    from grid differences at the 1e-16 level being amplified."""
+    for f in (vg.Gaussian(a=100.0, c=0.5, dim=4), vg.Ridge(M=50, s=0.05)):
         seed = 99
         I = vg.Integrator(4 * [[0, 1]], neval=6000, precision='fp64', seed=seed)
         st = O.State(4 * [[0, 1]], 6000)
         for itn in range(1, 4):
-            r = I(kind_cls, nitn=1)
-            out = st.iterate(kind_cls.kind, kind_cls.params(4), seed=seed, stream=0, itn=itn)
+            set_state(I, st.grid, st.sigf, st.sum_sigf)
+            r = I(f, nitn=1)
+            out = st.iterate(f.kind, f.params(4), seed=seed, stream=0, itn=itn)
             assert I.last_neval == out['neval']
             assert rel(r.itn_results[0].mean, out['mean']) <= RTOL
-            assert rel(r.itn_results[0].var, out['var']) <= 1e-10
-            assert rel(I.sigf, st.sigf) <= 1e-10
+            assert rel(r.itn_results[0].var, out['var']) <= RTOL
+            assert rel(I.sigf, st.sigf) <= RTOL
             g = I.map.grid
             for d in range(4):
                 K = st.ninc[d]
-                assert np.max(np.abs(g[d, :K + 1] - st.grid[d, :K + 1])) <= 1e-12
+                assert np.max(np.abs(g[d, :K + 1] - st.grid[d, :K + 1])) <= RTOL
+        # free-running: same draws, independent state
+        I = vg.Integrator(4 * [[0, 1]], neval=6000, precision='fp64', seed=seed)
+        st = O.State(4 * [[0, 1]], 6000)
+        for itn in range(1, 6):
+            r = I(f, nitn=1)
+            out = st.iterate(f.kind, f.params(4), seed=seed, stream=0, itn=itn)
+            assert I.last_neval == out['neval']
+            assert rel(r.itn_results[0].mean, out['mean']) <= 1e-9
 
 
 def test_dropin_matches_fused_fp64():

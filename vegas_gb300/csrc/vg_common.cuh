@@ -34,23 +34,28 @@ __device__ __forceinline__ VgU4 vg_philox(uint32_t c0, uint32_t c1, uint32_t c2,
     return VgU4{c0, c1, c2, c3};
 }
 
-// Uniforms for sample i, axes [0, dim): FP64 (53 bits, two words per axis,
-// group d>>1 | 0x80) and FP32 (24 bits, one word per axis, group d>>2).
+// Uniforms for sample i, axes [0, dim) (dim <= DIMB): FP64 takes two words
+// per axis (53 bits, counter word 3 = stream<<8 | 0x80 | d>>1), FP32 one word
+// per axis (24 bits, counter word 3 = stream<<8 | d>>2).  Same stream as the
+// oracle (vo_uniform_f64 / vo_uniform_f32).
 template <typename T>
 struct VgUniform;
 
 template <>
 struct VgUniform<double> {
+    template <int DIMB>
     static __device__ __forceinline__ void draw(uint64_t seed, uint32_t stream, uint32_t itn,
                                                 uint64_t i, int dim, double *u)
     {
-        for (int g = 0; 2 * g < dim; g++) {
+#pragma unroll
+        for (int g = 0; 2 * g < DIMB; g++) {
+            if (2 * g >= dim) break;
             VgU4 r = vg_philox((uint32_t)i, (uint32_t)(i >> 32), itn,
                                (stream << 8) | 0x80u | (uint32_t)g, (uint32_t)seed,
                                (uint32_t)(seed >> 32));
             uint64_t m0 = ((uint64_t)r.x << 21) | (uint64_t)(r.y >> 11);
             u[2 * g] = (double)m0 * (1.0 / 9007199254740992.0);
-            if (2 * g + 1 < dim) {
+            if (2 * g + 1 < DIMB) {
                 uint64_t m1 = ((uint64_t)r.z << 21) | (uint64_t)(r.w >> 11);
                 u[2 * g + 1] = (double)m1 * (1.0 / 9007199254740992.0);
             }
@@ -60,17 +65,20 @@ struct VgUniform<double> {
 
 template <>
 struct VgUniform<float> {
+    template <int DIMB>
     static __device__ __forceinline__ void draw(uint64_t seed, uint32_t stream, uint32_t itn,
                                                 uint64_t i, int dim, float *u)
     {
-        for (int g = 0; 4 * g < dim; g++) {
+        const float s = 1.0f / 16777216.0f;
+#pragma unroll
+        for (int g = 0; 4 * g < DIMB; g++) {
+            if (4 * g >= dim) break;
             VgU4 r = vg_philox((uint32_t)i, (uint32_t)(i >> 32), itn, (stream << 8) | (uint32_t)g,
                                (uint32_t)seed, (uint32_t)(seed >> 32));
-            const float s = 1.0f / 16777216.0f;
             u[4 * g] = (float)(r.x >> 8) * s;
-            if (4 * g + 1 < dim) u[4 * g + 1] = (float)(r.y >> 8) * s;
-            if (4 * g + 2 < dim) u[4 * g + 2] = (float)(r.z >> 8) * s;
-            if (4 * g + 3 < dim) u[4 * g + 3] = (float)(r.w >> 8) * s;
+            if (4 * g + 1 < DIMB) u[4 * g + 1] = (float)(r.y >> 8) * s;
+            if (4 * g + 2 < DIMB) u[4 * g + 2] = (float)(r.z >> 8) * s;
+            if (4 * g + 3 < DIMB) u[4 * g + 3] = (float)(r.w >> 8) * s;
         }
     }
 };

@@ -1,0 +1,29 @@
+// vg_fused.cuh -- dimension-bucket dispatch of the fused tile kernel for one
+// built-in integrand (included by one vg_fused_*.cu file per integrand so the
+// instantiations compile in parallel).
+#pragma once
+#include "vg_tile.cuh"
+
+namespace vg {
+
+template <int KIND>
+int launch_fused_kind(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st)
+{
+    if (f64) {
+        if (a.dim <= 8) return launch_tile<double, MODE_FUSED, KIND, 8, 2>(a, &P, tab_len, st);
+        return launch_tile<double, MODE_FUSED, KIND, 64, 1>(a, &P, tab_len, st);
+    }
+    if (a.dim <= 4) return launch_tile<float, MODE_FUSED, KIND, 4, 4>(a, &P, tab_len, st);
+    if (a.dim <= 8) return launch_tile<float, MODE_FUSED, KIND, 8, 4>(a, &P, tab_len, st);
+    if (a.dim <= 16) return launch_tile<float, MODE_FUSED, KIND, 16, 2>(a, &P, tab_len, st);
+    return launch_tile<float, MODE_FUSED, KIND, 64, 1>(a, &P, tab_len, st);
+}
+
+int launch_fused_gauss(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+int launch_fused_ridge(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+int launch_fused_lorentz(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+int launch_fused_mixture(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+int launch_fused_lattice(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+int launch_fused_const(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+
+}  // namespace vg

@@ -1,0 +1,10 @@
+// vg_fused_lattice.cu -- fused tile-kernel instantiations for the built-in
+// integrand VG_F_LATTICE (see vg_integrands.cuh).
+#include "vg_fused.cuh"
+
+namespace vg {
+int launch_fused_lattice(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st)
+{
+    return launch_fused_kind<VG_F_LATTICE>(a, P, tab_len, f64, st);
+}
+}  // namespace vg

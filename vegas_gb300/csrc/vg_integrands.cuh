@@ -27,7 +27,7 @@ constexpr double VG_PI = 3.14159265358979323846;
 constexpr double VG_LOG2E = 1.4426950408889634074;
 
 // ------------------------------------------------------------------ FP64
-template <int KIND>
+template <int KIND, int DIMB>
 __device__ __forceinline__ double vg_eval_f64(const VgParams &P, int dim, const double *x)
 {
     const double *p = P.p;
@@ -172,23 +172,29 @@ __device__ __forceinline__ float vg_ex2(float x)
     return r;
 }
 
-template <int KIND>
+template <int KIND, int DIMB>
 __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *__restrict__ tab,
                                              int nterm, int dim, const float *x)
 {
     if (KIND == VG_F_GAUSS) {
         float s = 0.f;
-        for (int d = 0; d < dim; d++) {
+#pragma unroll
+        for (int d = 0; d < DIMB; d++) {
+            if (d >= dim) break;
             float t = x[d] - k.c[1];
             s = fmaf(t, t, s);
         }
         return k.c[2] * vg_ex2(-k.c[0] * s);
     } else if (KIND == VG_F_RIDGE) {
         float m = 0.f;
-        for (int d = 0; d < dim; d++) m += x[d];
+#pragma unroll
+        for (int d = 0; d < DIMB; d++)
+            if (d < dim) m += x[d];
         m *= k.c[3];
         float R = 0.f;
-        for (int d = 0; d < dim; d++) {
+#pragma unroll
+        for (int d = 0; d < DIMB; d++) {
+            if (d >= dim) break;
             float t = x[d] - m;
             R = fmaf(t, t, R);
         }
@@ -211,7 +217,9 @@ __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *
         return k.c[2] * ((a0 + a1) + (a2 + a3));
     } else if (KIND == VG_F_LORENTZ) {
         float f = 1.f;
-        for (int d = 0; d < dim; d++) {
+#pragma unroll
+        for (int d = 0; d < DIMB; d++) {
+            if (d >= dim) break;
             float t = x[d] - tab[d];
             f *= __fdividef(tab[2 * dim + d], fmaf(t, t, tab[3 * dim + d]));
         }
@@ -221,7 +229,9 @@ __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *
         float acc = 0.f;
         for (int q = 0; q < K; q++) {
             float r2 = 0.f;
-            for (int d = 0; d < dim; d++) {
+#pragma unroll
+            for (int d = 0; d < DIMB; d++) {
+                if (d >= dim) break;
                 float t = x[d] - tab[q * dim + d];
                 r2 = fmaf(t, t, r2);
             }
@@ -230,8 +240,10 @@ __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *
         return k.c[1] * acc;
     } else if (KIND == VG_F_LATTICE) {
         float S = 0.f;
-        for (int i = 0; i < dim; i++) {
-            float xi = x[i], xn = x[(i + 1 == dim) ? 0 : i + 1];
+#pragma unroll
+        for (int i = 0; i < DIMB; i++) {
+            if (i >= dim) break;
+            float xi = x[i], xn = (i + 1 == dim) ? x[0] : x[(i + 1) % DIMB];
             float dx = xn - xi;
             float x2 = xi * xi;
             S = fmaf(dx * dx, k.c[0], S);

@@ -1,0 +1,717 @@
+// vg_tile.cuh -- the persistent tile kernel of a vegas+ iteration.
+//
+// Reference: src/vegas/_vegas.pyx (vegas 6.4.1): sampling and map of
+// Integrator._random_batch (pyx:1731-1752), the per-hypercube two-pass
+// reduction of Integrator.__call__ (pyx:2136-2193), the training feed
+// (pyx:2173, 2196-2197 -> AdaptiveMap.add_training_data pyx:421-464).
+//
+// Samples of an iteration are ordered by hypercube (as in the reference).  A
+// tile is NT*S consecutive samples; thread t owns samples [t*S, t*S+S) of the
+// tile.  CTAs take tiles from an atomic counter; everything a tile produces
+// is indexed by the tile, so results do not depend on which CTA ran it.
+//
+// Template parameters: T (float | double) is the sampling/map/integrand
+// arithmetic; DIMB is a compile-time bound on the dimension (arrays stay in
+// registers); S samples per thread; MODE points / reduce / fused; KIND the
+// built-in integrand of the fused mode.
+#pragma once
+#include <math.h>
+#include <string.h>
+
+#include "vg_common.cuh"
+#include "vg_integrands.cuh"
+
+namespace vg {
+
+constexpr int NT = 256;          // threads per tile CTA
+constexpr int BASE_TILE = 256;   // granularity of the tile schedule tile_h0[]
+constexpr int ALLOC_NT = 1024;
+constexpr int ALLOC_PER = 4;
+constexpr int FIN_NT = 1024;
+
+enum { MODE_POINTS = 0, MODE_REDUCE = 1, MODE_FUSED = 2 };
+
+// Partial statistics of a hypercube cut by a tile boundary.
+struct TileRec {
+    int64_t h;       // hypercube, -1 if the slot is empty
+    double n;        // samples of h inside the tile
+    double S;        // sum of wf
+    double Q;        // sum of squared deviations about S/n (EPSILON-guarded)
+    double D;        // sum of deviations (round-off residue: Neely correction)
+    int32_t spans;   // head slot only: h also continues past the tile
+    int32_t pad;
+};
+
+struct TilePart {
+    VgKSum mean, var, sigf;
+};
+
+struct IterArgs {
+    int dim;
+    int nstrat[VG_MAX_DIM];
+    int ninc[VG_MAX_DIM];
+    const double *grid, *inc;
+    int64_t ldg, ldi;
+    int64_t H;
+    int64_t ncap;
+    double *sigf;
+    double beta;
+    int adaptive;             // update sigf (pyx:2083, 2183-2186)
+    int adaptive_alloc;       // allocate from sigf (pyx:1668)
+    int train;                // accumulate training histogram (pyx:2196)
+    double *sum_f;
+    unsigned long long *n_f;
+    vg_stats *stats;
+    int32_t *neval_h;
+    int64_t *offsets;
+    int64_t *bsum, *bmax;
+    int64_t *tile_h0;         // first hypercube of each BASE_TILE samples
+    unsigned long long *counter;  // dynamic tile counter (reset by allocation)
+    TileRec *recs;
+    TilePart *parts;
+    int64_t ntiles_cap;       // in BASE_TILE units
+    int64_t neval;
+    double neval_frac;
+    int64_t min_neval_hcube, max_neval_hcube;
+    uint64_t seed;
+    uint32_t stream;
+    uint32_t itn;
+    const double *u;          // injected uniforms [n, dim] or nullptr
+    const void *f_in;         // MODE_REDUCE
+    int f_f64;
+    void *x_out, *y_out;      // MODE_POINTS
+    double *wgt_out;
+    int64_t *hc_out;
+    int table_smem;           // grid table staged in shared memory
+    int hist_smem;            // training histogram in shared memory
+    int maxK;
+    int tab_len;              // integrand table length (floats)
+    int T;                    // tile size of the launched kernel
+};
+
+template <typename T>
+struct GridEntry;
+template <>
+struct GridEntry<float> {
+    typedef float2 type;
+};
+template <>
+struct GridEntry<double> {
+    typedef double2 type;
+};
+
+struct SmemPlan {
+    size_t table, hsum, hcnt, bins, win_off, win_n, seg_S, keyF, keyL, P, red, itab, total;
+};
+
+template <typename T>
+__host__ __device__ inline SmemPlan smem_plan(int dim, int maxK, int Ttile, int table_smem,
+                                              int hist_smem, int tab_len, int bins_smem)
+{
+    SmemPlan p;
+    size_t o = 0;
+    p.table = o;
+    if (table_smem) o = (o + sizeof(typename GridEntry<T>::type) * (size_t)dim * (maxK + 1) + 15) & ~(size_t)15;
+    p.hsum = o;
+    if (hist_smem) o = (o + sizeof(T) * (size_t)dim * maxK + 15) & ~(size_t)15;
+    p.hcnt = o;
+    if (hist_smem) o = (o + sizeof(unsigned int) * (size_t)dim * maxK + 15) & ~(size_t)15;
+    p.bins = o;
+    if (bins_smem) o = (o + sizeof(unsigned short) * (size_t)Ttile * dim + 15) & ~(size_t)15;
+    p.win_off = o; o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
+    p.win_n = o;   o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
+    p.seg_S = o;   o = (o + sizeof(double) * (Ttile + 2) + 15) & ~(size_t)15;
+    p.keyF = o;    o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
+    p.keyL = o;    o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
+    p.P = o;       o = (o + sizeof(double2) * NT + 15) & ~(size_t)15;
+    p.red = o;     o = (o + sizeof(VgKSum) * (NT / 32) * 3 + 64 + 15) & ~(size_t)15;
+    p.itab = o;    o = (o + sizeof(float) * (tab_len + 4) + 15) & ~(size_t)15;
+    p.total = o;
+    return p;
+}
+
+// Inclusive segmented scan over the NT threads of (flag, value2); the result
+// for thread t is returned and stored in P[t].
+__device__ __forceinline__ double2 seg_scan(int flag, double2 v, double2 *P, double2 *wsum,
+                                            int *wflag)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int f = flag;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        double ux = __shfl_up_sync(0xffffffffu, v.x, off);
+        double uy = __shfl_up_sync(0xffffffffu, v.y, off);
+        int uf = __shfl_up_sync(0xffffffffu, f, off);
+        if (lane >= off) {
+            if (!f) {
+                v.x = ux + v.x;
+                v.y = uy + v.y;
+            }
+            f |= uf;
+        }
+    }
+    if (lane == 31) {
+        wsum[w] = v;
+        wflag[w] = f;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int NW = NT / 32;
+        double2 x = lane < NW ? wsum[lane] : make_double2(0.0, 0.0);
+        int g = lane < NW ? wflag[lane] : 1;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            double ux = __shfl_up_sync(0xffffffffu, x.x, off);
+            double uy = __shfl_up_sync(0xffffffffu, x.y, off);
+            int ug = __shfl_up_sync(0xffffffffu, g, off);
+            if (lane >= off) {
+                if (!g) {
+                    x.x = ux + x.x;
+                    x.y = uy + x.y;
+                }
+                g |= ug;
+            }
+        }
+        if (lane < NW) wsum[lane] = x;
+    }
+    __syncthreads();
+    if (w > 0 && !f) {
+        double2 c = wsum[w - 1];
+        v.x = c.x + v.x;
+        v.y = c.y + v.y;
+    }
+    P[threadIdx.x] = v;
+    __syncthreads();
+    return v;
+}
+
+// ------------------------------------------------- integrand, batched over S
+template <typename T, int KIND, int DIMB, int S>
+struct BatchEval {
+    static __device__ __forceinline__ void run(const VgParams &prm, const VgF32Consts &kc,
+                                               const float *tab, int nterm, int dim,
+                                               const T (&x)[S][DIMB], double (&f)[S])
+    {
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            if (sizeof(T) == 8) f[k] = vg_eval_f64<KIND, DIMB>(prm, dim, (const double *)x[k]);
+            else f[k] = (double)vg_eval_f32<KIND, DIMB>(kc, tab, nterm, dim, (const float *)x[k]);
+        }
+    }
+};
+
+// Ridge in FP32: all S samples of the thread share each pass over the M term
+// offsets v_j (one shared-memory load feeds 4*S exponentials).
+template <int DIMB, int S>
+struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
+    static __device__ __forceinline__ void run(const VgParams &prm, const VgF32Consts &kc,
+                                               const float *tab, int nterm, int dim,
+                                               const float (&x)[S][DIMB], double (&f)[S])
+    {
+        float E0[S], w[S], a0[S], a1[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            float m = 0.f;
+#pragma unroll
+            for (int d = 0; d < DIMB; d++)
+                if (d < dim) m += x[k][d];
+            m *= kc.c[3];
+            float R = 0.f;
+#pragma unroll
+            for (int d = 0; d < DIMB; d++)
+                if (d < dim) {
+                    float t = x[k][d] - m;
+                    R = fmaf(t, t, R);
+                }
+            E0[k] = -kc.c[0] * R;
+            w[k] = m * kc.c[1];
+            a0[k] = 0.f;
+            a1[k] = 0.f;
+        }
+        const float4 *t4 = reinterpret_cast<const float4 *>(tab);
+        const int n4 = nterm >> 2;
+#pragma unroll 2
+        for (int q = 0; q < n4; q++) {
+            const float4 v = t4[q];
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                float d0 = w[k] - v.x, d1 = w[k] - v.y, d2 = w[k] - v.z, d3 = w[k] - v.w;
+                a0[k] += vg_ex2(fmaf(-d0, d0, E0[k]));
+                a1[k] += vg_ex2(fmaf(-d1, d1, E0[k]));
+                a0[k] += vg_ex2(fmaf(-d2, d2, E0[k]));
+                a1[k] += vg_ex2(fmaf(-d3, d3, E0[k]));
+            }
+        }
+        for (int j = n4 << 2; j < nterm; j++) {
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                float d0 = w[k] - tab[j];
+                a0[k] += vg_ex2(fmaf(-d0, d0, E0[k]));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < S; k++) f[k] = (double)(kc.c[2] * (a0[k] + a1[k]));
+    }
+};
+
+// ------------------------------------------------------------------ kernel
+template <typename T, int MODE, int KIND, int DIMB, int S>
+__global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    typedef typename GridEntry<T>::type GE;
+    constexpr int TT = NT * S;
+    constexpr int KSUB = TT / BASE_TILE;   // base tiles per tile
+    const int dim = a.dim;
+    const int tid = threadIdx.x;
+    const int use_bins = (MODE != MODE_POINTS) && a.train;
+    const SmemPlan sp = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, a.tab_len,
+                                     use_bins);
+    GE *table = (GE *)(smem + sp.table);
+    T *hsum = (T *)(smem + sp.hsum);
+    unsigned int *hcnt = (unsigned int *)(smem + sp.hcnt);
+    unsigned short *sbins = (unsigned short *)(smem + sp.bins);
+    int *win_off = (int *)(smem + sp.win_off);
+    int *win_n = (int *)(smem + sp.win_n);
+    double *seg_S = (double *)(smem + sp.seg_S);
+    int *keyF = (int *)(smem + sp.keyF);
+    int *keyL = (int *)(smem + sp.keyL);
+    double2 *Pv = (double2 *)(smem + sp.P);
+    VgKSum *red = (VgKSum *)(smem + sp.red);
+    float *itab = (float *)(smem + sp.itab);
+    double2 *wsum = (double2 *)red;   // scan scratch (aliases red; used apart)
+    int *wflag = (int *)(red + NT / 32 + 1);
+    __shared__ int64_t s_tile;
+
+    const int64_t N = a.stats->neval;
+    const int64_t ntiles = (N + TT - 1) / TT;
+    if (a.stats->ntiles == 0) return;   // allocation failed: nothing to do
+
+    // ---- per-CTA setup: grid table, histogram, integrand constants
+    if (a.table_smem) {
+        for (int d = 0; d < dim; d++) {
+            const int K = a.ninc[d];
+            for (int i = tid; i <= K; i += NT) {
+                GE e;
+                if (i < K) {
+                    e.x = (T)a.grid[d * a.ldg + i];
+                    e.y = (T)a.inc[d * a.ldi + i];
+                } else {
+                    e.x = (T)a.grid[d * a.ldg + K];
+                    e.y = (T)a.inc[d * a.ldi + K - 1];
+                }
+                table[(size_t)d * (a.maxK + 1) + i] = e;
+            }
+        }
+    }
+    if (use_bins && a.hist_smem) {
+        for (int i = tid; i < dim * a.maxK; i += NT) {
+            hsum[i] = (T)0;
+            hcnt[i] = 0u;
+        }
+    }
+    VgF32Consts kc;
+    if (MODE == MODE_FUSED && sizeof(T) == 4) {
+        kc = vg_prepare_f32<KIND>(prm, dim);
+        vg_fill_table_f32<KIND>(prm, dim, itab, kc);
+    } else {
+        for (int i = 0; i < 8; i++) kc.c[i] = 0.f;
+    }
+    const double dv_y = __ddiv_rn(1.0, (double)a.H);
+    const double beta_half = __ddiv_rn(a.beta, 2.0);
+    int nan_local = 0;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_tile = (int64_t)atomicAdd(a.counter, 1ull);
+        __syncthreads();
+        const int64_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const int64_t tile_start = tile * (int64_t)TT;
+        const int tile_len = (int)min((int64_t)TT, N - tile_start);
+        const int64_t h0 = a.tile_h0[tile * KSUB];
+        const int64_t bnext = (tile + 1) * KSUB;            // base tile after this tile
+        const int64_t nbase = (N + BASE_TILE - 1) / BASE_TILE;
+        const int64_t hnext = bnext < nbase ? a.tile_h0[bnext] : a.H;
+        const int64_t hlast = (hnext < a.H) ? hnext : a.H - 1;
+        const int nwin = (int)(hlast - h0 + 1);
+        if (nwin < 1 || nwin > TT) {   // impossible while every count is >= 2
+            if (tid == 0) a.stats->status = VG_ERR_UNSUPPORTED;
+            break;
+        }
+        for (int k = tid; k <= nwin; k += NT) {
+            int64_t h = h0 + k;
+            int64_t o = (h <= a.H) ? a.offsets[h] : N;
+            int64_t r = o - tile_start;
+            win_off[k] = (int)(r < 0 ? 0 : (r > tile_len ? tile_len : r));
+            if (k < nwin) win_n[k] = a.neval_h[h];
+        }
+        __syncthreads();
+
+        // ---- pass 0: draw, map, evaluate the thread's samples
+        const int li0 = tid * S;
+        int nmine = tile_len - li0;
+        nmine = nmine < 0 ? 0 : (nmine > S ? S : nmine);
+        int lh = 0;
+        if (nmine > 0) {
+            int lo = 0, hi = nwin - 1;   // last k with win_off[k] <= li0
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (win_off[mid] <= li0) lo = mid;
+                else hi = mid - 1;
+            }
+            lh = lo;
+        }
+        int y0[DIMB];
+        {
+            int64_t hh = h0 + lh;
+#pragma unroll
+            for (int d = 0; d < DIMB; d++) {
+                if (d < dim) {
+                    int64_t q = hh / a.nstrat[d];
+                    y0[d] = (int)(hh - q * a.nstrat[d]);
+                    hh = q;
+                } else {
+                    y0[d] = 0;
+                }
+            }
+        }
+        T xs[S][DIMB];
+        double wg[S];
+        int lhs[S];
+        int cur = lh;
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            lhs[k] = cur;
+            wg[k] = 0.0;
+#pragma unroll
+            for (int d = 0; d < DIMB; d++) xs[k][d] = (T)0.5;
+            if (k < nmine) {
+                const int li = li0 + k;
+                while (li >= win_off[cur + 1]) {   // next hypercube: mixed-radix increment
+                    cur++;
+                    int carry = 1;
+#pragma unroll
+                    for (int d = 0; d < DIMB; d++) {
+                        if (d < dim && carry) {
+                            if (++y0[d] < a.nstrat[d]) carry = 0;
+                            else y0[d] = 0;
+                        }
+                    }
+                }
+                lhs[k] = cur;
+                const int64_t ig = tile_start + li;
+                const int nh = win_n[cur];
+                T u[DIMB];
+                if (a.u != nullptr) {
+#pragma unroll
+                    for (int d = 0; d < DIMB; d++)
+                        if (d < dim) u[d] = (T)a.u[ig * dim + d];
+                } else {
+                    VgUniform<T>::template draw<DIMB>(a.seed, a.stream, a.itn, (uint64_t)ig, dim, u);
+                }
+                T jac = (T)1;
+                T yv[DIMB];
+#pragma unroll
+                for (int d = 0; d < DIMB; d++) {
+                    if (d >= dim) continue;
+                    const int K = a.ninc[d];
+                    T yd;
+                    if (sizeof(T) == 8)
+                        yd = (T)__ddiv_rn(__dadd_rn((double)y0[d], (double)u[d]), (double)a.nstrat[d]);
+                    else
+                        yd = (T)__fdiv_rn((float)y0[d] + (float)u[d], (float)a.nstrat[d]);
+                    yv[d] = yd;
+                    T yn;
+                    if (sizeof(T) == 8) yn = (T)__dmul_rn((double)yd, (double)K);
+                    else yn = (T)((float)yd * (float)K);
+                    int iy = (sizeof(T) == 8) ? (int)floor((double)yn) : (int)floorf((float)yn);
+                    T dy = yn - (T)iy;
+                    const int clamp = iy >= K;
+                    const int ie = clamp ? K : iy;
+                    GE e;
+                    if (a.table_smem) {
+                        e = table[(size_t)d * (a.maxK + 1) + ie];
+                    } else if (!clamp) {
+                        e.x = (T)a.grid[d * a.ldg + ie];
+                        e.y = (T)a.inc[d * a.ldi + ie];
+                    } else {
+                        e.x = (T)a.grid[d * a.ldg + K];
+                        e.y = (T)a.inc[d * a.ldi + K - 1];
+                    }
+                    if (sizeof(T) == 8) {
+                        xs[k][d] = clamp ? e.x
+                                         : (T)__dadd_rn((double)e.x, __dmul_rn((double)e.y, (double)dy));
+                        jac = (T)__dmul_rn((double)jac, __dmul_rn((double)e.y, (double)K));
+                    } else {
+                        xs[k][d] = clamp ? e.x : (T)fmaf((float)e.y, (float)dy, (float)e.x);
+                        jac = (T)((float)jac * ((float)e.y * (float)K));
+                    }
+                    if (use_bins)
+                        sbins[(li0 + k) * dim + d] =
+                            (unsigned short)((yd > (T)0 && yd < (T)1 && iy < K) ? iy : 0xffff);
+                }
+                // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
+                if (sizeof(T) == 8) wg[k] = __dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
+                else wg[k] = (double)((float)jac * ((float)dv_y / (float)nh));
+                if (MODE == MODE_POINTS) {
+                    T *xo = (T *)a.x_out;
+#pragma unroll
+                    for (int d = 0; d < DIMB; d++)
+                        if (d < dim) xo[ig * dim + d] = xs[k][d];
+                    if (a.y_out) {
+                        T *yo = (T *)a.y_out;
+#pragma unroll
+                        for (int d = 0; d < DIMB; d++)
+                            if (d < dim) yo[ig * dim + d] = yv[d];
+                    }
+                    if (a.wgt_out) a.wgt_out[ig] = wg[k];
+                    if (a.hc_out) a.hc_out[ig] = h0 + cur;
+                }
+            }
+        }
+        if (MODE == MODE_POINTS) continue;
+
+        double fv[S];
+        if (MODE == MODE_FUSED) {
+            BatchEval<T, KIND, DIMB, S>::run(prm, kc, itab, a.tab_len, dim, xs, fv);
+        } else {
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                fv[k] = 0.0;
+                if (k < nmine) {
+                    const int64_t ig = tile_start + li0 + k;
+                    fv[k] = a.f_f64 ? ((const double *)a.f_in)[ig]
+                                    : (double)((const float *)a.f_in)[ig];
+                }
+            }
+        }
+        double wf[S];
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            wf[k] = 0.0;
+            if (k >= nmine) continue;
+            if (fv[k] != fv[k]) nan_local = 1;
+            const double w1 = __dmul_rn(wg[k], fv[k]);   // wgt * f, pyx:2143
+            wf[k] = w1;
+            if (use_bins) {
+                // fdv2 = (wgt*f*neval)^2, pyx:2173; |fdv2| into the bins, pyx:460-463
+                const double t1 = __dmul_rn(w1, (double)win_n[lhs[k]]);
+                const double fd = __dmul_rn(t1, t1);
+                for (int d = 0; d < dim; d++) {
+                    const unsigned short b = sbins[(li0 + k) * dim + d];
+                    if (b == 0xffff) continue;
+                    if (a.hist_smem) {
+                        atomicAdd(&hsum[d * a.maxK + b], (T)fd);
+                        atomicAdd(&hcnt[d * a.maxK + b], 1u);
+                    } else {
+                        atomicAdd(&a.sum_f[d * a.ldi + b], fd);
+                        atomicAdd(&a.n_f[d * a.ldi + b], 1ull);
+                    }
+                }
+            }
+        }
+
+        // ---- pass 1: per-run sums of wf; segmented scan across threads
+        const int has = nmine > 0;
+        const int fk = has ? lhs[0] : 0x7fffffff;
+        const int lk = has ? lhs[nmine - 1] : 0x7fffffff;
+        double fsum = 0.0, lsum = 0.0;
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            if (k < nmine && lhs[k] == fk) fsum += wf[k];
+            if (k < nmine && lhs[k] == lk) lsum += wf[k];
+        }
+        keyF[tid] = fk;
+        keyL[tid] = lk;
+        __syncthreads();
+        const int prevL = tid > 0 ? keyL[tid - 1] : -1;
+        const int nextF = tid < NT - 1 ? keyF[tid + 1] : -2;
+        const int flag = (tid == 0) || (lk != prevL);
+        double2 Pi = seg_scan(flag, make_double2(lsum, 0.0), Pv, wsum, wflag);
+        const double carry1 = (tid > 0 && prevL == fk && has) ? Pv[tid - 1].x : 0.0;
+        const int ends_last = has && (lk != nextF);
+        if (has && lk != fk) seg_S[fk] = fsum + carry1;
+        if (ends_last) seg_S[lk] = Pi.x;
+        VgKSum acc_mean = {0.0, 0.0}, acc_var = {0.0, 0.0}, acc_sigf = {0.0, 0.0};
+        __syncthreads();
+
+        // ---- pass 2: deviations about the hypercube mean (pyx:2154-2171)
+        double2 dq_first = make_double2(0.0, 0.0), dq_last = make_double2(0.0, 0.0);
+        {
+            int k = 0;
+            while (k < nmine) {
+                const int key = lhs[k];
+                int k1 = k;
+                double Sloc = 0.0;
+                while (k1 < nmine && lhs[k1] == key) Sloc += wf[k1++];
+                const int nin = win_off[key + 1] - win_off[key];
+                const bool is_first = (key == fk), is_last = (key == lk);
+                const double Sseg = (is_first || is_last) ? seg_S[key] : Sloc;
+                const double m = __ddiv_rn(Sseg, (double)nin);
+                const double thr = __dmul_rn(VG_EPSILON, fabs(m));
+                double Dr = 0.0, Qr = 0.0;
+                for (int q = k; q < k1; q++) {
+                    const double dwf = __dsub_rn(wf[q], m);
+                    if (fabs(dwf) < thr) {
+                        Qr = __dadd_rn(Qr, __dmul_rn(thr, thr));
+                    } else {
+                        Qr = __dadd_rn(Qr, __dmul_rn(dwf, dwf));
+                        Dr = __dadd_rn(Dr, dwf);
+                    }
+                }
+                if (is_first) dq_first = make_double2(Dr, Qr);
+                if (is_last) dq_last = make_double2(Dr, Qr);
+                if (!is_first && !is_last) {   // hypercube wholly inside this thread
+                    const double nd = (double)nin;
+                    const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(nd, Qr), __dmul_rn(Dr, Dr)),
+                                                __dsub_rn(nd, 1.));
+                    acc_mean.add(__dadd_rn(Sseg, Dr));
+                    acc_var.add(vh);
+                    if (a.adaptive) {
+                        const double sg = pow(fabs(vh), beta_half);
+                        a.sigf[h0 + key] = sg;
+                        acc_sigf.add(sg);
+                    }
+                }
+                k = k1;
+            }
+        }
+        __syncthreads();
+        double2 Pq = seg_scan(flag, dq_last, Pv, wsum, wflag);
+        const double2 carry2 =
+            (tid > 0 && prevL == fk && has) ? Pv[tid - 1] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int which = 0; which < 2; which++) {
+            int key;
+            double2 dq;
+            if (which == 0) {
+                if (!(has && lk != fk)) continue;
+                key = fk;
+                dq = make_double2(dq_first.x + carry2.x, dq_first.y + carry2.y);
+            } else {
+                if (!ends_last) continue;
+                key = lk;
+                dq = Pq;
+            }
+            const int64_t h = h0 + key;
+            const int nin = win_off[key + 1] - win_off[key];
+            const int nh = win_n[key];
+            const double Sseg = seg_S[key];
+            const int64_t ostart = a.offsets[h];
+            const bool starts_before = ostart < tile_start;
+            const bool ends_after = ostart + nh > tile_start + tile_len;
+            if (!starts_before && !ends_after) {
+                const double nd = (double)nin;
+                const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(nd, dq.y), __dmul_rn(dq.x, dq.x)),
+                                            __dsub_rn(nd, 1.));
+                acc_mean.add(__dadd_rn(Sseg, dq.x));
+                acc_var.add(vh);
+                if (a.adaptive) {
+                    const double sg = pow(fabs(vh), beta_half);
+                    a.sigf[h] = sg;
+                    acc_sigf.add(sg);
+                }
+            } else {
+                TileRec r;
+                r.h = h;
+                r.n = (double)nin;
+                r.S = Sseg;
+                r.Q = dq.y;
+                r.D = dq.x;
+                r.spans = (starts_before && ends_after) ? 1 : 0;
+                r.pad = 0;
+                a.recs[2 * tile + (starts_before ? 0 : 1)] = r;
+            }
+        }
+        if (tid == 0) {   // empty record slots
+            const int64_t o0 = a.offsets[h0];
+            if (!(o0 < tile_start)) a.recs[2 * tile].h = -1;
+            int lastkey = nwin - 1;
+            while (lastkey > 0 && win_off[lastkey] >= tile_len) lastkey--;
+            const int64_t hL = h0 + lastkey;
+            const bool tail = (a.offsets[hL] + a.neval_h[hL] > tile_start + tile_len) &&
+                              !(hL == h0 && o0 < tile_start);
+            if (!tail) a.recs[2 * tile + 1].h = -1;
+        }
+        // per-tile totals, fixed-order block reduction
+        VgKSum m = vg_block_ksum<NT>(acc_mean, red);
+        VgKSum v = vg_block_ksum<NT>(acc_var, red);
+        VgKSum s = vg_block_ksum<NT>(acc_sigf, red);
+        if (tid == 0) {
+            TilePart p;
+            p.mean = m;
+            p.var = v;
+            p.sigf = s;
+            a.parts[tile] = p;
+        }
+    }
+
+    // ---- CTA epilogue: NaN flag, histogram flush
+    if (MODE != MODE_POINTS) {
+        if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
+        if (use_bins && a.hist_smem) {
+            __syncthreads();
+            for (int d = 0; d < dim; d++) {
+                const int K = a.ninc[d];
+                for (int i = tid; i < K; i += NT) {
+                    const unsigned int c = hcnt[d * a.maxK + i];
+                    if (c) {
+                        atomicAdd(&a.sum_f[d * a.ldi + i], (double)hsum[d * a.maxK + i]);
+                        atomicAdd(&a.n_f[d * a.ldi + i], (unsigned long long)c);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- launcher
+template <typename T, int MODE, int KIND, int DIMB, int S>
+int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
+{
+    constexpr int TT = NT * S;
+    const int dim = a.dim;
+    a.tab_len = tab_len;
+    a.T = TT;
+    const int bins = (MODE != MODE_POINTS) && a.train;
+    const size_t budget = 200 * 1024;
+    a.table_smem = 1;
+    a.hist_smem = bins;
+    SmemPlan p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+    if (p.total > budget && a.hist_smem) {
+        a.hist_smem = 0;
+        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+    }
+    if (p.total > budget) {
+        a.table_smem = 0;
+        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+    }
+    if (p.total > 227 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
+    auto kern = tile_kernel<T, MODE, KIND, DIMB, S>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        VG_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           227 * 1024));
+        attr_set = true;
+    }
+    int per_sm = 0;
+    VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, p.total));
+    if (per_sm < 1) per_sm = 1;
+    int64_t grid = (int64_t)vg_num_sms() * per_sm;
+    const int64_t tcap = (a.ntiles_cap * BASE_TILE + TT - 1) / TT;
+    if (grid > tcap) grid = tcap;
+    if (grid < 1) grid = 1;
+    static VgParams empty;
+    kern<<<(unsigned)grid, NT, p.total, st>>>(a, prm ? *prm : empty);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
+// Dispatch on the dimension bucket (DIMB) for a given precision/mode/kind.
+template <typename T, int MODE, int KIND>
+int launch_dim(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st);
+
+int finalize_launch(IterArgs &a, cudaStream_t st);
+
+}  // namespace vg
