@@ -687,13 +687,13 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
         a.table_smem = 0;
         p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
     }
-    if (p.total > 227 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
+    if (p.total > 220 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
     auto kern = tile_kernel<T, MODE, KIND, DIMB, S>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static size_t attr_bytes = 0;   // largest dynamic shared memory enabled so far
+    if (p.total > attr_bytes) {
         VG_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           227 * 1024));
-        attr_set = true;
+                                           (int)p.total));
+        attr_bytes = p.total;
     }
     int per_sm = 0;
     VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, p.total));
