@@ -83,6 +83,62 @@ struct VgUniform<float> {
     }
 };
 
+// --------------------------------------------------- fast transcendentals
+// FP32-mode replacements for FP64 pow/log on GB300, whose FP64 rate is about
+// 1/64 of its FP32 rate.  The binary exponent is split off exactly with
+// integer arithmetic, so the full double range is handled; the mantissa's
+// log2 and the fraction's exp2 use the MUFU (ex2/lg2.approx).  Relative
+// error ~2e-6, enough for the allocation weights and grid damping of the FP32
+// mode; the FP64 mode keeps the exact FP64 library functions.
+__device__ __forceinline__ float vg_lg2_approx(float x)
+{
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float vg_ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// log2(x) for finite x > 0 (FP32 result, exact exponent split).
+__device__ __forceinline__ float vg_log2_split(double x)
+{
+    int hi = __double2hiint(x), lo = __double2loint(x);
+    int e = (hi >> 20) & 0x7ff;
+    if (e == 0) {   // subnormal: scale by 2^54
+        x *= 18014398509481984.0;
+        hi = __double2hiint(x);
+        lo = __double2loint(x);
+        e = ((hi >> 20) & 0x7ff) - 54;
+    }
+    double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, lo);   // [1, 2)
+    return (float)(e - 1023) + vg_lg2_approx((float)m);
+}
+
+// 2^p for |p| < 2^24 as a double (0 below the normal range, inf above).
+__device__ __forceinline__ double vg_exp2_split(float p)
+{
+    float fl = floorf(p);
+    float fr = p - fl;                      // [0, 1)
+    int n = (int)fl;
+    double r = (double)vg_ex2_approx(fr);   // [1, 2)
+    if (n < -1021) return 0.0;
+    if (n > 1022) return __longlong_as_double(0x7ff0000000000000LL);
+    long long bits = __double_as_longlong(r) + ((long long)n << 52);
+    return __longlong_as_double(bits);
+}
+
+// x^y for x >= 0 (fast path), falling back to pow for 0, inf and NaN.
+__device__ __forceinline__ double vg_pow_fast(double x, double y)
+{
+    if (!(x > 0.0) || x > 1.7e308) return pow(x, y);
+    return vg_exp2_split((float)y * vg_log2_split(x));
+}
+
 // ------------------------------------------------------- compensated sum
 // Neumaier summation in FP64 for the per-iteration totals.
 struct VgKSum {

@@ -6,9 +6,25 @@
 
 namespace vg {
 
+// Expensive integrands (many exponentials per evaluation) run split: an EVAL
+// kernel without the reduction's shared memory and barriers (higher
+// occupancy for the latency-bound SFU loop) writes f, a REDUCE kernel reads
+// it back.  Cheap integrands run in the single fused kernel.
 template <int KIND>
 int launch_fused_kind(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st)
 {
+    if (!f64 && KIND == VG_F_RIDGE) {
+        int rc;
+        if (a.dim <= 4) rc = launch_tile<float, MODE_EVAL, KIND, 4, 2>(a, &P, tab_len, st);
+        else if (a.dim <= 8) rc = launch_tile<float, MODE_EVAL, KIND, 8, 2>(a, &P, tab_len, st);
+        else if (a.dim <= 16) rc = launch_tile<float, MODE_EVAL, KIND, 16, 2>(a, &P, tab_len, st);
+        else rc = launch_tile<float, MODE_EVAL, KIND, 64, 1>(a, &P, tab_len, st);
+        if (rc) return rc;
+        VG_CUDA_CHECK(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st));
+        a.f_in = a.f_eval;
+        a.f_f64 = 0;
+        return launch_reduce(a, 0, st);
+    }
     if (f64) {
         if (a.dim <= 8) return launch_tile<double, MODE_FUSED, KIND, 8, 2>(a, &P, tab_len, st);
         return launch_tile<double, MODE_FUSED, KIND, 64, 1>(a, &P, tab_len, st);

@@ -180,44 +180,82 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
 
 
 // ========================================================== finalize
-// Chan et al. merge of partial (n, S, Q, D) for hypercubes cut by tiles,
-// then the tile-ordered compensated sums of all per-tile partials.
-__global__ void __launch_bounds__(FIN_NT) finalize_kernel(IterArgs a)
+// Stage 1 (one thread per tile, FIN_TILES tiles per block): the tile's
+// partial sums plus, for a tile whose last hypercube continues into later
+// tiles, the Chan et al. merge of that hypercube's partial records; a
+// fixed-order block reduction gives one partial per block.
+// Stage 2 (one block): those partials in block order -> iteration mean, var,
+// sum_sigf (compensated FP64), and the constant-integrand reset.
+constexpr int FIN_TILES = 128;
+
+template <int FAST>
+__global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
+{
+    __shared__ VgKSum red[FIN_TILES / 32];
+    const vg_stats *st = a.stats;
+    const int64_t N = st->neval;
+    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
+    const int64_t nblk = (ntiles + FIN_TILES - 1) / FIN_TILES;
+    if ((int64_t)blockIdx.x >= nblk) return;
+    const double beta_half = __ddiv_rn(a.beta, 2.0);
+    VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
+    const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
+    if (t < ntiles) {
+        const TilePart p = a.parts[t];
+        cm = p.mean;
+        cv = p.var;
+        cs = p.sigf;
+        const TileRec r = a.recs[2 * t + 1];
+        if (r.h >= 0) {
+            double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
+            for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+                const TileRec q = a.recs[2 * t2];
+                if (q.h != r.h) break;
+                const double n2 = n + q.n;
+                const double delta = q.S / q.n - Sx / n;
+                Q = Q + q.Q + delta * delta * (n * q.n / n2);
+                Sx += q.S;
+                D += q.D;
+                n = n2;
+                if (!q.spans) break;
+            }
+            const double vh =
+                __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
+            cm.add(__dadd_rn(Sx, D));
+            cv.add(vh);
+            if (a.adaptive) {
+                const double sg = FAST ? vg_pow_fast(fabs(vh), beta_half) : pow(fabs(vh), beta_half);
+                a.sigf[r.h] = sg;
+                cs.add(sg);
+            }
+        }
+    }
+    const VgKSum M = vg_block_ksum<FIN_TILES>(cm, red);
+    const VgKSum V = vg_block_ksum<FIN_TILES>(cv, red);
+    const VgKSum Sg = vg_block_ksum<FIN_TILES>(cs, red);
+    if (threadIdx.x == 0) {
+        TilePart p;
+        p.mean = M;
+        p.var = V;
+        p.sigf = Sg;
+        a.part2[blockIdx.x] = p;
+    }
+}
+
+__global__ void __launch_bounds__(FIN_NT) finalize2_kernel(IterArgs a)
 {
     __shared__ VgKSum red[FIN_NT / 32];
     __shared__ int reset;
     const vg_stats *st = a.stats;
     const int64_t N = st->neval;
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    const double beta_half = __ddiv_rn(a.beta, 2.0);
+    const int64_t nblk = (ntiles + FIN_TILES - 1) / FIN_TILES;
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
-    for (int64_t t = threadIdx.x; t < ntiles; t += FIN_NT) {
-        const TilePart p = a.parts[t];
+    for (int64_t b = threadIdx.x; b < nblk; b += FIN_NT) {
+        const TilePart p = a.part2[b];
         cm.merge(p.mean);
         cv.merge(p.var);
         cs.merge(p.sigf);
-        TileRec r = a.recs[2 * t + 1];
-        if (r.h < 0) continue;
-        double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
-        for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
-            const TileRec q = a.recs[2 * t2];
-            if (q.h != r.h) break;
-            const double n2 = n + q.n;
-            const double delta = q.S / q.n - Sx / n;
-            Q = Q + q.Q + delta * delta * (n * q.n / n2);
-            Sx += q.S;
-            D += q.D;
-            n = n2;
-            if (!q.spans) break;
-        }
-        const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
-        cm.add(__dadd_rn(Sx, D));
-        cv.add(vh);
-        if (a.adaptive) {
-            const double sg = pow(fabs(vh), beta_half);
-            a.sigf[r.h] = sg;
-            cs.add(sg);
-        }
     }
     const VgKSum M = vg_block_ksum<FIN_NT>(cm, red);
     const VgKSum V = vg_block_ksum<FIN_NT>(cv, red);
@@ -246,8 +284,9 @@ __global__ void __launch_bounds__(FIN_NT) finalize_kernel(IterArgs a)
 
 // ================================================================ host
 struct WorkLayout {
-    size_t neval_h, offsets, bsum, bmax, tile_h0, counter, recs, parts, newgrid, newinc, total;
-    int64_t nblk, ntiles_cap;
+    size_t neval_h, offsets, bsum, bmax, tile_h0, counter, recs, parts, part2, feval, newgrid,
+        newinc, total;
+    int64_t nblk, ntiles_cap, ncap;
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -277,6 +316,9 @@ WorkLayout layout(const vg_integrator *it, int64_t ncap)
     L.counter = o; o = align256(o + sizeof(unsigned long long));
     L.recs = o;    o = align256(o + sizeof(TileRec) * 2 * L.ntiles_cap);
     L.parts = o;   o = align256(o + sizeof(TilePart) * L.ntiles_cap);
+    L.part2 = o;   o = align256(o + sizeof(TilePart) * (L.ntiles_cap / FIN_TILES + 2));
+    L.feval = o;   o = align256(o + sizeof(float) * ncap);
+    L.ncap = ncap;
     L.newgrid = o; o = align256(o + sizeof(double) * it->dim * it->ldg);
     L.newinc = o;  o = align256(o + sizeof(double) * it->dim * it->ldi);
     L.total = o;
@@ -327,6 +369,8 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     a.counter = (unsigned long long *)(w + L.counter);
     a.recs = (TileRec *)(w + L.recs);
     a.parts = (TilePart *)(w + L.parts);
+    a.part2 = (TilePart *)(w + L.part2);
+    a.f_eval = (float *)(w + L.feval);
     a.ntiles_cap = L.ntiles_cap;
     a.neval = it->neval;
     a.neval_frac = it->neval_frac;
@@ -342,9 +386,15 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
 }  // namespace
 
 namespace vg {
-int finalize_launch(IterArgs &a, cudaStream_t st)
+int finalize_launch(IterArgs &a, cudaStream_t st, int fast)
 {
-    finalize_kernel<<<1, FIN_NT, 0, st>>>(a);
+    // tiles of the launched kernel, bounded by the capacity
+    const int64_t tcap = (a.ntiles_cap * BASE_TILE + a.T - 1) / a.T;
+    const int64_t nblk = (tcap + FIN_TILES - 1) / FIN_TILES;
+    if (fast) finalize1_kernel<1><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
+    else finalize1_kernel<0><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
+    VG_LAUNCH_CHECK();
+    finalize2_kernel<<<1, FIN_NT, 0, st>>>(a);
     VG_LAUNCH_CHECK();
     return VG_OK;
 }
@@ -418,7 +468,7 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = reset_counter(a, st))) return rc;
     if ((rc = vg::launch_reduce(a, it->precision == VG_F64, st))) return rc;
-    return vg::finalize_launch(a, st);
+    return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
 extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, int kind,
@@ -457,13 +507,13 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = reset_counter(a, st))) return rc;
     if ((rc = vg::launch_fused(a, kind, P, tab_len, it->precision == VG_F64, st))) return rc;
-    return vg::finalize_launch(a, st);
+    return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
 int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
                     const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
                     const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
-                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st);
+                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast);
 
 extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
 {
@@ -476,7 +526,8 @@ extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
     double *ng = (double *)(w + L.newgrid);
     double *ni = (double *)(w + L.newinc);
     int rc = vg_adapt_launch(it->dim, it->ninc, it->ninc, it->grid, it->inc, it->ldg, it->ldi,
-                             it->sum_f, it->n_f, it->alpha, ng, ni, it->ldg, it->ldi, st);
+                             it->sum_f, it->n_f, it->alpha, ng, ni, it->ldg, it->ldi, st,
+                             it->precision == VG_F32);
     if (rc) return rc;
     VG_CUDA_CHECK(cudaMemcpyAsync(it->grid, ng, sizeof(double) * it->dim * it->ldg,
                                   cudaMemcpyDeviceToDevice, st));

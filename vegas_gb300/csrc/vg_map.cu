@@ -121,7 +121,28 @@ struct AdaptArgs {
     int64_t ldg_new, ldi_new;
     int max_old;      // length of the shared avg_f buffer (pyx:533)
     int sequential;   // one block walks all axes, carrying avg_f (pyx:533 semantics)
+    int fast;         // FP32 mode: MUFU transcendentals and reciprocal multiplies
 };
+
+// ((1 - v) / -ln v)^alpha of the damping step (pyx:560-562), FP32-mode path:
+// 1 - v and the exponent split in double, logs/exps on the MUFU.
+__device__ __forceinline__ double damp_fast(double v, double alpha)
+{
+    const double one_m = 1.0 - v;
+    float lnv;
+    if (one_m < 0.25) lnv = log1pf((float)(v - 1.0));
+    else lnv = vg_log2_split(v) * 0.69314718055994531f;
+    const float q = (float)one_m / (-lnv);
+    return (double)vg_ex2_approx((float)alpha * vg_lg2_approx(q));
+}
+
+// a / b in double with one Newton step on a float reciprocal (FP32 mode).
+__device__ __forceinline__ double div_fast(double a, double b)
+{
+    double r = (double)(1.0f / (float)b);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+}
 
 constexpr int ADAPT_NT = 1024;
 
@@ -180,8 +201,10 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
     if (alpha != 0 && K > 1) {
         if (a.sum_f != nullptr) {
             for (int i = t; i < K; i += ADAPT_NT) {
-                double nf = __dadd_rn((double)a.n_f[d * a.ldi + i], VG_TINY);
-                avg[i] = (nf > 0) ? __ddiv_rn(a.sum_f[d * a.ldi + i], nf) : 0.0;
+                const unsigned long long c = a.n_f[d * a.ldi + i];
+                const double nf = __dadd_rn((double)c, VG_TINY);
+                if (a.fast) avg[i] = c ? div_fast(a.sum_f[d * a.ldi + i], (double)c) : 0.0;
+                else avg[i] = (nf > 0) ? __ddiv_rn(a.sum_f[d * a.ldi + i], nf) : 0.0;
             }
             __syncthreads();
         }
@@ -197,9 +220,16 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
             __syncthreads();
             double s = block_sum(tmp, K, part);
             // normalise + damp, pyx:554-562
+            const double rs = (s > 0) ? 1.0 / s : 0.0;
             for (int i = t; i < K; i += ADAPT_NT) {
-                double v = (s > 0) ? __dadd_rn(__ddiv_rn(tmp[i], s), VG_TINY) : VG_TINY;
-                if (v > 0 && v <= 0.99999999) v = pow(__ddiv_rn(-(1 - v), log(v)), alpha);
+                double v;
+                if (a.fast) {
+                    v = (s > 0) ? tmp[i] * rs + VG_TINY : VG_TINY;
+                    if (v > 0 && v <= 0.99999999) v = damp_fast(v, alpha);
+                } else {
+                    v = (s > 0) ? __dadd_rn(__ddiv_rn(tmp[i], s), VG_TINY) : VG_TINY;
+                    if (v > 0 && v <= 0.99999999) v = pow(__ddiv_rn(-(1 - v), log(v)), alpha);
+                }
                 avg[i] = v;
             }
             __syncthreads();
@@ -346,7 +376,7 @@ extern "C" int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, i
 int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
                     const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
                     const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
-                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st)
+                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast)
 {
     if (dim < 1 || dim > VG_MAX_DIM) return vg_fail(VG_ERR_UNSUPPORTED, "dim %d", dim);
     AdaptArgs a;
@@ -380,6 +410,7 @@ int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, c
     a.ldg_new = ldg_new;
     a.ldi_new = ldi_new;
     a.max_old = max_old;
+    a.fast = fast;
     if (max_new == 1) {
         adapt_single_kernel<<<1, 64, 0, st>>>(a);
         VG_LAUNCH_CHECK();
@@ -409,5 +440,5 @@ extern "C" int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_nin
 {
     vg_clear_error();
     return vg_adapt_launch(dim, old_ninc, new_ninc, grid, inc, ldg, ldi, sum_f, n_f, alpha,
-                           new_grid, new_inc, ldg_new, ldi_new, (cudaStream_t)stream);
+                           new_grid, new_inc, ldg_new, ldi_new, (cudaStream_t)stream, 0);
 }

@@ -29,7 +29,11 @@ constexpr int ALLOC_NT = 1024;
 constexpr int ALLOC_PER = 4;
 constexpr int FIN_NT = 1024;
 
-enum { MODE_POINTS = 0, MODE_REDUCE = 1, MODE_FUSED = 2 };
+// POINTS: write points for a torch integrand; REDUCE: read f and reduce;
+// FUSED: evaluate a built-in integrand and reduce in one kernel; EVAL:
+// evaluate a built-in integrand and write f (first half of the split path
+// used for expensive integrands, followed by a REDUCE launch).
+enum { MODE_POINTS = 0, MODE_REDUCE = 1, MODE_FUSED = 2, MODE_EVAL = 3 };
 
 // Partial statistics of a hypercube cut by a tile boundary.
 struct TileRec {
@@ -80,6 +84,8 @@ struct IterArgs {
     const void *f_in;         // MODE_REDUCE
     int f_f64;
     void *x_out, *y_out;      // MODE_POINTS
+    float *f_eval;            // MODE_EVAL output / MODE_REDUCE input of the split path
+    TilePart *part2;          // finalize: one partial per finalize block
     double *wgt_out;
     int64_t *hc_out;
     int table_smem;           // grid table staged in shared memory
@@ -106,7 +112,8 @@ struct SmemPlan {
 
 template <typename T>
 __host__ __device__ inline SmemPlan smem_plan(int dim, int maxK, int Ttile, int table_smem,
-                                              int hist_smem, int tab_len, int bins_smem)
+                                              int hist_smem, int tab_len, int bins_smem,
+                                              int need_red)
 {
     SmemPlan p;
     size_t o = 0;
@@ -120,11 +127,11 @@ __host__ __device__ inline SmemPlan smem_plan(int dim, int maxK, int Ttile, int 
     if (bins_smem) o = (o + sizeof(unsigned short) * (size_t)Ttile * dim + 15) & ~(size_t)15;
     p.win_off = o; o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
     p.win_n = o;   o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
-    p.seg_S = o;   o = (o + sizeof(double) * (Ttile + 2) + 15) & ~(size_t)15;
-    p.keyF = o;    o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
-    p.keyL = o;    o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
-    p.P = o;       o = (o + sizeof(double2) * NT + 15) & ~(size_t)15;
-    p.red = o;     o = (o + sizeof(VgKSum) * (NT / 32) * 3 + 64 + 15) & ~(size_t)15;
+    p.seg_S = o;   if (need_red) o = (o + sizeof(double) * (Ttile + 2) + 15) & ~(size_t)15;
+    p.keyF = o;    if (need_red) o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
+    p.keyL = o;    if (need_red) o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
+    p.P = o;       if (need_red) o = (o + sizeof(double2) * NT + 15) & ~(size_t)15;
+    p.red = o;     if (need_red) o = (o + sizeof(VgKSum) * (NT / 32) * 3 + 64 + 15) & ~(size_t)15;
     p.itab = o;    o = (o + sizeof(float) * (tab_len + 4) + 15) & ~(size_t)15;
     p.total = o;
     return p;
@@ -264,9 +271,10 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
     constexpr int KSUB = TT / BASE_TILE;   // base tiles per tile
     const int dim = a.dim;
     const int tid = threadIdx.x;
-    const int use_bins = (MODE != MODE_POINTS) && a.train;
+    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
+    const int use_bins = NEED_RED && a.train;
     const SmemPlan sp = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, a.tab_len,
-                                     use_bins);
+                                     use_bins, NEED_RED);
     GE *table = (GE *)(smem + sp.table);
     T *hsum = (T *)(smem + sp.hsum);
     unsigned int *hcnt = (unsigned int *)(smem + sp.hcnt);
@@ -311,7 +319,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
         }
     }
     VgF32Consts kc;
-    if (MODE == MODE_FUSED && sizeof(T) == 4) {
+    if ((MODE == MODE_FUSED || MODE == MODE_EVAL) && sizeof(T) == 4) {
         kc = vg_prepare_f32<KIND>(prm, dim);
         vg_fill_table_f32<KIND>(prm, dim, itab, kc);
     } else {
@@ -473,8 +481,14 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
         if (MODE == MODE_POINTS) continue;
 
         double fv[S];
-        if (MODE == MODE_FUSED) {
+        if (MODE == MODE_FUSED || MODE == MODE_EVAL) {
             BatchEval<T, KIND, DIMB, S>::run(prm, kc, itab, a.tab_len, dim, xs, fv);
+            if (MODE == MODE_EVAL) {
+#pragma unroll
+                for (int k = 0; k < S; k++)
+                    if (k < nmine) a.f_eval[tile_start + li0 + k] = (float)fv[k];
+                continue;
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < S; k++) {
@@ -569,7 +583,8 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                     acc_mean.add(__dadd_rn(Sseg, Dr));
                     acc_var.add(vh);
                     if (a.adaptive) {
-                        const double sg = pow(fabs(vh), beta_half);
+                        const double sg = (sizeof(T) == 8) ? pow(fabs(vh), beta_half)
+                                                           : vg_pow_fast(fabs(vh), beta_half);
                         a.sigf[h0 + key] = sg;
                         acc_sigf.add(sg);
                     }
@@ -608,7 +623,8 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                 acc_mean.add(__dadd_rn(Sseg, dq.x));
                 acc_var.add(vh);
                 if (a.adaptive) {
-                    const double sg = pow(fabs(vh), beta_half);
+                    const double sg = (sizeof(T) == 8) ? pow(fabs(vh), beta_half)
+                                                       : vg_pow_fast(fabs(vh), beta_half);
                     a.sigf[h] = sg;
                     acc_sigf.add(sg);
                 }
@@ -648,7 +664,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
     }
 
     // ---- CTA epilogue: NaN flag, histogram flush
-    if (MODE != MODE_POINTS) {
+    if (NEED_RED) {
         if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
         if (use_bins && a.hist_smem) {
             __syncthreads();
@@ -674,18 +690,19 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
     const int dim = a.dim;
     a.tab_len = tab_len;
     a.T = TT;
-    const int bins = (MODE != MODE_POINTS) && a.train;
+    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
+    const int bins = NEED_RED && a.train;
     const size_t budget = 200 * 1024;
     a.table_smem = 1;
     a.hist_smem = bins;
-    SmemPlan p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+    SmemPlan p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins, NEED_RED);
     if (p.total > budget && a.hist_smem) {
         a.hist_smem = 0;
-        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins, NEED_RED);
     }
     if (p.total > budget) {
         a.table_smem = 0;
-        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins);
+        p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins, NEED_RED);
     }
     if (p.total > 220 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
     auto kern = tile_kernel<T, MODE, KIND, DIMB, S>;
@@ -712,6 +729,7 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
 template <typename T, int MODE, int KIND>
 int launch_dim(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st);
 
-int finalize_launch(IterArgs &a, cudaStream_t st);
+int finalize_launch(IterArgs &a, cudaStream_t st, int fast);
+int launch_reduce(IterArgs &a, int f64, cudaStream_t st);
 
 }  // namespace vg
