@@ -186,25 +186,28 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
 // fixed-order block reduction gives one partial per block.
 // Stage 2 (one block): those partials in block order -> iteration mean, var,
 // sum_sigf (compensated FP64), and the constant-integrand reset.
-constexpr int FIN_TILES = 128;
+constexpr int FIN_TILES = 32;   // one warp per finalize block: few FP64 lanes per value
 
 template <int FAST>
 __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
 {
-    __shared__ VgKSum red[FIN_TILES / 32];
+    __shared__ VgKSum red[1];
     const vg_stats *st = a.stats;
     const int64_t N = st->neval;
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    const int64_t nblk = (ntiles + FIN_TILES - 1) / FIN_TILES;
+    const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
+    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     if ((int64_t)blockIdx.x >= nblk) return;
     const double beta_half = __ddiv_rn(a.beta, 2.0);
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
     const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
-    if (t < ntiles) {
+    if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
         const TilePart p = a.parts[t];
         cm = p.mean;
         cv = p.var;
         cs = p.sigf;
+    }
+    if (t < ntiles) {   // a hypercube starting in tile t and cut by its end
         const TileRec r = a.recs[2 * t + 1];
         if (r.h >= 0) {
             double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
@@ -242,24 +245,27 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
     }
 }
 
-__global__ void __launch_bounds__(FIN_NT) finalize2_kernel(IterArgs a)
+constexpr int FIN2_NT = 32;
+
+__global__ void __launch_bounds__(FIN2_NT) finalize2_kernel(IterArgs a)
 {
-    __shared__ VgKSum red[FIN_NT / 32];
+    __shared__ VgKSum red[1];
     __shared__ int reset;
     const vg_stats *st = a.stats;
     const int64_t N = st->neval;
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    const int64_t nblk = (ntiles + FIN_TILES - 1) / FIN_TILES;
+    const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
+    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
-    for (int64_t b = threadIdx.x; b < nblk; b += FIN_NT) {
+    for (int64_t b = threadIdx.x; b < nblk; b += FIN2_NT) {
         const TilePart p = a.part2[b];
         cm.merge(p.mean);
         cv.merge(p.var);
         cs.merge(p.sigf);
     }
-    const VgKSum M = vg_block_ksum<FIN_NT>(cm, red);
-    const VgKSum V = vg_block_ksum<FIN_NT>(cv, red);
-    const VgKSum Sg = vg_block_ksum<FIN_NT>(cs, red);
+    const VgKSum M = vg_block_ksum<FIN2_NT>(cm, red);
+    const VgKSum V = vg_block_ksum<FIN2_NT>(cv, red);
+    const VgKSum Sg = vg_block_ksum<FIN2_NT>(cs, red);
     if (threadIdx.x == 0) {
         vg_stats *s = a.stats;
         s->mean = M.value();
@@ -279,7 +285,7 @@ __global__ void __launch_bounds__(FIN_NT) finalize2_kernel(IterArgs a)
     }
     __syncthreads();
     if (reset)
-        for (int64_t h = threadIdx.x; h < a.H; h += FIN_NT) a.sigf[h] = 1.0;
+        for (int64_t h = threadIdx.x; h < a.H; h += FIN2_NT) a.sigf[h] = 1.0;
 }
 
 // ================================================================ host
@@ -316,7 +322,7 @@ WorkLayout layout(const vg_integrator *it, int64_t ncap)
     L.counter = o; o = align256(o + sizeof(unsigned long long));
     L.recs = o;    o = align256(o + sizeof(TileRec) * 2 * L.ntiles_cap);
     L.parts = o;   o = align256(o + sizeof(TilePart) * L.ntiles_cap);
-    L.part2 = o;   o = align256(o + sizeof(TilePart) * (L.ntiles_cap / FIN_TILES + 2));
+    L.part2 = o;   o = align256(o + sizeof(TilePart) * (L.ntiles_cap / FIN_TILES + 4096 / FIN_TILES + 2));
     L.feval = o;   o = align256(o + sizeof(float) * ncap);
     L.ncap = ncap;
     L.newgrid = o; o = align256(o + sizeof(double) * it->dim * it->ldg);
@@ -390,11 +396,12 @@ int finalize_launch(IterArgs &a, cudaStream_t st, int fast)
 {
     // tiles of the launched kernel, bounded by the capacity
     const int64_t tcap = (a.ntiles_cap * BASE_TILE + a.T - 1) / a.T;
-    const int64_t nblk = (tcap + FIN_TILES - 1) / FIN_TILES;
+    const int64_t nwork = tcap > a.ncta ? tcap : a.ncta;
+    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     if (fast) finalize1_kernel<1><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
     else finalize1_kernel<0><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
     VG_LAUNCH_CHECK();
-    finalize2_kernel<<<1, FIN_NT, 0, st>>>(a);
+    finalize2_kernel<<<1, FIN2_NT, 0, st>>>(a);
     VG_LAUNCH_CHECK();
     return VG_OK;
 }

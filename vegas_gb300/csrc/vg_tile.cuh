@@ -93,6 +93,7 @@ struct IterArgs {
     int maxK;
     int tab_len;              // integrand table length (floats)
     int T;                    // tile size of the launched kernel
+    int ncta;                 // CTAs of the launched reduction kernel (one partial each)
 };
 
 template <typename T>
@@ -261,6 +262,17 @@ struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
     }
 };
 
+// a / b: exact in FP64 mode (reference parity), a reciprocal multiply refined
+// by one Newton step in FP32 mode (GB300 FP64 division is expensive).
+template <typename T>
+__device__ __forceinline__ double vg_div(double a, double b)
+{
+    if (sizeof(T) == 8) return __ddiv_rn(a, b);
+    double r = (double)(1.0f / (float)b);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+}
+
 // ------------------------------------------------------------------ kernel
 template <typename T, int MODE, int KIND, int DIMB, int S>
 __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
@@ -328,12 +340,24 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
     const double dv_y = __ddiv_rn(1.0, (double)a.H);
     const double beta_half = __ddiv_rn(a.beta, 2.0);
     int nan_local = 0;
+    // per-thread running sums over every hypercube this thread finalises
+    double acc_m = 0.0, acc_v = 0.0, acc_s = 0.0;
+    int64_t next_static = blockIdx.x;
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) s_tile = (int64_t)atomicAdd(a.counter, 1ull);
-        __syncthreads();
-        const int64_t tile = s_tile;
+        int64_t tile;
+        if (NEED_RED) {
+            // reduction modes: fixed tile -> CTA assignment, so the per-CTA
+            // partial sums (and hence the result) are deterministic
+            tile = next_static;
+            next_static += gridDim.x;
+        } else {
+            // evaluation-only modes: dynamic tiles for load balance
+            if (tid == 0) s_tile = (int64_t)atomicAdd(a.counter, 1ull);
+            __syncthreads();
+            tile = s_tile;
+        }
         if (tile >= ntiles) break;
         const int64_t tile_start = tile * (int64_t)TT;
         const int tile_len = (int)min((int64_t)TT, N - tile_start);
@@ -506,20 +530,33 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
             wf[k] = 0.0;
             if (k >= nmine) continue;
             if (fv[k] != fv[k]) nan_local = 1;
-            const double w1 = __dmul_rn(wg[k], fv[k]);   // wgt * f, pyx:2143
+            double w1;
+            float wf32 = 0.f;
+            if (sizeof(T) == 8) {
+                w1 = __dmul_rn(wg[k], fv[k]);   // wgt * f, pyx:2143
+            } else {
+                wf32 = (float)wg[k] * (float)fv[k];
+                w1 = (double)wf32;
+            }
             wf[k] = w1;
             if (use_bins) {
                 // fdv2 = (wgt*f*neval)^2, pyx:2173; |fdv2| into the bins, pyx:460-463
-                const double t1 = __dmul_rn(w1, (double)win_n[lhs[k]]);
-                const double fd = __dmul_rn(t1, t1);
+                T fd;
+                if (sizeof(T) == 8) {
+                    const double t1 = __dmul_rn(w1, (double)win_n[lhs[k]]);
+                    fd = (T)__dmul_rn(t1, t1);
+                } else {
+                    const float t1 = wf32 * (float)win_n[lhs[k]];
+                    fd = (T)(t1 * t1);
+                }
                 for (int d = 0; d < dim; d++) {
                     const unsigned short b = sbins[(li0 + k) * dim + d];
                     if (b == 0xffff) continue;
                     if (a.hist_smem) {
-                        atomicAdd(&hsum[d * a.maxK + b], (T)fd);
+                        atomicAdd(&hsum[d * a.maxK + b], fd);
                         atomicAdd(&hcnt[d * a.maxK + b], 1u);
                     } else {
-                        atomicAdd(&a.sum_f[d * a.ldi + b], fd);
+                        atomicAdd(&a.sum_f[d * a.ldi + b], (double)fd);
                         atomicAdd(&a.n_f[d * a.ldi + b], 1ull);
                     }
                 }
@@ -547,7 +584,6 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
         const int ends_last = has && (lk != nextF);
         if (has && lk != fk) seg_S[fk] = fsum + carry1;
         if (ends_last) seg_S[lk] = Pi.x;
-        VgKSum acc_mean = {0.0, 0.0}, acc_var = {0.0, 0.0}, acc_sigf = {0.0, 0.0};
         __syncthreads();
 
         // ---- pass 2: deviations about the hypercube mean (pyx:2154-2171)
@@ -562,7 +598,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                 const int nin = win_off[key + 1] - win_off[key];
                 const bool is_first = (key == fk), is_last = (key == lk);
                 const double Sseg = (is_first || is_last) ? seg_S[key] : Sloc;
-                const double m = __ddiv_rn(Sseg, (double)nin);
+                const double m = vg_div<T>(Sseg, (double)nin);
                 const double thr = __dmul_rn(VG_EPSILON, fabs(m));
                 double Dr = 0.0, Qr = 0.0;
                 for (int q = k; q < k1; q++) {
@@ -578,15 +614,15 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                 if (is_last) dq_last = make_double2(Dr, Qr);
                 if (!is_first && !is_last) {   // hypercube wholly inside this thread
                     const double nd = (double)nin;
-                    const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(nd, Qr), __dmul_rn(Dr, Dr)),
+                    const double vh = vg_div<T>(__dsub_rn(__dmul_rn(nd, Qr), __dmul_rn(Dr, Dr)),
                                                 __dsub_rn(nd, 1.));
-                    acc_mean.add(__dadd_rn(Sseg, Dr));
-                    acc_var.add(vh);
+                    acc_m += __dadd_rn(Sseg, Dr);
+                    acc_v += vh;
                     if (a.adaptive) {
                         const double sg = (sizeof(T) == 8) ? pow(fabs(vh), beta_half)
                                                            : vg_pow_fast(fabs(vh), beta_half);
                         a.sigf[h0 + key] = sg;
-                        acc_sigf.add(sg);
+                        acc_s += sg;
                     }
                 }
                 k = k1;
@@ -618,15 +654,15 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
             const bool ends_after = ostart + nh > tile_start + tile_len;
             if (!starts_before && !ends_after) {
                 const double nd = (double)nin;
-                const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(nd, dq.y), __dmul_rn(dq.x, dq.x)),
+                const double vh = vg_div<T>(__dsub_rn(__dmul_rn(nd, dq.y), __dmul_rn(dq.x, dq.x)),
                                             __dsub_rn(nd, 1.));
-                acc_mean.add(__dadd_rn(Sseg, dq.x));
-                acc_var.add(vh);
+                acc_m += __dadd_rn(Sseg, dq.x);
+                acc_v += vh;
                 if (a.adaptive) {
                     const double sg = (sizeof(T) == 8) ? pow(fabs(vh), beta_half)
                                                        : vg_pow_fast(fabs(vh), beta_half);
                     a.sigf[h] = sg;
-                    acc_sigf.add(sg);
+                    acc_s += sg;
                 }
             } else {
                 TileRec r;
@@ -650,21 +686,22 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                               !(hL == h0 && o0 < tile_start);
             if (!tail) a.recs[2 * tile + 1].h = -1;
         }
-        // per-tile totals, fixed-order block reduction
-        VgKSum m = vg_block_ksum<NT>(acc_mean, red);
-        VgKSum v = vg_block_ksum<NT>(acc_var, red);
-        VgKSum s = vg_block_ksum<NT>(acc_sigf, red);
+    }
+
+    // ---- CTA epilogue: partial sums (one compensated block reduction),
+    // NaN flag, histogram flush
+    if (NEED_RED) {
+        __syncthreads();
+        const VgKSum m = vg_block_ksum<NT>(VgKSum{acc_m, 0.0}, red);
+        const VgKSum v = vg_block_ksum<NT>(VgKSum{acc_v, 0.0}, red);
+        const VgKSum sg = vg_block_ksum<NT>(VgKSum{acc_s, 0.0}, red);
         if (tid == 0) {
             TilePart p;
             p.mean = m;
             p.var = v;
-            p.sigf = s;
-            a.parts[tile] = p;
+            p.sigf = sg;
+            a.parts[blockIdx.x] = p;
         }
-    }
-
-    // ---- CTA epilogue: NaN flag, histogram flush
-    if (NEED_RED) {
         if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
         if (use_bins && a.hist_smem) {
             __syncthreads();
@@ -719,6 +756,8 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
     const int64_t tcap = (a.ntiles_cap * BASE_TILE + TT - 1) / TT;
     if (grid > tcap) grid = tcap;
     if (grid < 1) grid = 1;
+    if (NEED_RED && grid > a.ntiles_cap) grid = a.ntiles_cap;
+    a.ncta = (int)grid;
     static VgParams empty;
     kern<<<(unsigned)grid, NT, p.total, st>>>(a, prm ? *prm : empty);
     VG_LAUNCH_CHECK();
