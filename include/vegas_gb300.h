@@ -193,6 +193,28 @@ int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, i
  */
 int vg_end_iteration(const vg_integrator *it, void *stream);
 
+/*
+ * One vegas+ iteration (allocation, fused evaluation + reduction, adapt) for
+ * a built-in integrand that allocates no device memory.  No counterpart in
+ * the reference: it exists for callers that cannot allocate device memory --
+ * plug-ins whose host application owns all device memory through its own
+ * pool, services under a hard device-memory budget, callers that must not
+ * allocate on their iteration path.  The caller still provides the
+ * integrator's inputs and outputs (grid, inc, sigf, training histogram,
+ * stats); it->work / it->work_bytes are ignored.  Scratch is a static device
+ * array of VG_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
+ * until the process exits; an iteration whose vg_workspace_bytes() exceeds it
+ * fails with VG_ERR_MEMORY.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array: calls that overlap on the
+ * GPU (other streams, other threads) race and must be serialised by the
+ * caller.  Every scratch region is rewritten before it is read; the tile
+ * counter is zeroed on every call.
+ */
+#define VG_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const double *u, int kind,
+                         const double *params, int nparams, void *stream);
+
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);

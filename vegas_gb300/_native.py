@@ -26,6 +26,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr']
 
 VG_MAX_DIM = 64
+VG_NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 VG_F32, VG_F64 = 0, 1
 VG_OK, VG_ERR_VALUE, VG_ERR_MEMORY, VG_ERR_CUDA, VG_ERR_NAN, VG_ERR_UNSUPPORTED, VG_ERR_TIMEOUT = range(7)
 (VG_F_GAUSS, VG_F_RIDGE, VG_F_LORENTZ, VG_F_MIXTURE, VG_F_LATTICE, VG_F_CONST) = range(6)
@@ -135,6 +136,7 @@ SIGNATURES = {
     'vg_reduce': (I32, [P, U32, P, P, I32, P]),
     'vg_fused_iteration': (I32, [P, U32, P, I32, P, I32, P]),
     'vg_end_iteration': (I32, [P, P]),
+    'vg_iteration_noalloc': (I32, [P, U32, P, I32, P, I32, P]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),
