@@ -215,6 +215,46 @@ int vg_end_iteration(const vg_integrator *it, void *stream);
 int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const double *u, int kind,
                          const double *params, int nparams, void *stream);
 
+/* ------------------------------------------------------ learned proposal */
+/*
+ * Coupling-layer normalising flow with piecewise-quadratic transforms on the
+ * unit cube (no counterpart in the reference: vegas has no learned
+ * proposal).  It is composed after the AdaptiveMap: vegas samples zhat in the
+ * unit cube, the flow maps it to z, the integration box maps z to x.
+ * Parameters theta follow the layout of the FP64 checker
+ * (oracle/flow_oracle.py); `mirror` holds BF16 copies of the dense layers for
+ * the tensor cores (vg_flow_mirror_elems() 16-bit elements, rebuilt by
+ * vg_flow_refresh after any change of theta).
+ */
+typedef struct vg_flow {
+    int32_t dim, nlayers, K, hidden;   /* dim <= 16, nlayers <= 8, K <= 64, hidden == 128 */
+    float *theta;                      /* [nparams] FP32 parameters                       */
+    void *mirror;                      /* BF16 dense-layer copies                          */
+    float *grad;                       /* [nparams] gradient accumulator (caller zeroes)   */
+    float *adam_m, *adam_v;            /* [nparams] Adam moments                           */
+    double *loss;                      /* [1] accumulated -sum w logdet                    */
+} vg_flow;
+
+int64_t vg_flow_nparams(int dim, int nlayers, int K, int hidden);
+int64_t vg_flow_mirror_elems(int dim, int nlayers, int K, int hidden);
+/* Workspace of vg_flow_grad for n rows (bytes). */
+int64_t vg_flow_train_bytes(const vg_flow *fl, int64_t n);
+int vg_flow_refresh(const vg_flow *fl, void *stream);
+/* Sampling direction: zhat[n,dim] -> z[n,dim]; logdet[n] = sum log pdf, so
+ * log|dz/dzhat| = -logdet. */
+int vg_flow_sample(const vg_flow *fl, int64_t n, const float *zhat, float *z, float *logdet,
+                   void *stream);
+/* Density direction: z -> zhat, logdet = log q_flow(z). */
+int vg_flow_density(const vg_flow *fl, int64_t n, const float *z, float *zhat, float *logdet,
+                    void *stream);
+/* Gradient of loss = -sum_i w_i logdet(z_i) w.r.t. theta, accumulated into fl->grad
+ * (and the loss into fl->loss): forward and backward kernels, BF16 MMAs. */
+int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const float *w, void *work,
+                 size_t work_bytes, void *stream);
+/* Adam step on theta with gradient grad*scale (clipped at +-clip), then refresh. */
+int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta1, float beta2, float eps,
+                 int step, float clip, void *stream);
+
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);

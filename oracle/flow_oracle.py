@@ -29,6 +29,24 @@ import torch
 EPS_W = 1e-3   # minimum bin width fraction: W = EPS_W + (1 - K*EPS_W) softmax
 
 
+def init_theta(dim, nlayers=6, K=32, hidden=128, seed=0, scale=1.0, out_scale=0.0):
+    """Initial parameters: He-scaled W1, W2; W3 = out_scale * N(0, 1/hidden) (0 gives the
+    identity transform: equal bin widths and heights)."""
+    rng = np.random.default_rng(seed)
+    theta = np.zeros(nparams(dim, nlayers, K, hidden), np.float32)
+    o = 0
+    for s in layer_sizes(dim, nlayers, K, hidden):
+        for name, fan in (('W1', s['dA']), ('b1', 0), ('W2', hidden), ('b2', 0),
+                          ('W3', hidden), ('b3', 0)):
+            n = s[name]
+            if name == 'W3':
+                theta[o:o + n] = out_scale * rng.normal(0, 1 / math.sqrt(fan), n)
+            elif fan:
+                theta[o:o + n] = scale * rng.normal(0, math.sqrt(2.0 / fan), n)
+            o += n
+    return theta
+
+
 def masks(dim, nlayers):
     """(A, B) index lists per layer: bit b = (l//2) % nbits of the index,
     B = indices whose bit equals l % 2."""
@@ -115,10 +133,17 @@ def spline_inverse(c, wlog, vlog, K):
     return x, torch.log(pdf)
 
 
+BF16 = False   # emulate the GPU's BF16 operands of the two MMA layers
+
+
+def _bf16(t):
+    return t.to(torch.bfloat16).to(t.dtype) if BF16 else t
+
+
 def conditioner(L, xA):
-    h1 = torch.relu(xA @ L['W1'].T + L['b1'])
-    h2 = torch.relu(h1 @ L['W2'].T + L['b2'])
-    return h2 @ L['W3'].T + L['b3']
+    h1 = _bf16(torch.relu(xA @ L['W1'].T + L['b1']))
+    h2 = _bf16(torch.relu(h1 @ _bf16(L['W2']).T + L['b2']))
+    return h2 @ _bf16(L['W3']).T + L['b3']
 
 
 def density_pass(theta, x, dim, nlayers=6, K=32, hidden=128):

@@ -1,0 +1,187 @@
+"""Coupling-layer flow: the FP64 oracle on its own (CPU) and the GPU kernels
+against it (GPU).
+
+Tolerances of the GPU kernels (BF16 operands with FP32 accumulation in the
+two dense layers, FP32 spline), against the oracle run with the same BF16
+rounding of activations and weights:
+  sampling / density outputs z:      |dz| <= 2e-3 absolute
+  logdet:                            |d logdet| <= 2e-2 absolute (6 layers)
+  round trip density(sample(zhat)):  |d zhat| <= 2e-3
+  gradient of the training loss:     relative L2 error <= 3e-2 and
+                                     cosine similarity >= 0.999
+(the backward rounds dL/dout, dL/dh2 and dL/dh1 to BF16 for the tensor-core
+weight-gradient GEMMs).
+"""
+import numpy as np
+import pytest
+import torch
+
+import flow_oracle as F
+from vegas_gb300 import _native as N
+
+
+def _theta(dim, nlayers=6, K=32, hidden=128, seed=1, out_scale=0.5):
+    return F.init_theta(dim, nlayers, K, hidden, seed=seed, out_scale=out_scale)
+
+
+# ------------------------------------------------------------------ oracle
+def test_oracle_identity_at_zero_output_layer():
+    x = torch.rand(100, 4, dtype=torch.float64)
+    th = torch.tensor(F.init_theta(4, out_scale=0.0), dtype=torch.float64)
+    z, ld = F.density_pass(th, x, 4)
+    assert torch.allclose(z, x, atol=1e-12)
+    assert float(ld.abs().max()) < 1e-12
+
+
+@pytest.mark.parametrize('dim', [1, 3, 4])
+def test_oracle_inverse_and_logdet(dim):
+    torch.manual_seed(0)
+    th = torch.tensor(_theta(dim, K=8, hidden=16), dtype=torch.float64)
+    xhat = torch.rand(200, dim, dtype=torch.float64)
+    x, ld_s = F.sample_pass(th, xhat, dim, K=8, hidden=16)
+    xb, ld_d = F.density_pass(th, x, dim, K=8, hidden=16)
+    assert float((xb - xhat).abs().max()) < 1e-10
+    assert float((ld_s - ld_d).abs().max()) < 1e-9
+
+
+def test_oracle_logdet_is_log_jacobian():
+    """logdet(x) = log |det d xhat / d x| (autograd Jacobian)."""
+    dim = 3
+    th = torch.tensor(_theta(dim, K=6, hidden=8), dtype=torch.float64)
+    x = torch.rand(5, dim, dtype=torch.float64)
+    _, ld = F.density_pass(th, x, dim, K=6, hidden=8)
+    for i in range(5):
+        J = torch.autograd.functional.jacobian(
+            lambda v: F.density_pass(th, v.unsqueeze(0), dim, K=6, hidden=8)[0][0], x[i])
+        assert abs(float(torch.logdet(J)) - float(ld[i])) < 1e-9
+
+
+def test_oracle_density_normalised():
+    """q_flow integrates to 1 on the unit cube (midpoint rule, dim 2)."""
+    dim = 2
+    th = torch.tensor(_theta(dim, K=8, hidden=16), dtype=torch.float64)
+    m = 400
+    g = (torch.arange(m, dtype=torch.float64) + 0.5) / m
+    x = torch.stack(torch.meshgrid(g, g, indexing='ij'), -1).reshape(-1, 2)
+    _, ld = F.density_pass(th, x, dim, K=8, hidden=16)
+    assert abs(float(torch.exp(ld).mean()) - 1.0) < 1e-3
+
+
+def test_oracle_gradient_finite_difference():
+    dim = 3
+    theta = _theta(dim, nlayers=2, K=4, hidden=8).astype(np.float64)
+    rng = np.random.default_rng(0)
+    x = rng.random((50, dim))
+    w = rng.random(50) + 0.1
+    loss, g = F.loss_and_grad(theta, x, w, dim, nlayers=2, K=4, hidden=8)
+    for i in rng.choice(len(theta), 20, replace=False):
+        e = np.zeros_like(theta)
+        e[i] = 1e-6
+        lp, _ = F.loss_and_grad(theta + e, x, w, dim, nlayers=2, K=4, hidden=8)
+        lm, _ = F.loss_and_grad(theta - e, x, w, dim, nlayers=2, K=4, hidden=8)
+        assert abs((lp - lm) / 2e-6 - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+def test_library_layout_matches_oracle():
+    L = N.load()
+    for dim in (1, 2, 3, 4, 8, 16):
+        for K in (8, 32, 48):
+            assert L.vg_flow_nparams(dim, 6, K, 128) == F.nparams(dim, 6, K, 128)
+    assert L.vg_flow_nparams(17, 6, 32, 128) == -1
+    assert L.vg_flow_nparams(4, 6, 32, 64) == -1
+
+
+# --------------------------------------------------------------------- GPU
+def _gpu_flow(dim, theta, K=32):
+    from vegas_gb300.flow import Flow
+    fl = Flow(dim, nlayers=6, K=K, hidden=128)
+    fl.set_theta(theta)
+    return fl
+
+
+def _oracle_bf16(fn, *args, **kw):
+    F.BF16 = True
+    try:
+        return fn(*args, **kw)
+    finally:
+        F.BF16 = False
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dim', [1, 3, 4, 8])
+def test_gpu_flow_passes_vs_oracle(dim):
+    theta = _theta(dim)
+    fl = _gpu_flow(dim, theta)
+    torch.manual_seed(dim)
+    n = 1000
+    u = torch.rand(n, dim, dtype=torch.float32)
+    th64 = torch.tensor(theta, dtype=torch.float64)
+    # sampling direction
+    z, ld = fl.sample(u.cuda())
+    zo, ldo = _oracle_bf16(F.sample_pass, th64, u.double(), dim)
+    assert float((z.cpu().double() - zo).abs().max()) <= 2e-3
+    assert float((ld.cpu().double() - ldo).abs().max()) <= 2e-2
+    # density direction at the oracle's points
+    zh, ld2 = fl.density(zo.float().cuda())
+    zho, ld2o = _oracle_bf16(F.density_pass, th64, zo, dim)
+    assert float((zh.cpu().double() - zho).abs().max()) <= 2e-3
+    assert float((ld2.cpu().double() - ld2o).abs().max()) <= 2e-2
+    # round trip on the GPU
+    zh2, ld3 = fl.density(z)
+    assert float((zh2 - u.cuda()).abs().max()) <= 2e-3
+    assert float((ld3 - ld).abs().max()) <= 2e-2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dim', [3, 4, 8])
+def test_gpu_flow_gradient_vs_oracle(dim):
+    theta = _theta(dim, seed=2, out_scale=0.3)
+    fl = _gpu_flow(dim, theta)
+    rng = np.random.default_rng(dim)
+    n = 777   # ragged: not a multiple of the 128-row tile
+    x = rng.random((n, dim)).astype(np.float32)
+    w = (rng.random(n) ** 3 + 0.01).astype(np.float32)
+    fl.grad.zero_()
+    fl.loss.zero_()
+    fl.accumulate_grad(torch.from_numpy(x).cuda(), torch.from_numpy(w).cuda())
+    g = fl.grad.cpu().double().numpy() / w.astype(np.float64).sum()
+    loss = float(fl.loss.item()) / w.astype(np.float64).sum()
+    lo, go = _oracle_bf16(F.loss_and_grad, theta, x.astype(np.float64), w.astype(np.float64), dim)
+    assert abs(loss - lo) <= 1e-3 * max(1.0, abs(lo))
+    err = np.linalg.norm(g - go) / np.linalg.norm(go)
+    cos = float(g @ go / (np.linalg.norm(g) * np.linalg.norm(go)))
+    assert err <= 3e-2, err
+    assert cos >= 0.999, cos
+
+
+@pytest.mark.gpu
+def test_gpu_flow_training_learns_a_bump():
+    """Adam steps on samples of a narrow off-diagonal 2-bump target reduce
+    the variance of f/q by a large factor."""
+    from vegas_gb300.flow import Flow
+    dim = 4
+    dev = torch.device('cuda')
+    c = torch.tensor([[0.3, 0.7, 0.4, 0.6], [0.7, 0.3, 0.6, 0.4]], device=dev)
+
+    def f(x):
+        d2 = ((x.unsqueeze(1) - c) ** 2).sum(-1)
+        return torch.exp(-d2 / (2 * 0.05 ** 2)).sum(1)
+
+    fl = Flow(dim, lr=3e-3, seed=3)
+    gen = torch.Generator(device=dev).manual_seed(0)
+
+    def var_per_eval(n=1 << 16):
+        u = torch.rand(n, dim, device=dev, generator=gen)
+        z, ld = fl.sample(u)
+        r = f(z) * torch.exp(-ld)
+        return float(r.var() / r.mean() ** 2)
+
+    v0 = var_per_eval()
+    for it in range(300):
+        u = torch.rand(4096, dim, device=dev, generator=gen)
+        with torch.no_grad():
+            z, ld = fl.sample(u)
+            w = (f(z) * torch.exp(-ld)) ** 2    # (f/q)^2 with q(z) = exp(logdet(z))
+        fl.train_step(z, w)
+    v1 = var_per_eval()
+    assert v1 < v0 / 5, (v0, v1)

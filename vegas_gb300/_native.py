@@ -114,6 +114,15 @@ class VgIntegrator(ctypes.Structure):
     ]
 
 
+class VgFlow(ctypes.Structure):
+    _fields_ = [
+        ('dim', ctypes.c_int32), ('nlayers', ctypes.c_int32), ('K', ctypes.c_int32),
+        ('hidden', ctypes.c_int32), ('theta', ctypes.c_void_p), ('mirror', ctypes.c_void_p),
+        ('grad', ctypes.c_void_p), ('adam_m', ctypes.c_void_p), ('adam_v', ctypes.c_void_p),
+        ('loss', ctypes.c_void_p),
+    ]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -137,6 +146,15 @@ SIGNATURES = {
     'vg_fused_iteration': (I32, [P, U32, P, I32, P, I32, P]),
     'vg_end_iteration': (I32, [P, P]),
     'vg_iteration_noalloc': (I32, [P, U32, P, I32, P, I32, P]),
+    'vg_flow_nparams': (I64, [I32, I32, I32, I32]),
+    'vg_flow_mirror_elems': (I64, [I32, I32, I32, I32]),
+    'vg_flow_train_bytes': (I64, [P, I64]),
+    'vg_flow_refresh': (I32, [P, P]),
+    'vg_flow_sample': (I32, [P, I64, P, P, P, P]),
+    'vg_flow_density': (I32, [P, I64, P, P, P, P]),
+    'vg_flow_grad': (I32, [P, I64, P, P, P, SZ, P]),
+    'vg_flow_adam': (I32, [P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, I32, ctypes.c_float, P]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),

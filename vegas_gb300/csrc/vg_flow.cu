@@ -1,0 +1,956 @@
+// vg_flow.cu -- learned proposal: a coupling-layer normalising flow with
+// piecewise-quadratic transforms (Mueller et al., "Neural Importance
+// Sampling", ACM TOG 2019), composed after the AdaptiveMap.  No reference
+// counterpart: the reference vegas has no learned proposal.
+//
+// The flow lives on the unit cube.  Density direction (training): z (sample)
+// -> layer 0 CDF -> ... -> layer L-1 CDF -> zhat, logdet = sum log pdf.
+// Sampling direction: zhat -> inverse CDFs L-1..0 -> z, log|dz/dzhat| =
+// -logdet.  Conditioner of layer l: out = W3 relu(W2 relu(W1 z_A + b1) + b2)
+// + b3; per transformed coordinate j, out[j(2K+1) + k] are K width logits and
+// out[j(2K+1) + K + k] K+1 vertex logits.  Parameter layout, masks and spline
+// match oracle/flow_oracle.py (the FP64 checker).
+//
+// Kernels (CTA = 256 threads = 8 warps, 128 rows per tile):
+//   flow_pass_kernel    sampling or density pass through all layers (inference)
+//   flow_fwd_kernel     training forward: density pass storing each layer input
+//   flow_bwd_kernel     training backward of one layer: recompute activations,
+//                       spline backward, dOUT/dH2/dH1 through the MLP, write
+//                       the transposed activations/gradients the weight
+//                       gradients need
+//   flow_wgrad_kernel   weight gradients dW = dY^T X over the batch as split-K
+//                       GEMMs (K = batch rows) + flow_wgrad_reduce_kernel
+//   flow_adam_kernel    Adam update of the FP32 parameters
+//   flow_mirror_kernel  BF16 copies of W2, W3 (and transposes) for the MMAs
+// The 128x128 hidden layer and the output layer run on the tensor cores as
+// BF16 mma.sync.m16n8k16 with FP32 accumulation.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <string.h>
+
+#include "vg_common.cuh"
+
+namespace {
+
+constexpr int FH = 128;           // hidden width (fixed)
+constexpr int FROWS = 128;        // rows per tile
+constexpr int FNT = 256;          // threads per CTA
+constexpr int FMAXD = 16;         // maximum dimension
+constexpr int FMAXL = 8;          // maximum layers
+constexpr int FMAXK = 48;         // maximum bins (shared-memory bound of the backward)
+constexpr int HSTR = FH + 8;      // padded row stride (bf16) of hidden activations
+constexpr float EPS_W = 1e-3f;    // minimum bin width fraction (oracle EPS_W)
+constexpr size_t VG_FLOW_SMEM_MAX = 227 * 1024;   // dynamic shared memory per CTA
+
+struct FlowLayer {
+    int dA, dB, P;                 // conditioning / transformed dims, outputs
+    int A[FMAXD], B[FMAXD];
+    int64_t oW1, ob1, oW2, ob2, oW3, ob3;   // offsets into theta
+    int64_t mW2, mW2t, mW3, mW3t;           // offsets (elements) into the bf16 mirror
+    int realA;                     // 0 when the layer conditions on nothing
+};
+
+struct FlowGeom {
+    int dim, L, K, CH;             // CH = per-coordinate output chunk rows (2K+1 padded to 8)
+    int CHK;                       // CH padded to a multiple of 16 (K dim of dOUT . W3)
+    FlowLayer ly[FMAXL];
+    int64_t nparams, nmirror;
+};
+
+// masks: bit b = (l/2) % nbits of the coordinate index; B = bit == l % 2
+int make_geom(FlowGeom &g, int dim, int L, int K, int hidden)
+{
+    memset(&g, 0, sizeof(g));
+    if (dim < 1 || dim > FMAXD) return vg_fail(VG_ERR_UNSUPPORTED, "flow dim %d (1..%d)", dim, FMAXD);
+    if (L < 1 || L > FMAXL) return vg_fail(VG_ERR_UNSUPPORTED, "flow layers %d (1..%d)", L, FMAXL);
+    if (K < 2 || K > FMAXK) return vg_fail(VG_ERR_UNSUPPORTED, "flow bins %d (2..%d)", K, FMAXK);
+    if (hidden != FH) return vg_fail(VG_ERR_UNSUPPORTED, "flow hidden width must be %d", FH);
+    g.dim = dim;
+    g.L = L;
+    g.K = K;
+    g.CH = ((2 * K + 1) + 7) / 8 * 8;
+    g.CHK = (g.CH + 15) / 16 * 16;
+    int nbits = 1;
+    while ((1 << nbits) < dim) nbits++;
+    int64_t o = 0, m = 0;
+    for (int l = 0; l < L; l++) {
+        FlowLayer &y = g.ly[l];
+        int b = (l / 2) % nbits;
+        y.dA = y.dB = 0;
+        for (int i = 0; i < dim; i++) {
+            if (((i >> b) & 1) == (l % 2)) y.B[y.dB++] = i;
+            else y.A[y.dA++] = i;
+        }
+        y.realA = 1;
+        if (y.dA == 0 || y.dB == 0) {   // dim 1: condition on nothing
+            y.dA = 0;
+            y.dB = dim;
+            for (int i = 0; i < dim; i++) y.B[i] = i;
+            y.realA = 0;
+        }
+        const int dA = y.dA > 0 ? y.dA : 1;
+        y.P = y.dB * (2 * K + 1);
+        y.oW1 = o; o += (int64_t)FH * dA;
+        y.ob1 = o; o += FH;
+        y.oW2 = o; o += (int64_t)FH * FH;
+        y.ob2 = o; o += FH;
+        y.oW3 = o; o += (int64_t)y.P * FH;
+        y.ob3 = o; o += y.P;
+        y.mW2 = m;  m += (int64_t)FH * HSTR;              // [n][k]
+        y.mW2t = m; m += (int64_t)FH * HSTR;              // [k][n]
+        y.mW3 = m;  m += (int64_t)y.dB * g.CH * HSTR;     // [j][o][k]
+        y.mW3t = m; m += (int64_t)y.dB * FH * (g.CHK + 8);   // [j][k][o]
+    }
+    g.nparams = o;
+    g.nmirror = m;
+    return VG_OK;
+}
+
+// ------------------------------------------------------------ MMA helpers
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Warp GEMM block: acc[MT][NT8] (+)= A[m0.., k] * B[k, n0..], K a multiple of
+// 16.  A is row-major bf16 with K contiguous (lda elements per row); B is
+// given as Bt[n][k] row-major (K contiguous, ldb).  Fragment layouts of
+// mma.m16n8k16 (PTX ISA): g = lane/4, t = lane%4.
+template <int MT, int NT8>
+__device__ __forceinline__ void warp_gemm(float (&acc)[MT][NT8][4], const __nv_bfloat16 *A, int lda,
+                                          int m0, const __nv_bfloat16 *Bt, int ldb, int n0, int K)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        uint32_t af[MT][4];
+#pragma unroll
+        for (int mt = 0; mt < MT; mt++) {
+            const __nv_bfloat16 *r0 = A + (size_t)(m0 + 16 * mt + g) * lda + k0 + 2 * t;
+            const __nv_bfloat16 *r1 = r0 + (size_t)8 * lda;
+            af[mt][0] = *reinterpret_cast<const uint32_t *>(r0);
+            af[mt][1] = *reinterpret_cast<const uint32_t *>(r1);
+            af[mt][2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+            af[mt][3] = *reinterpret_cast<const uint32_t *>(r1 + 8);
+        }
+#pragma unroll
+        for (int nt = 0; nt < NT8; nt++) {
+            const __nv_bfloat16 *c0 = Bt + (size_t)(n0 + 8 * nt + g) * ldb + k0 + 2 * t;
+            uint32_t bf[2];
+            bf[0] = *reinterpret_cast<const uint32_t *>(c0);
+            bf[1] = *reinterpret_cast<const uint32_t *>(c0 + 8);
+#pragma unroll
+            for (int mt = 0; mt < MT; mt++) mma_bf16(acc[mt][nt], af[mt], bf);
+        }
+    }
+}
+
+template <int MT, int NT8>
+__device__ __forceinline__ void zero_acc(float (&acc)[MT][NT8][4])
+{
+#pragma unroll
+    for (int i = 0; i < MT; i++)
+#pragma unroll
+        for (int j = 0; j < NT8; j++)
+#pragma unroll
+            for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
+}
+
+// ----------------------------------------------------------- spline math
+// Row of 2K+1 logits o[]; forward and inverse of the piecewise-quadratic
+// CDF.  On exit o[k] holds the softmax probability s_k (k < K) and o[K+k] the
+// unnormalised vertex height u_k (k <= K), which the backward reuses.
+struct SplineState {
+    float Z, P, E, W, ub, ub1, alpha, num, pdfu;
+    int b;
+};
+
+__device__ __forceinline__ void spline_prepare(float *o, int K, float &Zout)
+{
+    float mx = -3.0e38f, mv = -3.0e38f;
+    for (int k = 0; k < K; k++) mx = fmaxf(mx, o[k]);
+    for (int k = 0; k <= K; k++) mv = fmaxf(mv, o[K + k]);
+    float se = 0.f;
+    for (int k = 0; k < K; k++) {
+        const float e = __expf(o[k] - mx);
+        o[k] = e;
+        se += e;
+    }
+    const float rse = 1.f / se;
+    for (int k = 0; k < K; k++) o[k] *= rse;
+    for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);
+    const float c1 = 1.f - K * EPS_W;
+    float Z = 0.f;
+    for (int k = 0; k < K; k++) Z += 0.5f * (o[K + k] + o[K + k + 1]) * (EPS_W + c1 * o[k]);
+    Zout = Z;
+}
+
+// CDF at x (density direction).
+__device__ __forceinline__ float spline_cdf(const float *o, int K, float Z, float x,
+                                            SplineState &s)
+{
+    const float c1 = 1.f - K * EPS_W;
+    float E = 0.f, P = 0.f;
+    int b = K - 1;
+    for (int k = 0; k < K; k++) {
+        const float W = EPS_W + c1 * o[k];
+        if (x < E + W || k == K - 1) {
+            b = k;
+            break;
+        }
+        E += W;
+        P += 0.5f * (o[K + k] + o[K + k + 1]) * W;
+    }
+    const float W = EPS_W + c1 * o[b];
+    const float ub = o[K + b], ub1 = o[K + b + 1];
+    float al = (x - E) / W;
+    al = fminf(fmaxf(al, 0.f), 1.f);
+    const float num = P + W * (al * ub + 0.5f * al * al * (ub1 - ub));
+    s.Z = Z; s.P = P; s.E = E; s.W = W; s.ub = ub; s.ub1 = ub1; s.alpha = al; s.b = b;
+    s.num = num;
+    s.pdfu = (1.f - al) * ub + al * ub1;
+    return num / Z;
+}
+
+// Inverse CDF at c (sampling direction): returns x, fills the state at x.
+__device__ __forceinline__ float spline_inv(const float *o, int K, float Z, float c,
+                                            SplineState &s)
+{
+    const float c1 = 1.f - K * EPS_W;
+    const float cz = c * Z;
+    float E = 0.f, P = 0.f;
+    int b = K - 1;
+    for (int k = 0; k < K; k++) {
+        const float W = EPS_W + c1 * o[k];
+        const float seg = 0.5f * (o[K + k] + o[K + k + 1]) * W;
+        if (cz < P + seg || k == K - 1) {
+            b = k;
+            break;
+        }
+        E += W;
+        P += seg;
+    }
+    const float W = EPS_W + c1 * o[b];
+    const float ub = o[K + b], ub1 = o[K + b + 1];
+    const float qa = 0.5f * W * (ub1 - ub), qb = W * ub;
+    const float r = fmaxf(cz - P, 0.f);
+    float al = 2.f * r / fmaxf(qb + sqrtf(fmaxf(qb * qb + 4.f * qa * r, 0.f)), 1e-30f);
+    al = fminf(fmaxf(al, 0.f), 1.f);
+    s.Z = Z; s.P = P; s.E = E; s.W = W; s.ub = ub; s.ub1 = ub1; s.alpha = al; s.b = b;
+    s.num = P + W * (al * ub + 0.5f * al * al * (ub1 - ub));
+    s.pdfu = (1.f - al) * ub + al * ub1;
+    return E + al * W;
+}
+
+// Backward of (C, logpdf) at the state s w.r.t. x and the logits: on entry
+// o[] holds the softmax probabilities and vertex heights left by
+// spline_prepare; on exit o[0..2K] holds dL/dlogits.  Returns dL/dx.
+//   C = (P_b + W_b (a u_b + a^2/2 (u_{b+1}-u_b))) / Z,
+//   log pdf = log((1-a) u_b + a u_{b+1}) - log Z,   a = (x - E_b) / W_b,
+//   W_k = EPS_W + (1 - K EPS_W) softmax(w)_k,  u_k = exp(v_k - max v).
+__device__ __forceinline__ float spline_backward(float *o, int K, const SplineState &s, float gC,
+                                                 float gL)
+{
+    const float c1 = 1.f - K * EPS_W;
+    const float Z = s.Z, al = s.alpha, W = s.W, ub = s.ub, ub1 = s.ub1;
+    const int b = s.b;
+    const float g_num = gC / Z;
+    const float g_Z = -gC * s.num / (Z * Z) - gL / Z;
+    const float g_pdfu = gL / s.pdfu;
+    const float g_al = g_pdfu * (ub1 - ub) + g_num * W * (ub + al * (ub1 - ub));
+    const float g_ub = g_pdfu * (1.f - al) + g_num * W * (al - 0.5f * al * al);
+    const float g_ub1 = g_pdfu * al + g_num * W * 0.5f * al * al;
+    const float g_Wb = g_num * (al * ub + 0.5f * al * al * (ub1 - ub)) - g_al * al / W;
+    const float g_x = g_al / W;
+    const float g_E = -g_al / W;
+    // pass A: dot = sum_k s_k c1 dL/dW_k (softmax Jacobian)
+    float dot = 0.f;
+    for (int k = 0; k < K; k++) {
+        const float us = o[K + k] + o[K + k + 1];
+        float gW = 0.5f * g_Z * us;
+        if (k < b) gW += g_E + 0.5f * g_num * us;
+        if (k == b) gW += g_Wb;
+        dot += o[k] * c1 * gW;
+    }
+    // pass B: write the logit gradients in place (W_{k-1} carried in Wprev)
+    float Wprev = 0.f;
+    for (int k = 0; k <= K; k++) {
+        const float Wk = (k < K) ? EPS_W + c1 * o[k] : 0.f;
+        float gu = 0.5f * g_Z * (Wprev + Wk);
+        if (k >= 1 && k <= b) gu += 0.5f * g_num * Wprev;
+        if (k < b) gu += 0.5f * g_num * Wk;
+        if (k == b) gu += g_ub;
+        if (k == b + 1) gu += g_ub1;
+        if (k < K) {
+            const float us = o[K + k] + o[K + k + 1];
+            float gW = 0.5f * g_Z * us;
+            if (k < b) gW += g_E + 0.5f * g_num * us;
+            if (k == b) gW += g_Wb;
+            o[k] = o[k] * (c1 * gW - dot);
+        }
+        o[K + k] = gu * o[K + k];
+        Wprev = Wk;
+    }
+    return g_x;
+}
+
+// ------------------------------------------------------------ shared tiles
+struct FlowSmem {
+    float *Z;             // [FROWS][FMAXD] state
+    float *G;             // [FROWS][FMAXD] gradient w.r.t. the layer output
+    __nv_bfloat16 *H1;    // [FROWS][HSTR]
+    __nv_bfloat16 *H2;    // [FROWS][HSTR]
+    float *OUT;           // [FROWS][ostr] f32 conditioner outputs (2 chunks)
+    __nv_bfloat16 *DOB;   // [FROWS][dstr] bf16 dL/dout of one chunk (backward)
+    float *LD;            // [FROWS]
+    float *RED;           // [FNT] scratch for column sums
+    int ostr, dstr;
+};
+
+__host__ __device__ inline size_t flow_smem_bytes(int CH, int CHK, int backward)
+{
+    size_t o = 0;
+    o += sizeof(float) * FROWS * FMAXD;                 // Z
+    o += sizeof(float) * FROWS * FMAXD;                 // G
+    o += sizeof(__nv_bfloat16) * FROWS * HSTR * 2;      // H1, H2
+    o += sizeof(float) * FROWS * (2 * CH + 4);          // OUT
+    if (backward) o += sizeof(__nv_bfloat16) * FROWS * (CHK + 8);   // DOB
+    o += sizeof(float) * FROWS;                         // LD
+    o += sizeof(float) * FNT;                           // RED
+    return o;
+}
+
+__device__ inline FlowSmem flow_smem(unsigned char *base, int CH, int CHK, int backward)
+{
+    FlowSmem s;
+    size_t o = 0;
+    s.Z = (float *)(base + o);           o += sizeof(float) * FROWS * FMAXD;
+    s.G = (float *)(base + o);           o += sizeof(float) * FROWS * FMAXD;
+    s.H1 = (__nv_bfloat16 *)(base + o);  o += sizeof(__nv_bfloat16) * FROWS * HSTR;
+    s.H2 = (__nv_bfloat16 *)(base + o);  o += sizeof(__nv_bfloat16) * FROWS * HSTR;
+    s.OUT = (float *)(base + o);         o += sizeof(float) * FROWS * (2 * CH + 4);
+    s.DOB = (__nv_bfloat16 *)(base + o); if (backward) o += sizeof(__nv_bfloat16) * FROWS * (CHK + 8);
+    s.LD = (float *)(base + o);          o += sizeof(float) * FROWS;
+    s.RED = (float *)(base + o);
+    s.ostr = 2 * CH + 4;
+    s.dstr = CHK + 8;
+    return s;
+}
+
+// H1 = relu(W1 z_A + b1) (FP32 FMA, K = dA is tiny), H2 = relu(H1 W2^T + b2)
+// on the tensor cores.
+__device__ void flow_hidden(const FlowGeom &g, const FlowLayer &y, const float *theta,
+                            const __nv_bfloat16 *mirror, FlowSmem &sm)
+{
+    const int tid = threadIdx.x;
+    {
+        const int r = tid & (FROWS - 1), half = tid >> 7;
+        const float *W1 = theta + y.oW1;
+        const float *b1 = theta + y.ob1;
+        const int dA = y.realA ? y.dA : 1;
+        float xa[FMAXD];
+        for (int a2 = 0; a2 < dA; a2++) xa[a2] = y.realA ? sm.Z[r * FMAXD + y.A[a2]] : 0.f;
+        for (int c = 64 * half; c < 64 * half + 64; c += 2) {
+            float v0 = b1[c], v1 = b1[c + 1];
+            for (int a2 = 0; a2 < dA; a2++) {
+                v0 = fmaf(W1[c * dA + a2], xa[a2], v0);
+                v1 = fmaf(W1[(c + 1) * dA + a2], xa[a2], v1);
+            }
+            *reinterpret_cast<uint32_t *>(&sm.H1[r * HSTR + c]) = pack_bf16(fmaxf(v0, 0.f), fmaxf(v1, 0.f));
+        }
+    }
+    __syncthreads();
+    {
+        const int w = tid >> 5, lane = tid & 31, gq = lane >> 2, t = lane & 3;
+        const int m0 = 32 * (w & 3), n0 = 64 * (w >> 2);
+        float acc[2][8][4];
+        zero_acc(acc);
+        warp_gemm<2, 8>(acc, sm.H1, HSTR, m0, mirror + y.mW2, HSTR, n0, FH);
+        const float *b2 = theta + y.ob2;
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int r = m0 + 16 * mt + gq, c = n0 + 8 * nt + 2 * t;
+                const float bb0 = b2[c], bb1 = b2[c + 1];
+                *reinterpret_cast<uint32_t *>(&sm.H2[r * HSTR + c]) =
+                    pack_bf16(fmaxf(acc[mt][nt][0] + bb0, 0.f), fmaxf(acc[mt][nt][1] + bb1, 0.f));
+                *reinterpret_cast<uint32_t *>(&sm.H2[(r + 8) * HSTR + c]) =
+                    pack_bf16(fmaxf(acc[mt][nt][2] + bb0, 0.f), fmaxf(acc[mt][nt][3] + bb1, 0.f));
+            }
+    }
+    __syncthreads();
+}
+
+// OUT chunk(s) for transformed coordinates j0 (and j0+1): OUT[r][jj*CH + o]
+__device__ void flow_out(const FlowGeom &g, const FlowLayer &y, const float *theta,
+                         const __nv_bfloat16 *mirror, FlowSmem &sm, int j0, int nj)
+{
+    const int tid = threadIdx.x;
+    const int w = tid >> 5, lane = tid & 31, gq = lane >> 2, t = lane & 3;
+    const int jj = w >> 2;
+    if (jj < nj) {
+        const int j = j0 + jj;
+        const int m0 = 32 * (w & 3);
+        const __nv_bfloat16 *Bt = mirror + y.mW3 + (int64_t)j * g.CH * HSTR;
+        const float *b3 = theta + y.ob3 + (int64_t)j * (2 * g.K + 1);
+        const int nreal = 2 * g.K + 1;
+        // CH/8 n-tiles, processed in groups of 3 to bound registers
+        for (int nb = 0; nb < g.CH / 8; nb += 3) {
+            float acc[2][3][4];
+            zero_acc(acc);
+            const int ntile = min(3, g.CH / 8 - nb);
+            if (ntile == 3) warp_gemm<2, 3>(acc, sm.H2, HSTR, m0, Bt, HSTR, 8 * nb, FH);
+            else if (ntile == 2) {
+                float a2[2][2][4];
+                zero_acc(a2);
+                warp_gemm<2, 2>(a2, sm.H2, HSTR, m0, Bt, HSTR, 8 * nb, FH);
+                for (int i = 0; i < 2; i++) for (int q = 0; q < 2; q++) for (int e = 0; e < 4; e++) acc[i][q][e] = a2[i][q][e];
+            } else {
+                float a1[2][1][4];
+                zero_acc(a1);
+                warp_gemm<2, 1>(a1, sm.H2, HSTR, m0, Bt, HSTR, 8 * nb, FH);
+                for (int i = 0; i < 2; i++) for (int e = 0; e < 4; e++) acc[i][0][e] = a1[i][0][e];
+            }
+            for (int mt = 0; mt < 2; mt++)
+                for (int nt = 0; nt < ntile; nt++) {
+                    const int r = m0 + 16 * mt + gq, c = 8 * (nb + nt) + 2 * t;
+                    const float bb0 = c < nreal ? b3[c] : 0.f, bb1 = c + 1 < nreal ? b3[c + 1] : 0.f;
+                    float *o0 = sm.OUT + r * sm.ostr + jj * g.CH + c;
+                    float *o1 = sm.OUT + (r + 8) * sm.ostr + jj * g.CH + c;
+                    o0[0] = acc[mt][nt][0] + bb0;
+                    o0[1] = acc[mt][nt][1] + bb1;
+                    o1[0] = acc[mt][nt][2] + bb0;
+                    o1[1] = acc[mt][nt][3] + bb1;
+                }
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void flow_mirror_kernel(FlowGeom g, const float *__restrict__ theta,
+                                   __nv_bfloat16 *__restrict__ mirror)
+{
+    const int l = blockIdx.y;
+    const FlowLayer &y = g.ly[l];
+    const int nreal = 2 * g.K + 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float *W2 = theta + y.oW2;
+    const float *W3 = theta + y.oW3;
+    for (int64_t i = i0; i < (int64_t)FH * HSTR; i += stride) {
+        const int r = (int)(i / HSTR), c = (int)(i % HSTR);
+        mirror[y.mW2 + i] = __float2bfloat16(c < FH ? W2[r * FH + c] : 0.f);      // [n][k]
+        mirror[y.mW2t + i] = __float2bfloat16(c < FH ? W2[c * FH + r] : 0.f);     // [k][n]
+    }
+    const int64_t n3 = (int64_t)y.dB * g.CH * HSTR;
+    for (int64_t i = i0; i < n3; i += stride) {
+        const int j = (int)(i / ((int64_t)g.CH * HSTR));
+        const int rem = (int)(i % ((int64_t)g.CH * HSTR));
+        const int o = rem / HSTR, k = rem % HSTR;
+        const float v = (o < nreal && k < FH) ? W3[((int64_t)j * nreal + o) * FH + k] : 0.f;
+        mirror[y.mW3 + i] = __float2bfloat16(v);
+    }
+    const int ls = g.CHK + 8;
+    const int64_t n3t = (int64_t)y.dB * FH * ls;
+    for (int64_t i = i0; i < n3t; i += stride) {
+        const int j = (int)(i / ((int64_t)FH * ls));
+        const int rem = (int)(i % ((int64_t)FH * ls));
+        const int k = rem / ls, o = rem % ls;
+        const float v = (o < nreal) ? W3[((int64_t)j * nreal + o) * FH + k] : 0.f;
+        mirror[y.mW3t + i] = __float2bfloat16(v);
+    }
+}
+
+// Inference through all layers: DIR 0 = density (CDF, layers 0..L-1),
+// DIR 1 = sampling (inverse CDF, layers L-1..0).  logdet = sum log pdf.
+// When zl != nullptr (training forward) the input of every layer is stored
+// to zl[l][row][dim].
+template <int DIR>
+__global__ void __launch_bounds__(FNT) flow_pass_kernel(FlowGeom g, const float *__restrict__ theta,
+                                                       const __nv_bfloat16 *__restrict__ mirror,
+                                                       int64_t n, const float *__restrict__ zin,
+                                                       float *__restrict__ zout,
+                                                       float *__restrict__ logdet,
+                                                       float *__restrict__ zl)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    FlowSmem sm = flow_smem(smem, g.CH, g.CHK, 0);
+    const int tid = threadIdx.x;
+    const int dim = g.dim;
+    const int64_t ntiles = (n + FROWS - 1) / FROWS;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t r0 = tile * FROWS;
+        for (int i = tid; i < FROWS * dim; i += FNT) {
+            const int r = i / dim, d = i % dim;
+            sm.Z[r * FMAXD + d] = (r0 + r < n) ? zin[(r0 + r) * dim + d] : 0.5f;
+        }
+        if (tid < FROWS) sm.LD[tid] = 0.f;
+        __syncthreads();
+        for (int step = 0; step < g.L; step++) {
+            const int l = DIR == 0 ? step : g.L - 1 - step;
+            const FlowLayer &y = g.ly[l];
+            if (zl != nullptr) {
+                for (int i = tid; i < FROWS * dim; i += FNT) {
+                    const int r = i / dim, d = i % dim;
+                    if (r0 + r < n) zl[((int64_t)l * n + r0 + r) * dim + d] = sm.Z[r * FMAXD + d];
+                }
+            }
+            flow_hidden(g, y, theta, mirror, sm);
+            for (int j0 = 0; j0 < y.dB; j0 += 2) {
+                const int nj = min(2, y.dB - j0);
+                flow_out(g, y, theta, mirror, sm, j0, nj);
+                const int r = tid & (FROWS - 1), jj = tid >> 7;
+                if (jj < nj) {
+                    float *o = sm.OUT + r * sm.ostr + jj * g.CH;
+                    float Z;
+                    spline_prepare(o, g.K, Z);
+                    SplineState st;
+                    const int col = y.B[j0 + jj];
+                    const float xin = sm.Z[r * FMAXD + col];
+                    float xo;
+                    if (DIR == 0) xo = spline_cdf(o, g.K, Z, xin, st);
+                    else xo = spline_inv(o, g.K, Z, xin, st);
+                    sm.Z[r * FMAXD + col] = fminf(fmaxf(xo, 0.f), 1.f);
+                    const float lp = __logf(st.pdfu) - __logf(st.Z);
+                    if (jj == 0) sm.LD[r] += lp;
+                    else sm.RED[r] = lp;
+                }
+                __syncthreads();
+                if (nj == 2 && tid < FROWS) sm.LD[tid] += sm.RED[tid];
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < FROWS * dim; i += FNT) {
+            const int r = i / dim, d = i % dim;
+            if (r0 + r < n) zout[(r0 + r) * dim + d] = sm.Z[r * FMAXD + d];
+        }
+        if (tid < FROWS && r0 + tid < n) logdet[r0 + tid] = sm.LD[tid];
+        __syncthreads();
+    }
+}
+
+// Training backward of layer l for one tile of rows.  Inputs: zl (layer
+// input), gout (dL/d layer output, rows x dim), w (loss weights).  Outputs:
+// gin (dL/d layer input), the transposed bf16 activations H1^T, H2^T and
+// gradients dOUT^T, dH2'^T, dH1'^T (column = row of the batch) for the
+// weight-gradient GEMMs, and atomically accumulated dW1, db1, db2, db3.
+__global__ void __launch_bounds__(FNT) flow_bwd_kernel(
+    FlowGeom g, int l, const float *__restrict__ theta, const __nv_bfloat16 *__restrict__ mirror,
+    int64_t n, int64_t ldn, const float *__restrict__ zl, const float *__restrict__ gout,
+    const float *__restrict__ w, float *__restrict__ gin, __nv_bfloat16 *__restrict__ h1t,
+    __nv_bfloat16 *__restrict__ h2t, __nv_bfloat16 *__restrict__ dot_, __nv_bfloat16 *__restrict__ dh2t,
+    __nv_bfloat16 *__restrict__ dh1t, float *__restrict__ grad, double *__restrict__ loss)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    FlowSmem sm = flow_smem(smem, g.CH, g.CHK, 1);
+    const FlowLayer &y = g.ly[l];
+    const int tid = threadIdx.x, dim = g.dim, K = g.K;
+    const int nreal = 2 * K + 1;
+    const int w8 = tid >> 5, lane = tid & 31, gq = lane >> 2, t = lane & 3;
+    const int64_t ntiles = ldn / FROWS;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t r0 = tile * FROWS;
+        for (int i = tid; i < FROWS * dim; i += FNT) {
+            const int r = i / dim, d = i % dim;
+            const bool ok = r0 + r < n;
+            sm.Z[r * FMAXD + d] = ok ? zl[((int64_t)l * n + r0 + r) * dim + d] : 0.5f;
+            sm.G[r * FMAXD + d] = ok ? gout[(r0 + r) * dim + d] : 0.f;
+        }
+        if (tid < FROWS) sm.LD[tid] = (r0 + tid < n) ? -w[r0 + tid] : 0.f;   // dL/dlogpdf
+        __syncthreads();
+        flow_hidden(g, y, theta, mirror, sm);
+        // transposed activations for dW2 = dH2'^T H1 and dW3 = dOUT^T H2
+        {
+            const int r = tid & (FROWS - 1), half = tid >> 7;
+            for (int c = 64 * half; c < 64 * half + 64; c++) {
+                h1t[(int64_t)c * ldn + r0 + r] = sm.H1[r * HSTR + c];
+                h2t[(int64_t)c * ldn + r0 + r] = sm.H2[r * HSTR + c];
+            }
+        }
+        // dH2 accumulated over the transformed coordinates: warp block 32x64
+        const int m0 = 32 * (w8 & 3), n0 = 64 * (w8 >> 2);
+        float dh2[2][8][4];
+        zero_acc(dh2);
+        for (int j = 0; j < y.dB; j++) {
+            flow_out(g, y, theta, mirror, sm, j, 1);
+            const int r = tid;   // threads 0..127: one row each
+            if (tid < FROWS) {
+                float *o = sm.OUT + r * sm.ostr;
+                float Z;
+                spline_prepare(o, K, Z);
+                SplineState st;
+                const int col = y.B[j];
+                const float xin = sm.Z[r * FMAXD + col];
+                spline_cdf(o, K, Z, xin, st);
+                const float gC = sm.G[r * FMAXD + col];
+                const float gL = sm.LD[r];
+                float lterm = (r0 + r < n) ? gL * (__logf(st.pdfu) - __logf(Z)) : 0.f;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) lterm += __shfl_xor_sync(0xffffffffu, lterm, off);
+                if ((tid & 31) == 0 && lterm != 0.f) atomicAdd(loss, (double)lterm);
+                const float gx = spline_backward(o, K, st, gC, gL);
+                sm.G[r * FMAXD + col] = gx;   // becomes dL/d(layer input) for B coordinates
+                for (int q = 0; q < sm.dstr; q += 2) {
+                    const float v0 = q < nreal ? o[q] : 0.f, v1 = q + 1 < nreal ? o[q + 1] : 0.f;
+                    *reinterpret_cast<uint32_t *>(&sm.DOB[r * sm.dstr + q]) = pack_bf16(v0, v1);
+                }
+            }
+            __syncthreads();
+            // dOUT^T to global (rows of the transposed matrix = outputs of coordinate j)
+            {
+                const int r = tid & (FROWS - 1), half = tid >> 7;
+                for (int q = half; q < nreal; q += 2)
+                    dot_[((int64_t)j * nreal + q) * ldn + r0 + r] = sm.DOB[r * sm.dstr + q];
+            }
+            // db3 for coordinate j: column sums of dOUT
+            for (int q = tid; q < nreal; q += FNT) {
+                float sacc = 0.f;
+                for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.DOB[r * sm.dstr + q]);
+                atomicAdd(&grad[y.ob3 + (int64_t)j * nreal + q], sacc);
+            }
+            // dH2 += dOUT_j W3_j  (K = CHK outputs)
+            warp_gemm<2, 8>(dh2, sm.DOB, sm.dstr, m0, mirror + y.mW3t + (int64_t)j * FH * (g.CHK + 8),
+                            g.CHK + 8, n0, g.CHK);
+            __syncthreads();
+        }
+        // dH2' = dH2 * relu'(H2) -> H2 buffer (bf16) and dH2'^T to global; db2
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++) {
+                const int r = m0 + 16 * mt + gq, c = n0 + 8 * nt + 2 * t;
+                __nv_bfloat16 *p0 = &sm.H2[r * HSTR + c];
+                __nv_bfloat16 *p1 = &sm.H2[(r + 8) * HSTR + c];
+                const float a0 = __bfloat162float(p0[0]) > 0.f ? dh2[mt][nt][0] : 0.f;
+                const float a1 = __bfloat162float(p0[1]) > 0.f ? dh2[mt][nt][1] : 0.f;
+                const float a2 = __bfloat162float(p1[0]) > 0.f ? dh2[mt][nt][2] : 0.f;
+                const float a3 = __bfloat162float(p1[1]) > 0.f ? dh2[mt][nt][3] : 0.f;
+                *reinterpret_cast<uint32_t *>(p0) = pack_bf16(a0, a1);
+                *reinterpret_cast<uint32_t *>(p1) = pack_bf16(a2, a3);
+            }
+        __syncthreads();
+        {
+            const int r = tid & (FROWS - 1), half = tid >> 7;
+            for (int c = 64 * half; c < 64 * half + 64; c++)
+                dh2t[(int64_t)c * ldn + r0 + r] = sm.H2[r * HSTR + c];
+        }
+        if (tid < FH) {
+            float sacc = 0.f;
+            for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.H2[r * HSTR + tid]);
+            atomicAdd(&grad[y.ob2 + tid], sacc);
+        }
+        // dH1 = dH2' W2 ; dH1' = dH1 * relu'(H1) -> H1 buffer
+        {
+            float dh1[2][8][4];
+            zero_acc(dh1);
+            warp_gemm<2, 8>(dh1, sm.H2, HSTR, m0, mirror + y.mW2t, HSTR, n0, FH);
+            __syncthreads();
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 8; nt++) {
+                    const int r = m0 + 16 * mt + gq, c = n0 + 8 * nt + 2 * t;
+                    __nv_bfloat16 *p0 = &sm.H1[r * HSTR + c];
+                    __nv_bfloat16 *p1 = &sm.H1[(r + 8) * HSTR + c];
+                    const float a0 = __bfloat162float(p0[0]) > 0.f ? dh1[mt][nt][0] : 0.f;
+                    const float a1 = __bfloat162float(p0[1]) > 0.f ? dh1[mt][nt][1] : 0.f;
+                    const float a2 = __bfloat162float(p1[0]) > 0.f ? dh1[mt][nt][2] : 0.f;
+                    const float a3 = __bfloat162float(p1[1]) > 0.f ? dh1[mt][nt][3] : 0.f;
+                    *reinterpret_cast<uint32_t *>(p0) = pack_bf16(a0, a1);
+                    *reinterpret_cast<uint32_t *>(p1) = pack_bf16(a2, a3);
+                }
+        }
+        __syncthreads();
+        {
+            const int r = tid & (FROWS - 1), half = tid >> 7;
+            for (int c = 64 * half; c < 64 * half + 64; c++)
+                dh1t[(int64_t)c * ldn + r0 + r] = sm.H1[r * HSTR + c];
+        }
+        // db1, dW1 (K = rows of the tile, FP32)
+        const int dA = y.realA ? y.dA : 1;
+        for (int idx = tid; idx < FH * (dA + 1); idx += FNT) {
+            const int c = idx % FH, a2 = idx / FH;   // a2 == dA -> bias
+            float sacc = 0.f;
+            for (int r = 0; r < FROWS; r++) {
+                const float d1 = __bfloat162float(sm.H1[r * HSTR + c]);
+                const float xv = (a2 == dA) ? 1.f : (y.realA ? sm.Z[r * FMAXD + y.A[a2]] : 0.f);
+                sacc = fmaf(d1, xv, sacc);
+            }
+            if (a2 == dA) atomicAdd(&grad[y.ob1 + c], sacc);
+            else atomicAdd(&grad[y.oW1 + (int64_t)c * dA + a2], sacc);
+        }
+        // dL/dz_A += dH1' W1 (conditioning coordinates)
+        if (y.realA && tid < FROWS) {
+            const int r = tid;
+            const float *W1 = theta + y.oW1;
+            for (int a2 = 0; a2 < y.dA; a2++) {
+                float sacc = 0.f;
+                for (int c = 0; c < FH; c++) sacc = fmaf(__bfloat162float(sm.H1[r * HSTR + c]), W1[c * dA + a2], sacc);
+                sm.G[r * FMAXD + y.A[a2]] += sacc;
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < FROWS * dim; i += FNT) {
+            const int r = i / dim, d = i % dim;
+            if (r0 + r < n) gin[(r0 + r) * dim + d] = sm.G[r * FMAXD + d];
+        }
+        __syncthreads();
+    }
+}
+
+// Weight gradients C[m][n] = sum_r A[m][r] B[n][r] over r in this CTA's
+// K-split (A, B bf16, K contiguous, ld = ldn); partial sums to
+// part[split][m][n].  Tile 64x64 per CTA, 8 warps of 16x32.
+__global__ void __launch_bounds__(FNT) flow_wgrad_kernel(const __nv_bfloat16 *__restrict__ A,
+                                                        const __nv_bfloat16 *__restrict__ B, int M,
+                                                        int N, int64_t ldn, int64_t kchunk,
+                                                        float *__restrict__ part)
+{
+    const int w8 = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
+    const int mb = blockIdx.x, nb = blockIdx.y, split = blockIdx.z;
+    const int m0 = 64 * mb + 16 * (w8 & 3), n0 = 64 * nb + 32 * (w8 >> 2);
+    const int64_t k0 = (int64_t)split * kchunk;
+    const int64_t k1 = k0 + kchunk < ldn ? k0 + kchunk : ldn;   // ldn, kchunk: multiples of 16
+    float acc[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int q = 0; q < 4; q++) acc[i][q] = 0.f;
+    const int ra = m0 + gq, rb = ra + 8;
+    for (int64_t k = k0; k < k1; k += 16) {
+        uint32_t af[4];
+        const __nv_bfloat16 *pa0 = A + (int64_t)ra * ldn + k + 2 * t;
+        const __nv_bfloat16 *pa1 = A + (int64_t)rb * ldn + k + 2 * t;
+        af[0] = ra < M ? *reinterpret_cast<const uint32_t *>(pa0) : 0u;
+        af[1] = rb < M ? *reinterpret_cast<const uint32_t *>(pa1) : 0u;
+        af[2] = ra < M ? *reinterpret_cast<const uint32_t *>(pa0 + 8) : 0u;
+        af[3] = rb < M ? *reinterpret_cast<const uint32_t *>(pa1 + 8) : 0u;
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            const int cn = n0 + 8 * nt + gq;
+            uint32_t bf[2];
+            const __nv_bfloat16 *pb = B + (int64_t)cn * ldn + k + 2 * t;
+            bf[0] = cn < N ? *reinterpret_cast<const uint32_t *>(pb) : 0u;
+            bf[1] = cn < N ? *reinterpret_cast<const uint32_t *>(pb + 8) : 0u;
+            mma_bf16(acc[nt], af, bf);
+        }
+    }
+    float *P = part + (int64_t)split * M * N;
+#pragma unroll
+    for (int nt = 0; nt < 4; nt++) {
+        const int c = n0 + 8 * nt + 2 * t;
+        if (ra < M && c < N) P[(int64_t)ra * N + c] = acc[nt][0];
+        if (ra < M && c + 1 < N) P[(int64_t)ra * N + c + 1] = acc[nt][1];
+        if (rb < M && c < N) P[(int64_t)rb * N + c] = acc[nt][2];
+        if (rb < M && c + 1 < N) P[(int64_t)rb * N + c + 1] = acc[nt][3];
+    }
+}
+
+__global__ void flow_wgrad_reduce_kernel(const float *__restrict__ part, int nsplit, int64_t MN,
+                                         float *__restrict__ out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int q = 0; q < nsplit; q++) s += part[(int64_t)q * MN + i];
+        out[i] += s;
+    }
+}
+
+__global__ void flow_adam_kernel(int64_t np, float *__restrict__ theta, const float *__restrict__ grad,
+                                 float *__restrict__ m, float *__restrict__ v, float scale, float lr,
+                                 float b1, float b2, float eps, float bc1, float bc2, float clip)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float gi = grad[i] * scale;
+        gi = fminf(fmaxf(gi, -clip), clip);
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        theta[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    }
+}
+
+int geom_of(FlowGeom &g, const vg_flow *fl) { return make_geom(g, fl->dim, fl->nlayers, fl->K, fl->hidden); }
+
+int set_smem(const void *kern, size_t bytes)
+{
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return vg_fail(VG_ERR_CUDA, "flow smem attribute: %s", cudaGetErrorString(e));
+    return VG_OK;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+extern "C" int64_t vg_flow_nparams(int dim, int nlayers, int K, int hidden)
+{
+    FlowGeom g;
+    if (make_geom(g, dim, nlayers, K, hidden)) return -1;
+    return g.nparams;
+}
+
+extern "C" int64_t vg_flow_mirror_elems(int dim, int nlayers, int K, int hidden)
+{
+    FlowGeom g;
+    if (make_geom(g, dim, nlayers, K, hidden)) return -1;
+    return g.nmirror;
+}
+
+extern "C" int64_t vg_flow_train_bytes(const vg_flow *fl, int64_t nrows)
+{
+    FlowGeom g;
+    if (geom_of(g, fl)) return -1;
+    const int64_t ldn = (nrows + FROWS - 1) / FROWS * FROWS;
+    int maxP = 0;
+    for (int l = 0; l < g.L; l++) maxP = g.ly[l].P > maxP ? g.ly[l].P : maxP;
+    int64_t b = 0;
+    b += (int64_t)g.L * nrows * g.dim * 4;        // layer inputs
+    b += 2 * nrows * g.dim * 4;                   // gradient ping-pong
+    b += (int64_t)FH * ldn * 2 * 4;               // h1t, h2t, dh2t, dh1t
+    b += (int64_t)maxP * ldn * 2;                 // dout^T
+    b += 16 * (int64_t)(maxP > FH ? maxP : FH) * FH * 4;   // split-K partials (dW3, dW2)
+    b += nrows * 4 + nrows * g.dim * 4;           // logdet + zhat scratch
+    return b + 4096;
+}
+
+extern "C" int vg_flow_refresh(const vg_flow *fl, void *stream)
+{
+    vg_clear_error();
+    FlowGeom g;
+    int rc = geom_of(g, fl);
+    if (rc) return rc;
+    dim3 grid(64, g.L);
+    flow_mirror_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(g, fl->theta, (__nv_bfloat16 *)fl->mirror);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
+static int flow_pass(const vg_flow *fl, int dir, int64_t n, const float *zin, float *zout,
+                     float *logdet, float *zl, cudaStream_t st)
+{
+    FlowGeom g;
+    int rc = geom_of(g, fl);
+    if (rc) return rc;
+    if (n <= 0) return VG_OK;
+    const size_t sm = flow_smem_bytes(g.CH, g.CHK, 0);
+    if (sm > VG_FLOW_SMEM_MAX) return vg_fail(VG_ERR_UNSUPPORTED, "flow bins %d: shared memory", g.K);
+    const void *k = dir == 0 ? (const void *)flow_pass_kernel<0> : (const void *)flow_pass_kernel<1>;
+    if ((rc = set_smem(k, sm))) return rc;
+    const int64_t ntiles = (n + FROWS - 1) / FROWS;
+    int64_t grid = (int64_t)vg_num_sms();
+    if (grid > ntiles) grid = ntiles;
+    if (dir == 0)
+        flow_pass_kernel<0><<<(unsigned)grid, FNT, sm, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+                                                             n, zin, zout, logdet, zl);
+    else
+        flow_pass_kernel<1><<<(unsigned)grid, FNT, sm, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+                                                             n, zin, zout, logdet, zl);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
+extern "C" int vg_flow_sample(const vg_flow *fl, int64_t n, const float *zhat, float *z,
+                              float *logdet, void *stream)
+{
+    vg_clear_error();
+    return flow_pass(fl, 1, n, zhat, z, logdet, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int vg_flow_density(const vg_flow *fl, int64_t n, const float *z, float *zhat,
+                               float *logdet, void *stream)
+{
+    vg_clear_error();
+    return flow_pass(fl, 0, n, z, zhat, logdet, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const float *w,
+                            void *work, size_t work_bytes, void *stream)
+{
+    vg_clear_error();
+    FlowGeom g;
+    int rc = geom_of(g, fl);
+    if (rc) return rc;
+    if (n <= 0) return VG_OK;
+    const int64_t need = vg_flow_train_bytes(fl, n);
+    if ((int64_t)work_bytes < need) return vg_fail(VG_ERR_VALUE, "flow workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t ldn = (n + FROWS - 1) / FROWS * FROWS;
+    int maxP = 0;
+    for (int l = 0; l < g.L; l++) maxP = g.ly[l].P > maxP ? g.ly[l].P : maxP;
+    char *p = (char *)work;
+    auto take = [&](int64_t bytes) { char *q = p; p += (bytes + 255) & ~255LL; return q; };
+    float *zl = (float *)take((int64_t)g.L * n * g.dim * 4);
+    float *ga = (float *)take(n * g.dim * 4);
+    float *gb = (float *)take(n * g.dim * 4);
+    __nv_bfloat16 *h1t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
+    __nv_bfloat16 *h2t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
+    __nv_bfloat16 *dh2t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
+    __nv_bfloat16 *dh1t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
+    __nv_bfloat16 *dott = (__nv_bfloat16 *)take((int64_t)maxP * ldn * 2);
+    float *part = (float *)take(16 * (int64_t)(maxP > FH ? maxP : FH) * FH * 4);
+    float *ld = (float *)take(n * 4);
+    float *zh = (float *)take(n * g.dim * 4);
+    if (p > (char *)work + work_bytes) return vg_fail(VG_ERR_VALUE, "flow workspace layout");
+    // forward (density direction) storing every layer's input
+    if ((rc = flow_pass(fl, 0, n, z, zh, ld, zl, st))) return rc;
+    VG_CUDA_CHECK(cudaMemsetAsync(ga, 0, n * g.dim * 4, st));
+    const size_t smb = flow_smem_bytes(g.CH, g.CHK, 1);
+    if (smb > VG_FLOW_SMEM_MAX) return vg_fail(VG_ERR_UNSUPPORTED, "flow bins %d: shared memory", g.K);
+    if ((rc = set_smem((const void *)flow_bwd_kernel, smb))) return rc;
+    int64_t grid = (int64_t)vg_num_sms();
+    if (grid > ldn / FROWS) grid = ldn / FROWS;
+    // split-K over the batch rows: at most 16 chunks of a multiple of 16 rows
+    const int64_t kchunk = ((ldn / 16) + 15) / 16 * 16;
+    float *gcur = ga, *gnext = gb;
+    for (int l = g.L - 1; l >= 0; l--) {
+        const FlowLayer &y = g.ly[l];
+        flow_bwd_kernel<<<(unsigned)grid, FNT, smb, st>>>(g, l, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+                                                          n, ldn, zl, gcur, w, gnext, h1t, h2t, dott,
+                                                          dh2t, dh1t, fl->grad, fl->loss);
+        VG_LAUNCH_CHECK();
+        // dW3 = dOUT^T H2  (M = P, N = hidden), dW2 = dH2'^T H1 (M = N = hidden)
+        const int64_t ks = kchunk;
+        const int ns = (int)((ldn + ks - 1) / ks);
+        dim3 g3((y.P + 63) / 64, (FH + 63) / 64, ns);
+        flow_wgrad_kernel<<<g3, FNT, 0, st>>>(dott, h2t, y.P, FH, ldn, ks, part);
+        VG_LAUNCH_CHECK();
+        flow_wgrad_reduce_kernel<<<256, 256, 0, st>>>(part, ns, (int64_t)y.P * FH, fl->grad + y.oW3);
+        VG_LAUNCH_CHECK();
+        dim3 g2((FH + 63) / 64, (FH + 63) / 64, ns);
+        flow_wgrad_kernel<<<g2, FNT, 0, st>>>(dh2t, h1t, FH, FH, ldn, ks, part);
+        VG_LAUNCH_CHECK();
+        flow_wgrad_reduce_kernel<<<256, 256, 0, st>>>(part, ns, (int64_t)FH * FH, fl->grad + y.oW2);
+        VG_LAUNCH_CHECK();
+        float *tmp = gcur;
+        gcur = gnext;
+        gnext = tmp;
+    }
+    return VG_OK;
+}
+
+extern "C" int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta1, float beta2,
+                            float eps, int step, float clip, void *stream)
+{
+    vg_clear_error();
+    FlowGeom g;
+    int rc = geom_of(g, fl);
+    if (rc) return rc;
+    const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
+    flow_adam_kernel<<<512, 256, 0, (cudaStream_t)stream>>>(g.nparams, fl->theta, fl->grad, fl->adam_m,
+                                                            fl->adam_v, scale, lr, beta1, beta2, eps,
+                                                            bc1, bc2, clip);
+    VG_LAUNCH_CHECK();
+    return vg_flow_refresh(fl, stream);
+}

@@ -15,6 +15,7 @@
 
 struct VgParams {
     int n;
+    float fc[8];                 // FP32 constants, precomputed on the host (vg_prepare_f32_host)
     double p[VG_MAX_PARAMS];
 };
 
@@ -101,36 +102,46 @@ struct VgF32Consts {
     float c[8];
 };
 
+// FP32 constants of each integrand, computed once on the host in FP64 (the
+// GPU's FP64 rate is too low to recompute them in every thread).
+inline void vg_prepare_f32_host(VgParams &P, int kind, int dim)
+{
+    const double *p = P.p;
+    for (int i = 0; i < 8; i++) P.fc[i] = 0.f;
+    if (kind == VG_F_GAUSS) {
+        P.fc[0] = (float)(p[0] * VG_LOG2E);  // a*log2(e)
+        P.fc[1] = (float)p[1];               // centre
+        P.fc[2] = (float)p[2];               // norm
+    } else if (kind == VG_F_RIDGE) {
+        double M = p[0], sg = p[1];
+        double kk = 1.0 / (2.0 * sg * sg) * VG_LOG2E;    // log2 units
+        double sk = sqrt(kk * dim);
+        P.fc[0] = (float)kk;                                // E0 = -kk * R
+        P.fc[1] = (float)sk;                                // w = m * sk
+        P.fc[2] = (float)(pow(2.0 * VG_PI * sg * sg, -0.5 * dim) / M);
+        P.fc[3] = (float)(1.0 / dim);
+        P.fc[4] = (float)(sk / M);                          // v_j = (j + 1/2) * sk/M
+        P.fc[5] = (float)M;
+    } else if (kind == VG_F_MIXTURE) {
+        double sg = p[1];
+        P.fc[0] = (float)(VG_LOG2E / (2.0 * sg * sg));
+        P.fc[1] = (float)(pow(2.0 * VG_PI * sg * sg, -0.5 * dim) / p[0]);
+        P.fc[5] = (float)p[0];
+    } else if (kind == VG_F_LATTICE) {
+        P.fc[0] = (float)(1.0 / (2.0 * p[0]));
+        P.fc[1] = (float)p[0];
+        P.fc[2] = (float)p[1];
+    } else if (kind == VG_F_CONST) {
+        P.fc[0] = (float)p[0];
+    }
+}
+
 template <int KIND>
 __device__ __forceinline__ VgF32Consts vg_prepare_f32(const VgParams &P, int dim)
 {
     VgF32Consts k;
-    const double *p = P.p;
-    for (int i = 0; i < 8; i++) k.c[i] = 0.f;
-    if (KIND == VG_F_GAUSS) {
-        k.c[0] = (float)(p[0] * VG_LOG2E);  // a*log2(e)
-        k.c[1] = (float)p[1];               // centre
-        k.c[2] = (float)p[2];               // norm
-    } else if (KIND == VG_F_RIDGE) {
-        double M = p[0], sg = p[1];
-        double kk = 1.0 / (2.0 * sg * sg) * VG_LOG2E;    // log2 units
-        double sk = sqrt(kk * dim);
-        k.c[0] = (float)kk;                                // E0 = -kk * R
-        k.c[1] = (float)sk;                                // w = m * sk, v_j = c_j * sk
-        k.c[2] = (float)(pow(2.0 * VG_PI * sg * sg, -0.5 * dim) / M);
-        k.c[3] = (float)(1.0 / dim);
-        k.c[4] = (float)(sk / M);                          // v_j = (j + 1/2) * sk/M
-    } else if (KIND == VG_F_MIXTURE) {
-        double sg = p[1];
-        k.c[0] = (float)(VG_LOG2E / (2.0 * sg * sg));
-        k.c[1] = (float)(pow(2.0 * VG_PI * sg * sg, -0.5 * dim) / p[0]);
-    } else if (KIND == VG_F_LATTICE) {
-        k.c[0] = (float)(1.0 / (2.0 * p[0]));
-        k.c[1] = (float)p[0];
-        k.c[2] = (float)p[1];
-    } else if (KIND == VG_F_CONST) {
-        k.c[0] = (float)p[0];
-    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) k.c[i] = P.fc[i];
     return k;
 }
 
@@ -140,18 +151,18 @@ __device__ __forceinline__ void vg_fill_table_f32(const VgParams &P, int dim, fl
                                                   const VgF32Consts &k)
 {
     if (KIND == VG_F_RIDGE) {
-        int M = (int)P.p[0];
-        for (int j = threadIdx.x; j < M; j += blockDim.x)
-            tab[j] = (float)(((double)j + 0.5) * (double)k.c[1] / P.p[0]);
+        const int M = (int)P.fc[5];
+        for (int j = threadIdx.x; j < M; j += blockDim.x) tab[j] = ((float)j + 0.5f) * k.c[4];
     } else if (KIND == VG_F_MIXTURE) {
-        int K = (int)P.p[0];
+        const int K = (int)P.fc[5];
         for (int j = threadIdx.x; j < K * dim; j += blockDim.x) tab[j] = (float)P.p[2 + j];
     } else if (KIND == VG_F_LORENTZ) {
         for (int j = threadIdx.x; j < dim; j += blockDim.x) {
-            tab[j] = (float)P.p[j];                         // centre
-            tab[dim + j] = (float)P.p[dim + j];             // width
-            tab[2 * dim + j] = (float)(P.p[dim + j] / VG_PI);
-            tab[3 * dim + j] = (float)(P.p[dim + j] * P.p[dim + j]);
+            const float c = (float)P.p[j], w = (float)P.p[dim + j];
+            tab[j] = c;                                     // centre
+            tab[dim + j] = w;                               // width
+            tab[2 * dim + j] = w * (float)(1.0 / VG_PI);
+            tab[3 * dim + j] = w * w;
         }
     }
 }

@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
     const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
     const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     if ((int64_t)blockIdx.x >= nblk) return;
-    const double beta_half = __ddiv_rn(a.beta, 2.0);
+    const double beta_half = a.beta_half;
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
     const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
     if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
@@ -386,6 +386,8 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     a.stream = it->stream_id;
     a.itn = itn;
     a.u = u;
+    a.dv_y = 1.0 / (double)it->nhcube;
+    a.beta_half = it->beta / 2.0;
     return VG_OK;
 }
 
@@ -511,6 +513,7 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
     default: return vg_fail(VG_ERR_VALUE, "unknown integrand kind %d", kind);
     }
     if (nparams < need) return vg_fail(VG_ERR_VALUE, "integrand needs %d parameters", need);
+    vg_prepare_f32_host(P, kind, it->dim);
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = reset_counter(a, st))) return rc;
     if ((rc = vg::launch_fused(a, kind, P, tab_len, it->precision == VG_F64, st))) return rc;

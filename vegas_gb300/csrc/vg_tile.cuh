@@ -94,6 +94,8 @@ struct IterArgs {
     int tab_len;              // integrand table length (floats)
     int T;                    // tile size of the launched kernel
     int ncta;                 // CTAs of the launched reduction kernel (one partial each)
+    double dv_y;              // 1 / nhcube (pyx:1639)
+    double beta_half;         // beta / 2 (pyx:2185)
 };
 
 template <typename T>
@@ -337,8 +339,9 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
     } else {
         for (int i = 0; i < 8; i++) kc.c[i] = 0.f;
     }
-    const double dv_y = __ddiv_rn(1.0, (double)a.H);
-    const double beta_half = __ddiv_rn(a.beta, 2.0);
+    const double dv_y = a.dv_y;
+    const float dv_yf = (float)a.dv_y;
+    const double beta_half = a.beta_half;
     int nan_local = 0;
     // per-thread running sums over every hypercube this thread finalises
     double acc_m = 0.0, acc_v = 0.0, acc_s = 0.0;
@@ -485,7 +488,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
                 }
                 // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
                 if (sizeof(T) == 8) wg[k] = __dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
-                else wg[k] = (double)((float)jac * ((float)dv_y / (float)nh));
+                else wg[k] = (double)((float)jac * (dv_yf / (float)nh));
                 if (MODE == MODE_POINTS) {
                     T *xo = (T *)a.x_out;
 #pragma unroll
