@@ -227,7 +227,7 @@ int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const double *u,
  * vg_flow_refresh after any change of theta).
  */
 typedef struct vg_flow {
-    int32_t dim, nlayers, K, hidden;   /* dim <= 16, nlayers <= 8, K <= 64, hidden == 128 */
+    int32_t dim, nlayers, K, hidden;   /* dim <= 16, nlayers <= 8, K <= 48, hidden == 128 */
     float *theta;                      /* [nparams] FP32 parameters                       */
     void *mirror;                      /* BF16 dense-layer copies                          */
     float *grad;                       /* [nparams] gradient accumulator (caller zeroes)   */
@@ -254,12 +254,34 @@ int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const float *w, v
 /* Adam step on theta with gradient grad*scale (clipped at +-clip), then refresh. */
 int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta1, float beta2, float eps,
                  int step, float clip, void *stream);
+/* Device status of the flow kernels: VG_ERR_TIMEOUT when a bounded wait of
+ * the tensor-core pass gave up (the pass then stopped early); reset clears it.
+ * Synchronises with the device. */
+int vg_flow_status(int *status, int reset);
+/* 1: run inference on the mma.sync kernels even where the tcgen05 pass
+ * applies (for comparisons); 0: default. */
+int vg_flow_set_path(int legacy);
+
+/*
+ * Built-in integrand at given points (FP32): f[i] = vol * f(lo + width * z_i)
+ * * exp(-logdet[i]) with z[n,dim] on the unit cube, vol = prod(width),
+ * logdet optional (NULL).  The evaluation step of the flow path, where the
+ * points come from vg_sample + vg_flow_sample instead of the fused kernel.
+ * Replaces the integrand call of Integrator.__call__ (_vegas.pyx:2126-2129)
+ * for the built-in integrands.  lo, width: host arrays [dim].
+ */
+int vg_eval_points(int kind, const double *params, int nparams, int dim, int64_t n,
+                   const float *z, const double *lo, const double *width, const float *logdet,
+                   float *f, void *stream);
 
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);
 int vg_probe_fp64_fma(double *out, int64_t nthreads, int iters, void *stream);
 int vg_probe_fp32_fma(float *out, int64_t nthreads, int iters, void *stream);
+/* tcgen05 check: D[128 x N] = A[128 x K] B[N x K]^T, bf16 inputs (row-major,
+ * K contiguous), FP32 output; status[0] = 1 if the bounded wait gave up. */
+int vg_probe_umma_gemm(const void *A, const void *B, float *D, int N, int K, int *status, void *stream);
 
 #ifdef __cplusplus
 }

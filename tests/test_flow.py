@@ -12,6 +12,8 @@ rounding of activations and weights:
 (the backward rounds dL/dout, dL/dh2 and dL/dh1 to BF16 for the tensor-core
 weight-gradient GEMMs).
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -107,29 +109,62 @@ def _oracle_bf16(fn, *args, **kw):
         F.BF16 = False
 
 
+@pytest.fixture(params=['tcgen05', 'mma.sync'])
+def flow_path(request):
+    L = N.load()
+    L.vg_flow_set_path(1 if request.param == 'mma.sync' else 0)
+    st = ctypes.c_int(0)
+    N.check(L.vg_flow_status(ctypes.byref(st), 1))
+    yield request.param
+    N.check(L.vg_flow_status(ctypes.byref(st), 1))
+    L.vg_flow_set_path(0)
+    assert st.value == 0, 'a bounded wait of the tensor-core pass gave up'
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize('dim', [1, 3, 4, 8])
-def test_gpu_flow_passes_vs_oracle(dim):
-    theta = _theta(dim)
-    fl = _gpu_flow(dim, theta)
+@pytest.mark.parametrize('dim,K', [(1, 32), (3, 32), (4, 32), (8, 32), (16, 32), (4, 16), (9, 16)])
+def test_gpu_flow_passes_vs_oracle(dim, K, flow_path):
+    theta = _theta(dim, K=K)
+    fl = _gpu_flow(dim, theta, K=K)
     torch.manual_seed(dim)
     n = 1000
     u = torch.rand(n, dim, dtype=torch.float32)
     th64 = torch.tensor(theta, dtype=torch.float64)
     # sampling direction
     z, ld = fl.sample(u.cuda())
-    zo, ldo = _oracle_bf16(F.sample_pass, th64, u.double(), dim)
+    zo, ldo = _oracle_bf16(F.sample_pass, th64, u.double(), dim, K=K)
     assert float((z.cpu().double() - zo).abs().max()) <= 2e-3
     assert float((ld.cpu().double() - ldo).abs().max()) <= 2e-2
     # density direction at the oracle's points
     zh, ld2 = fl.density(zo.float().cuda())
-    zho, ld2o = _oracle_bf16(F.density_pass, th64, zo, dim)
+    zho, ld2o = _oracle_bf16(F.density_pass, th64, zo, dim, K=K)
     assert float((zh.cpu().double() - zho).abs().max()) <= 2e-3
     assert float((ld2.cpu().double() - ld2o).abs().max()) <= 2e-2
     # round trip on the GPU
     zh2, ld3 = fl.density(z)
     assert float((zh2 - u.cuda()).abs().max()) <= 2e-3
     assert float((ld3 - ld).abs().max()) <= 2e-2
+
+
+@pytest.mark.gpu
+def test_gpu_flow_large_batch_paths_agree():
+    """Ragged batch over many super-tiles: the tcgen05 and mma.sync passes agree."""
+    dim = 8
+    fl = _gpu_flow(dim, _theta(dim))
+    L = N.load()
+    u = torch.rand(300001, dim, device='cuda', generator=torch.Generator(device='cuda').manual_seed(5))
+    st = ctypes.c_int(0)
+    N.check(L.vg_flow_status(ctypes.byref(st), 1))
+    z1, ld1 = fl.sample(u)
+    L.vg_flow_set_path(1)
+    try:
+        z2, ld2 = fl.sample(u)
+    finally:
+        L.vg_flow_set_path(0)
+    N.check(L.vg_flow_status(ctypes.byref(st), 1))
+    assert st.value == 0
+    assert float((z1 - z2).abs().max()) <= 2e-3
+    assert float((ld1 - ld2).abs().max()) <= 2e-2
 
 
 @pytest.mark.gpu

@@ -155,9 +155,13 @@ SIGNATURES = {
     'vg_flow_grad': (I32, [P, I64, P, P, P, SZ, P]),
     'vg_flow_adam': (I32, [P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                            ctypes.c_float, I32, ctypes.c_float, P]),
+    'vg_flow_status': (I32, [P, I32]),
+    'vg_flow_set_path': (I32, [I32]),
+    'vg_eval_points': (I32, [I32, P, I32, I32, I64, P, P, P, P, P, P]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),
+    'vg_probe_umma_gemm': (I32, [P, P, P, I32, I32, P, P]),
 }
 
 

@@ -29,6 +29,7 @@
 #include <string.h>
 
 #include "vg_common.cuh"
+#include "vg_umma.cuh"
 
 namespace {
 
@@ -47,6 +48,8 @@ struct FlowLayer {
     int A[FMAXD], B[FMAXD];
     int64_t oW1, ob1, oW2, ob2, oW3, ob3;   // offsets into theta
     int64_t mW2, mW2t, mW3, mW3t;           // offsets (elements) into the bf16 mirror
+    int64_t mU2, mU3;              // tcgen05 operand images of W2 [128 x 128] and W3 [NP x 128]
+    int NP;                        // W3 image rows: dB*CH padded to 16
     int realA;                     // 0 when the layer conditions on nothing
 };
 
@@ -55,6 +58,7 @@ struct FlowGeom {
     int CHK;                       // CH padded to a multiple of 16 (K dim of dOUT . W3)
     FlowLayer ly[FMAXL];
     int64_t nparams, nmirror;
+    int NPmax, dAmax, dBmax;
 };
 
 // masks: bit b = (l/2) % nbits of the coordinate index; B = bit == l % 2
@@ -100,6 +104,12 @@ int make_geom(FlowGeom &g, int dim, int L, int K, int hidden)
         y.mW2t = m; m += (int64_t)FH * HSTR;              // [k][n]
         y.mW3 = m;  m += (int64_t)y.dB * g.CH * HSTR;     // [j][o][k]
         y.mW3t = m; m += (int64_t)y.dB * FH * (g.CHK + 8);   // [j][k][o]
+        y.NP = (y.dB * g.CH + 15) / 16 * 16;
+        y.mU2 = m; m += (int64_t)FH * FH;
+        y.mU3 = m; m += (int64_t)y.NP * FH;
+        if (y.NP > g.NPmax) g.NPmax = y.NP;
+        if (dA > g.dAmax) g.dAmax = dA;
+        if (y.dB > g.dBmax) g.dBmax = y.dB;
     }
     g.nparams = o;
     g.nmirror = m;
@@ -470,6 +480,18 @@ __global__ void flow_mirror_kernel(FlowGeom g, const float *__restrict__ theta,
         const float v = (o < nreal) ? W3[((int64_t)j * nreal + o) * FH + k] : 0.f;
         mirror[y.mW3t + i] = __float2bfloat16(v);
     }
+    // tcgen05 operand images (K-major, 128-byte swizzle), byte-identical to
+    // the shared-memory tiles the MMA reads
+    for (int64_t i = i0; i < (int64_t)FH * FH; i += stride) {
+        const int r = (int)(i / FH), k = (int)(i % FH);
+        mirror[y.mU2 + umma::sw128_offset(FH, r, k) / 2] = __float2bfloat16(W2[r * FH + k]);
+    }
+    for (int64_t i = i0; i < (int64_t)y.NP * FH; i += stride) {
+        const int row = (int)(i / FH), k = (int)(i % FH);
+        const int j = row / g.CH, o = row % g.CH;
+        const float v = (j < y.dB && o < nreal) ? W3[((int64_t)j * nreal + o) * FH + k] : 0.f;
+        mirror[y.mU3 + umma::sw128_offset(y.NP, row, k) / 2] = __float2bfloat16(v);
+    }
 }
 
 // Inference through all layers: DIR 0 = density (CDF, layers 0..L-1),
@@ -782,6 +804,320 @@ __global__ void flow_adam_kernel(int64_t np, float *__restrict__ theta, const fl
     }
 }
 
+// ------------------------------------------------- tcgen05 inference pass
+// Spline of one coordinate with its 2K+1 logits in registers (compile-time
+// K, fully unrolled).  DIR 0: CDF at x; DIR 1: inverse CDF at x.  Returns
+// the transformed coordinate and lp = log pdf at the (input | output) point.
+template <int K, int DIR>
+__device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, float &lp)
+{
+    constexpr float c1 = 1.f - K * EPS_W;
+    float mx = o[0];
+#pragma unroll
+    for (int k = 1; k < K; k++) mx = fmaxf(mx, o[k]);
+    float mv = o[K];
+#pragma unroll
+    for (int k = 1; k <= K; k++) mv = fmaxf(mv, o[K + k]);
+    float se = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        o[k] = __expf(o[k] - mx);
+        se += o[k];
+    }
+    const float cw = __fdividef(c1, se);
+#pragma unroll
+    for (int k = 0; k < K; k++) o[k] = fmaf(cw, o[k], EPS_W);   // bin widths
+#pragma unroll
+    for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);   // vertex heights (unnormalised)
+    float Z = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) Z = fmaf(0.5f * (o[K + k] + o[K + k + 1]), o[k], Z);
+    const float t = DIR == 0 ? x : x * Z;
+    float E = 0.f, P = 0.f, Wb = o[K - 1], ub = o[2 * K - 1], ub1 = o[2 * K], Eb = 0.f, Pb = 0.f;
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float W = o[k];
+        const float seg = 0.5f * (o[K + k] + o[K + k + 1]) * W;
+        const bool here = !found && (k == K - 1 || (DIR == 0 ? (t < E + W) : (t < P + seg)));
+        if (here) {
+            Wb = W;
+            ub = o[K + k];
+            ub1 = o[K + k + 1];
+            Eb = E;
+            Pb = P;
+            found = true;
+        }
+        E += W;
+        P += seg;
+    }
+    float al, xo;
+    if (DIR == 0) {
+        al = fminf(fmaxf(__fdividef(x - Eb, Wb), 0.f), 1.f);
+        xo = __fdividef(Pb + Wb * (al * ub + 0.5f * al * al * (ub1 - ub)), Z);
+    } else {
+        const float qa = 0.5f * Wb * (ub1 - ub), qb = Wb * ub;
+        const float r = fmaxf(t - Pb, 0.f);
+        al = __fdividef(2.f * r, fmaxf(qb + sqrtf(fmaxf(qb * qb + 4.f * qa * r, 0.f)), 1e-30f));
+        al = fminf(fmaxf(al, 0.f), 1.f);
+        xo = Eb + al * Wb;
+    }
+    const float pdfu = (1.f - al) * ub + al * ub1;
+    lp = __logf(pdfu) - __logf(Z);
+    return xo;
+}
+
+__device__ int g_flow_status;   // set to VG_ERR_TIMEOUT when a bounded wait gave up
+
+constexpr int UST_MAX = 16;      // 128-row sub-tiles per super-tile
+
+struct UmmaPlan {
+    int ST;                      // sub-tiles per super-tile
+    int zst;                     // row stride of the state in shared memory (odd)
+    size_t oW2, oW3, oA, oW1, ob1, ob2, ob3, oZ, oLD, total;
+};
+
+__host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
+{
+    UmmaPlan p;
+    p.ST = ST;
+    p.zst = g.dim | 1;
+    size_t o = 0;
+    p.oW2 = o; o += (size_t)FH * FH * 2;
+    p.oW3 = o; o += (size_t)g.NPmax * FH * 2;
+    p.oA = o;  o += (size_t)FH * FH * 2;
+    p.oW1 = o; o += sizeof(float) * FH * 8;
+    p.ob1 = o; o += sizeof(float) * FH;
+    p.ob2 = o; o += sizeof(float) * FH;
+    p.ob3 = o; o += sizeof(float) * 8 * (2 * FMAXK + 1);
+    p.oZ = o;  o += sizeof(float) * (size_t)ST * FROWS * p.zst;
+    p.oLD = o; o += sizeof(float) * 2 * (size_t)ST * FROWS;
+    p.total = o + 1024;          // + alignment slack of the dynamic base
+    return p;
+}
+
+// Inference through all layers on the 5th-generation tensor cores.  One CTA
+// (8 warps) per SM; a super-tile of ST x 128 rows stays in shared memory
+// while the layers go by, so each layer's weights are fetched (bulk copy)
+// once per super-tile.  Per 128-row sub-tile and layer:
+//   H1 = relu(W1 z_A + b1)           FP32 FMA, written as the bf16 A operand
+//   TMEM[0:128)   = H1 W2^T           tcgen05.mma, M=128 N=128 K=128
+//   H2 = relu(TMEM + b2)              tcgen05.ld epilogue -> bf16 A operand
+//   TMEM[buf]     = H2 W3[g]^T        two transformed coordinates per MMA
+//                                     group, double-buffered in TMEM
+//   spline of each (row, coordinate)  registers; thread = (row, half)
+template <int K, int DIR>
+__global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, const float *__restrict__ theta,
+                                                               const __nv_bfloat16 *__restrict__ mirror,
+                                                               int64_t n, const float *__restrict__ zin,
+                                                               float *__restrict__ zout,
+                                                               float *__restrict__ logdet,
+                                                               float *__restrict__ zl, int ST)
+{
+    constexpr int NR = 2 * K + 1;
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t bars[5];   // 0 weights, 1 GEMM1, 2-3 GEMM2 buffers, 4 drain
+    __shared__ uint32_t tslot;
+    __shared__ int abort_flag;
+    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    const UmmaPlan pl = umma_plan(g, ST);
+    uint8_t *sW2 = base + pl.oW2, *sW3 = base + pl.oW3, *sA = base + pl.oA;
+    float *sW1 = (float *)(base + pl.oW1), *sb1 = (float *)(base + pl.ob1);
+    float *sb2 = (float *)(base + pl.ob2), *sb3 = (float *)(base + pl.ob3);
+    float *sZ = (float *)(base + pl.oZ), *sLD = (float *)(base + pl.oLD);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & (FROWS - 1), h = tid >> 7;
+    const int dim = g.dim, zst = pl.zst, CH = g.CH;
+    const uint32_t bar_w = umma::smem_u32(&bars[0]), bar_h = umma::smem_u32(&bars[1]);
+    const uint32_t bar_o0 = umma::smem_u32(&bars[2]), bar_d = umma::smem_u32(&bars[4]);
+    if (warp == 0) umma::tmem_alloc(umma::smem_u32(&tslot), 512);
+    if (tid == 0) {
+        for (int i = 0; i < 5; i++) umma::mbar_init(umma::smem_u32(&bars[i]), 1);
+        abort_flag = 0;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+    uint32_t ph_w = 0, ph_h = 0, ph_o0 = 0, ph_o1 = 0, ph_d = 0;
+    const int64_t rows_per = (int64_t)ST * FROWS;
+    const int64_t nsuper = (n + rows_per - 1) / rows_per;
+    bool aborted = false;
+    for (int64_t sup = blockIdx.x; sup < nsuper && !aborted; sup += gridDim.x) {
+        const int64_t r0 = sup * rows_per;
+        const int nrows = (int)((n - r0) < rows_per ? (n - r0) : rows_per);
+        const int nsub = (nrows + FROWS - 1) / FROWS;
+        for (int i = tid; i < nsub * FROWS * dim; i += FNT) {
+            const int rr = i / dim, d = i % dim;
+            sZ[rr * zst + d] = rr < nrows ? zin[(r0 + rr) * dim + d] : 0.5f;
+        }
+        for (int i = tid; i < 2 * nsub * FROWS; i += FNT) sLD[i] = 0.f;
+        __syncthreads();
+        for (int step = 0; step < g.L && !aborted; step++) {
+            const int l = DIR == 0 ? step : g.L - 1 - step;
+            const FlowLayer &y = g.ly[l];
+            const int dA = y.realA ? y.dA : 1;
+            // weights of this layer: bf16 operand images by bulk copy, FP32 vectors by threads
+            if (tid == 0) {
+                const uint32_t b2 = (uint32_t)FH * FH * 2, b3 = (uint32_t)y.NP * FH * 2;
+                umma::mbar_expect_tx(bar_w, b2 + b3);
+                umma::bulk_g2s(umma::smem_u32(sW2), mirror + y.mU2, b2, bar_w);
+                for (uint32_t off = 0; off < b3; off += 32768u) {
+                    const uint32_t sz = (b3 - off) < 32768u ? (b3 - off) : 32768u;
+                    umma::bulk_g2s(umma::smem_u32(sW3) + off, (const uint8_t *)(mirror + y.mU3) + off, sz, bar_w);
+                }
+            }
+            for (int i = tid; i < FH * dA; i += FNT) sW1[i] = theta[y.oW1 + i];
+            for (int i = tid; i < FH; i += FNT) {
+                sb1[i] = theta[y.ob1 + i];
+                sb2[i] = theta[y.ob2 + i];
+            }
+            for (int i = tid; i < y.dB * NR; i += FNT) sb3[i] = theta[y.ob3 + i];
+            if (!umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
+            ph_w ^= 1;
+            __syncthreads();
+            if (abort_flag) { aborted = true; break; }
+            for (int s = 0; s < nsub; s++) {
+                float *Zs = sZ + (size_t)s * FROWS * zst;
+                if (zl != nullptr) {
+                    for (int i = tid; i < FROWS * dim; i += FNT) {
+                        const int rr = i / dim, d = i % dim;
+                        const int64_t grow = r0 + (int64_t)s * FROWS + rr;
+                        if (grow < n) zl[((int64_t)l * n + grow) * dim + d] = Zs[rr * zst + d];
+                    }
+                }
+                // ---- H1 (FP32) -> A operand
+                {
+                    float xa[8];
+#pragma unroll
+                    for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? Zs[r * zst + y.A[a]] : 0.f;
+                    for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 8) {
+                        float v[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            float acc = sb1[c0 + q];
+                            for (int a = 0; a < dA; a++) acc = fmaf(sW1[(c0 + q) * dA + a], xa[a], acc);
+                            v[q] = fmaxf(acc, 0.f);
+                        }
+                        uint4 pk;
+                        pk.x = pack_bf16(v[0], v[1]);
+                        pk.y = pack_bf16(v[2], v[3]);
+                        pk.z = pack_bf16(v[4], v[5]);
+                        pk.w = pack_bf16(v[6], v[7]);
+                        *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(FH, r, c0)) = pk;
+                    }
+                }
+                umma::fence_async_smem();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (tid == 0) {
+                    umma::fence_after_sync();
+                    umma::gemm_128xN(tmem, umma::smem_u32(sA), umma::smem_u32(sW2), FH, FH, FH, 0);
+                    umma::mma_commit(bar_h);
+                }
+                if (!umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
+                ph_h ^= 1;
+                umma::fence_after_sync();
+                // ---- H2 epilogue: TMEM -> +b2, relu -> A operand
+                for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
+                    float v[32];
+                    umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+                    for (int q8 = 0; q8 < 32; q8 += 8) {
+                        uint4 pk;
+                        const int c = c0 + q8;
+                        pk.x = pack_bf16(fmaxf(v[q8 + 0] + sb2[c + 0], 0.f), fmaxf(v[q8 + 1] + sb2[c + 1], 0.f));
+                        pk.y = pack_bf16(fmaxf(v[q8 + 2] + sb2[c + 2], 0.f), fmaxf(v[q8 + 3] + sb2[c + 3], 0.f));
+                        pk.z = pack_bf16(fmaxf(v[q8 + 4] + sb2[c + 4], 0.f), fmaxf(v[q8 + 5] + sb2[c + 5], 0.f));
+                        pk.w = pack_bf16(fmaxf(v[q8 + 6] + sb2[c + 6], 0.f), fmaxf(v[q8 + 7] + sb2[c + 7], 0.f));
+                        *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(FH, r, c)) = pk;
+                    }
+                }
+                umma::fence_async_smem();
+                umma::fence_before_sync();
+                __syncthreads();
+                if (abort_flag) { aborted = true; break; }
+                // ---- output layer in groups of two coordinates, double-buffered in TMEM
+                const int ngroups = (y.dB + 1) / 2;
+                auto issue = [&](int gi) {
+                    const int ncoord = (2 * gi + 1 < y.dB) ? 2 : 1;
+                    const int N = ncoord == 2 ? 2 * CH : (CH + 15) / 16 * 16;
+                    const uint32_t dcol = (uint32_t)(FH + (gi & 1) * 2 * CH);
+                    umma::gemm_128xN(tmem + dcol, umma::smem_u32(sA),
+                                     umma::smem_u32(sW3) + (uint32_t)(2 * gi * CH) * 128u, N, FH, y.NP, 0);
+                    umma::mma_commit(bar_o0 + 8u * (uint32_t)(gi & 1));
+                };
+                if (tid == 0) {
+                    umma::fence_after_sync();
+                    issue(0);
+                    if (ngroups > 1) issue(1);
+                }
+                for (int gi = 0; gi < ngroups; gi++) {
+                    const int buf = gi & 1;
+                    bool ok;
+                    if (buf == 0) { ok = umma::mbar_wait(bar_o0, ph_o0); ph_o0 ^= 1; }
+                    else { ok = umma::mbar_wait(bar_o0 + 8u, ph_o1); ph_o1 ^= 1; }
+                    if (!ok) abort_flag = 1;
+                    umma::fence_after_sync();
+                    const int j = 2 * gi + h;
+                    if (ok && j < y.dB) {
+                        const uint32_t col = (uint32_t)(FH + buf * 2 * CH + h * CH);
+                        float o[NR];
+                        {
+                            float v[32];
+                            umma::tmem_ld32(tmem + lane_base + col, v);
+#pragma unroll
+                            for (int q = 0; q < 32; q++) o[q] = v[q];
+                            if (NR > 32) {
+                                umma::tmem_ld32(tmem + lane_base + col + 32u, v);
+#pragma unroll
+                                for (int q = 0; q < 32; q++)
+                                    if (32 + q < NR) o[32 + q] = v[q];
+                            }
+                            if (NR > 64) o[64] = umma::tmem_ld1(tmem + lane_base + col + 64u);
+                        }
+                        const float *bb = sb3 + j * NR;
+#pragma unroll
+                        for (int q = 0; q < NR; q++) o[q] += bb[q];
+                        const int cz = y.B[j];
+                        const float xin = Zs[r * zst + cz];
+                        float lp;
+                        const float xo = spline_reg<K, DIR>(o, xin, lp);
+                        Zs[r * zst + cz] = fminf(fmaxf(xo, 0.f), 1.f);
+                        sLD[(size_t)h * ST * FROWS + s * FROWS + r] += lp;
+                    }
+                    umma::fence_before_sync();
+                    __syncthreads();
+                    if (tid == 0 && gi + 2 < ngroups) {
+                        umma::fence_after_sync();
+                        issue(gi + 2);
+                    }
+                }
+                if (abort_flag) { aborted = true; break; }
+            }
+            __syncthreads();
+        }
+        if (aborted) break;
+        for (int i = tid; i < nrows * dim; i += FNT) {
+            const int rr = i / dim, d = i % dim;
+            zout[(r0 + rr) * dim + d] = sZ[rr * zst + d];
+        }
+        for (int rr = tid; rr < nrows; rr += FNT) logdet[r0 + rr] = sLD[rr] + sLD[(size_t)ST * FROWS + rr];
+        __syncthreads();
+    }
+    // drain: every MMA issued by thread 0 has completed before TMEM is freed
+    if (tid == 0) {
+        umma::mma_commit(bar_d);
+        if (!umma::mbar_wait(bar_d, ph_d)) abort_flag = 1;
+        if (aborted || abort_flag) atomicExch(&g_flow_status, VG_ERR_TIMEOUT);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (warp == 0) umma::tmem_dealloc(tmem, 512);
+}
+
 int geom_of(FlowGeom &g, const vg_flow *fl) { return make_geom(g, fl->dim, fl->nlayers, fl->K, fl->hidden); }
 
 int set_smem(const void *kern, size_t bytes)
@@ -837,6 +1173,38 @@ extern "C" int vg_flow_refresh(const vg_flow *fl, void *stream)
     return VG_OK;
 }
 
+// tcgen05 inference pass when the configuration fits it (K in {16, 32},
+// at most 8 conditioning coordinates per layer, shared memory); returns 1
+// when it launched, 0 when the caller should use the mma.sync pass.
+template <int K>
+static int flow_pass_umma_k(const FlowGeom &g, const vg_flow *fl, int dir, int64_t n, const float *zin,
+                            float *zout, float *logdet, float *zl, cudaStream_t st, int *rc)
+{
+    const size_t limit = VG_FLOW_SMEM_MAX;
+    int ST = UST_MAX;
+    while (ST > 1 && umma_plan(g, ST).total > limit) ST--;
+    const UmmaPlan pl = umma_plan(g, ST);
+    if (pl.total > limit) return 0;
+    size_t smem = pl.total < 120 * 1024 ? 120 * 1024 : pl.total;   // one CTA per SM (TMEM: 512 columns)
+    const void *k = dir == 0 ? (const void *)flow_pass_umma_kernel<K, 0> : (const void *)flow_pass_umma_kernel<K, 1>;
+    if ((*rc = set_smem(k, smem))) return 1;
+    const int64_t rows_per = (int64_t)ST * FROWS;
+    const int64_t nsuper = (n + rows_per - 1) / rows_per;
+    int64_t grid = (int64_t)vg_num_sms();
+    if (grid > nsuper) grid = nsuper;
+    if (dir == 0)
+        flow_pass_umma_kernel<K, 0><<<(unsigned)grid, FNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+                                                                       n, zin, zout, logdet, zl, ST);
+    else
+        flow_pass_umma_kernel<K, 1><<<(unsigned)grid, FNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+                                                                       n, zin, zout, logdet, zl, ST);
+    cudaError_t e = cudaGetLastError();
+    *rc = e == cudaSuccess ? VG_OK : vg_fail(VG_ERR_CUDA, "flow umma launch: %s", cudaGetErrorString(e));
+    return 1;
+}
+
+static int g_flow_force_legacy = 0;   // vg_flow_set_path(1): always use the mma.sync pass
+
 static int flow_pass(const vg_flow *fl, int dir, int64_t n, const float *zin, float *zout,
                      float *logdet, float *zl, cudaStream_t st)
 {
@@ -844,6 +1212,12 @@ static int flow_pass(const vg_flow *fl, int dir, int64_t n, const float *zin, fl
     int rc = geom_of(g, fl);
     if (rc) return rc;
     if (n <= 0) return VG_OK;
+    if (!g_flow_force_legacy && g.dAmax <= 8 && g.dBmax <= 8) {
+        int used = 0;
+        if (g.K == 32) used = flow_pass_umma_k<32>(g, fl, dir, n, zin, zout, logdet, zl, st, &rc);
+        else if (g.K == 16) used = flow_pass_umma_k<16>(g, fl, dir, n, zin, zout, logdet, zl, st, &rc);
+        if (used) return rc;
+    }
     const size_t sm = flow_smem_bytes(g.CH, g.CHK, 0);
     if (sm > VG_FLOW_SMEM_MAX) return vg_fail(VG_ERR_UNSUPPORTED, "flow bins %d: shared memory", g.K);
     const void *k = dir == 0 ? (const void *)flow_pass_kernel<0> : (const void *)flow_pass_kernel<1>;
@@ -953,4 +1327,23 @@ extern "C" int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta
                                                             bc1, bc2, clip);
     VG_LAUNCH_CHECK();
     return vg_flow_refresh(fl, stream);
+}
+
+extern "C" int vg_flow_set_path(int legacy)
+{
+    g_flow_force_legacy = legacy ? 1 : 0;
+    return VG_OK;
+}
+
+extern "C" int vg_flow_status(int *status, int reset)
+{
+    vg_clear_error();
+    int v = 0;
+    VG_CUDA_CHECK(cudaMemcpyFromSymbol(&v, g_flow_status, sizeof(int)));
+    if (reset) {
+        const int z = 0;
+        VG_CUDA_CHECK(cudaMemcpyToSymbol(g_flow_status, &z, sizeof(int)));
+    }
+    *status = v;
+    return VG_OK;
 }

@@ -480,15 +480,12 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
-extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, int kind,
-                                  const double *params, int nparams, void *stream)
+// Validate the parameters of a built-in integrand and fill P (including its
+// host-precomputed FP32 constants); tab_len = length of its per-CTA table.
+int vg_build_params(int kind, int dim, const double *params, int nparams, VgParams *Pp, int *tab_len_out)
 {
-    vg_clear_error();
-    IterArgs a;
-    int rc = fill_args(a, it, itn, u);
-    if (rc) return rc;
     if (nparams < 0 || nparams > VG_MAX_PARAMS) return vg_fail(VG_ERR_VALUE, "too many params");
-    static VgParams P;
+    VgParams &P = *Pp;
     memset(&P, 0, sizeof(P));
     P.n = nparams;
     for (int i = 0; i < nparams; i++) P.p[i] = params[i];
@@ -501,19 +498,33 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
             return vg_fail(VG_ERR_VALUE, "ridge M out of range 1..16384");
         tab_len = nparams >= 1 ? (int)params[0] : 0;
         break;
-    case VG_F_LORENTZ: need = 2 * it->dim; tab_len = 4 * it->dim; break;
+    case VG_F_LORENTZ: need = 2 * dim; tab_len = 4 * dim; break;
     case VG_F_MIXTURE:
-        need = nparams >= 1 ? 2 + (int)params[0] * it->dim : 1;
-        if (nparams >= 1 && (params[0] < 1 || params[0] * it->dim > VG_MAX_PARAMS - 2))
+        need = nparams >= 1 ? 2 + (int)params[0] * dim : 1;
+        if (nparams >= 1 && (params[0] < 1 || params[0] * dim > VG_MAX_PARAMS - 2))
             return vg_fail(VG_ERR_VALUE, "mixture size out of range");
-        tab_len = nparams >= 1 ? (int)params[0] * it->dim : 0;
+        tab_len = nparams >= 1 ? (int)params[0] * dim : 0;
         break;
     case VG_F_LATTICE: need = 2; break;
     case VG_F_CONST: need = 1; break;
     default: return vg_fail(VG_ERR_VALUE, "unknown integrand kind %d", kind);
     }
     if (nparams < need) return vg_fail(VG_ERR_VALUE, "integrand needs %d parameters", need);
-    vg_prepare_f32_host(P, kind, it->dim);
+    vg_prepare_f32_host(P, kind, dim);
+    *tab_len_out = tab_len;
+    return VG_OK;
+}
+
+extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, int kind,
+                                  const double *params, int nparams, void *stream)
+{
+    vg_clear_error();
+    IterArgs a;
+    int rc = fill_args(a, it, itn, u);
+    if (rc) return rc;
+    static VgParams P;
+    int tab_len = 0;
+    if ((rc = vg_build_params(kind, it->dim, params, nparams, &P, &tab_len))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = reset_counter(a, st))) return rc;
     if ((rc = vg::launch_fused(a, kind, P, tab_len, it->precision == VG_F64, st))) return rc;
