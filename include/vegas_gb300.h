@@ -279,9 +279,11 @@ int vg_eval_points(int kind, const double *params, int nparams, int dim, int64_t
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);
 int vg_probe_fp64_fma(double *out, int64_t nthreads, int iters, void *stream);
 int vg_probe_fp32_fma(float *out, int64_t nthreads, int iters, void *stream);
-/* tcgen05 check: D[128 x N] = A[128 x K] B[N x K]^T, bf16 inputs (row-major,
- * K contiguous), FP32 output; status[0] = 1 if the bounded wait gave up. */
-int vg_probe_umma_gemm(const void *A, const void *B, float *D, int N, int K, int *status, void *stream);
+/* tcgen05 check: D[128 x N] = A[128 x K] B[N x K]^T, bf16 inputs, FP32
+ * output.  A is [128][K] (K-major) or, with a_mn, [K][128] (MN-major); B is
+ * [N][K] or, with b_mn, [K][N].  status[0] = 1 if the bounded wait gave up. */
+int vg_probe_umma_gemm(const void *A, const void *B, float *D, int N, int K, int a_mn, int b_mn, int *status,
+                       void *stream);
 
 #ifdef __cplusplus
 }

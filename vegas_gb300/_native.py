@@ -161,7 +161,7 @@ SIGNATURES = {
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),
-    'vg_probe_umma_gemm': (I32, [P, P, P, I32, I32, P, P]),
+    'vg_probe_umma_gemm': (I32, [P, P, P, I32, I32, I32, I32, P, P]),
 }
 
 

@@ -952,7 +952,10 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
             const int rr = i / dim, d = i % dim;
             sZ[rr * zst + d] = rr < nrows ? zin[(r0 + rr) * dim + d] : 0.5f;
         }
-        for (int i = tid; i < 2 * nsub * FROWS; i += FNT) sLD[i] = 0.f;
+        for (int i = tid; i < nsub * FROWS; i += FNT) {
+            sLD[i] = 0.f;                          // log-det partial of the h = 0 threads
+            sLD[(size_t)ST * FROWS + i] = 0.f;     // ... of the h = 1 threads
+        }
         __syncthreads();
         for (int step = 0; step < g.L && !aborted; step++) {
             const int l = DIR == 0 ? step : g.L - 1 - step;

@@ -95,7 +95,7 @@ namespace {
 __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__restrict__ A,
                                                          const __nv_bfloat16 *__restrict__ B,
                                                          float *__restrict__ D, int N, int K,
-                                                         uint32_t ncols, int *status)
+                                                         uint32_t ncols, int a_mn, int b_mn, int *status)
 {
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t bar;
@@ -105,15 +105,32 @@ __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__
     uint8_t *sb = base + 128 * K * 2;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int kc = K / 8;
-    for (int i = tid; i < 128 * kc; i += blockDim.x) {
-        const int r = i / kc, k = (i % kc) * 8;
-        *reinterpret_cast<uint4 *>(sa + umma::sw128_offset(128, r, k)) =
-            *reinterpret_cast<const uint4 *>(A + (size_t)r * K + k);
+    if (!a_mn) {
+        for (int i = tid; i < 128 * kc; i += blockDim.x) {
+            const int r = i / kc, k = (i % kc) * 8;
+            *reinterpret_cast<uint4 *>(sa + umma::sw128_offset(128, r, k)) =
+                *reinterpret_cast<const uint4 *>(A + (size_t)r * K + k);
+        }
+    } else {   // A given as [K][128]: the tile of its transpose
+        for (int i = tid; i < K * 16; i += blockDim.x) {
+            const int k = i / 16, m = (i % 16) * 8;
+            *reinterpret_cast<uint4 *>(sa + umma::sw128_offset(K, k, m)) =
+                *reinterpret_cast<const uint4 *>(A + (size_t)k * 128 + m);
+        }
     }
-    for (int i = tid; i < N * kc; i += blockDim.x) {
-        const int r = i / kc, k = (i % kc) * 8;
-        *reinterpret_cast<uint4 *>(sb + umma::sw128_offset(N, r, k)) =
-            *reinterpret_cast<const uint4 *>(B + (size_t)r * K + k);
+    if (!b_mn) {
+        for (int i = tid; i < N * kc; i += blockDim.x) {
+            const int r = i / kc, k = (i % kc) * 8;
+            *reinterpret_cast<uint4 *>(sb + umma::sw128_offset(N, r, k)) =
+                *reinterpret_cast<const uint4 *>(B + (size_t)r * K + k);
+        }
+    } else {   // B given as [K][N]
+        const int nc = N / 8;
+        for (int i = tid; i < K * nc; i += blockDim.x) {
+            const int k = i / nc, m = (i % nc) * 8;
+            *reinterpret_cast<uint4 *>(sb + umma::sw128_offset(K, k, m)) =
+                *reinterpret_cast<const uint4 *>(B + (size_t)k * N + m);
+        }
     }
     umma::fence_async_smem();
     if (warp == 0) umma::tmem_alloc(umma::smem_u32(&slot), ncols);
@@ -123,7 +140,7 @@ __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__
     umma::fence_after_sync();
     const uint32_t tmem = slot;
     if (tid == 0) {
-        umma::gemm_128xN(tmem, umma::smem_u32(sa), umma::smem_u32(sb), N, K, N, 0);
+        umma::gemm_128xN_ex(tmem, umma::smem_u32(sa), a_mn, 128, umma::smem_u32(sb), b_mn, N, N, K, 0);
         umma::mma_commit(umma::smem_u32(&bar));
     }
     const bool ok = umma::mbar_wait(umma::smem_u32(&bar), 0);
@@ -147,19 +164,20 @@ __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__
 
 }  // namespace
 
-extern "C" int vg_probe_umma_gemm(const void *A, const void *B, float *D, int N, int K, int *status,
-                                  void *stream)
+extern "C" int vg_probe_umma_gemm(const void *A, const void *B, float *D, int N, int K, int a_mn, int b_mn,
+                                  int *status, void *stream)
 {
     vg_clear_error();
-    if (N < 16 || N > 256 || N % 16 || K < 64 || K % 64 || K > 256)
-        return vg_fail(VG_ERR_VALUE, "umma probe: N in 16..256 (multiple of 16), K in 64..256 (multiple of 64)");
+    if (N < 16 || N > 256 || N % 16 || K < 64 || K % 64 || K > 256 || (b_mn && N % 64))
+        return vg_fail(VG_ERR_VALUE, "umma probe: N in 16..256 (multiple of 16; of 64 for MN-major B), "
+                                     "K in 64..256 (multiple of 64)");
     uint32_t ncols = 32;
     while ((int)ncols < N) ncols <<= 1;
     const size_t smem = (size_t)(128 + N) * K * 2 + 1024;
     cudaError_t e = cudaFuncSetAttribute(probe_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return vg_fail(VG_ERR_CUDA, "umma probe smem: %s", cudaGetErrorString(e));
     probe_umma_kernel<<<1, 128, smem, (cudaStream_t)stream>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B,
-                                                              D, N, K, ncols, status);
+                                                              D, N, K, ncols, a_mn, b_mn, status);
     VG_LAUNCH_CHECK();
     return VG_OK;
 }
