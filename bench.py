@@ -212,10 +212,13 @@ def gpu_arm(args):
         t0 = time.perf_counter()
         r3 = integ3(f, nitn=5000, rtol=1e-4)
         torch.cuda.synchronize()
-        tta = {'seconds': time.perf_counter() - t0, 'iterations': r3.nitn,
-               'result': str(r3), 'rel_err': r3.sdev / abs(r3.mean),
-               'exact': exact, 'pull': (r3.mean - exact) / r3.sdev,
-               'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}
+        tta = {'ridge_plain': {
+            'seconds': time.perf_counter() - t0, 'iterations': r3.nitn,
+            'result': str(r3), 'rel_err': r3.sdev / abs(r3.mean),
+            'exact': exact, 'pull': (r3.mean - exact) / r3.sdev,
+            'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
+        if rank == 0:
+            tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
     if world > 1:
         dist.destroy_process_group()
     if rank != 0:
@@ -242,6 +245,92 @@ def gpu_arm(args):
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)
     print(json.dumps(out))
+
+
+MIX_DIM, MIX_NEVAL = 8, 1 << 20
+MIX_WORKLOAD = ('flow-augmented vegas+: dim=8, equal-weight mixture of 4 normalised Gaussians '
+                '(sigma=0.03) at seeded centres U[0.15,0.85]^8 (numpy default_rng(4)), 2^20 '
+                'evaluations/itn; flow: 6 coupling layers, 32-bin piecewise-quadratic splines, '
+                'conditioner MLP 2x128 BF16 on tcgen05 tensor cores')
+
+
+def mixture_integrand():
+    import numpy as np
+    import vegas_gb300 as vg
+    rng = np.random.default_rng(4)
+    return vg.GaussianMixture(rng.uniform(0.15, 0.85, (4, MIX_DIM)), sigma=0.03)
+
+
+def _tta_run(step, warm_itn, cap_s, target=1e-4):
+    """Wall-clock time until the running result (iterations after the first
+    warm_itn) reaches target relative error.  step() runs one iteration and
+    returns (mean, var, neval).  Past cap_s the time is extrapolated with the
+    1/n error law from the accumulated precision."""
+    import torch
+    from vegas_gb300 import RAvg, gvar
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(warm_itn):
+        step()
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    r = RAvg()
+    neval = 0
+    while True:
+        m, v, ne = step()
+        r.add(gvar(m, max(v, 0.0) ** 0.5))
+        neval += ne
+        rel = r.sdev / abs(r.mean) if r.mean != 0 else float('inf')
+        t = time.perf_counter() - t0
+        if rel <= target or t > cap_s:
+            break
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    t_acc = t - t_warm
+    est = t if rel <= target else t_warm + t_acc * (rel / target) ** 2
+    return {'seconds': est, 'measured_seconds': t, 'extrapolated': rel > target,
+            'warmup_seconds': t_warm, 'warmup_iterations': warm_itn, 'iterations': r.nitn,
+            'evaluations': neval, 'result': str(r), 'mean': r.mean, 'sdev': r.sdev, 'rel_err': rel,
+            'var_per_eval': (r.sdev ** 2) * neval,
+            'chi2_dof': (r.chi2 / r.dof if r.dof > 0 else 0.0)}
+
+
+def tta_flow_vs_plain(dev, cap_s=30.0):
+    """Time to 1e-4 relative error on the flow workload: plain vegas+ (fused
+    kernel path) against flow-augmented vegas+ (FlowIntegrator)."""
+    import vegas_gb300 as vg
+    from vegas_gb300.flow_vegas import FlowIntegrator
+    f = mixture_integrand()
+    exact = f.exact(MIX_DIM)
+    lim = MIX_DIM * [[0.0, 1.0]]
+    plain = vg.Integrator(lim, neval=MIX_NEVAL, seed=777, device=dev)
+
+    def pstep():
+        old = plain.nitn
+        plain.nitn = 1
+        rr = plain(f)
+        plain.nitn = old
+        v = rr.itn_results[-1]
+        return v.mean, v.sdev ** 2, plain.last_neval
+
+    out = {'workload': MIX_WORKLOAD, 'exact': exact}
+    out['plain'] = _tta_run(pstep, 10, cap_s)
+    fi = FlowIntegrator(lim, neval=MIX_NEVAL, seed=777, device=dev, plain_itn=10, kl_itn=10,
+                        train_itn=40, grace=10, patience=3, train_steps=4, train_batch=1 << 15,
+                        lr=1e-3)
+
+    def fstep():
+        fi(f, nitn=1)
+        h = fi.history[-1]
+        return h['mean'], h['sdev'] ** 2, h['neval']
+
+    out['flow'] = _tta_run(fstep, 50, cap_s)
+    out['flow']['flow_active_at_end'] = bool(fi.flow_on)
+    for k in ('plain', 'flow'):
+        r = out[k]
+        r['pull'] = (r['mean'] - exact) / r['sdev'] if r['sdev'] > 0 else None
+    out['speedup'] = out['plain']['seconds'] / out['flow']['seconds']
+    return out
 
 
 def measure_ex2_peak(L, dev):

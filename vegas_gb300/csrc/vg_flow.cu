@@ -811,45 +811,91 @@ __global__ void flow_adam_kernel(int64_t np, float *__restrict__ theta, const fl
 template <int K, int DIR>
 __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, float &lp)
 {
+    // Written for instruction-level parallelism (8 warps per SM): every
+    // reduction runs as 4 independent chains, and the bin search runs per
+    // block of 8 bins in parallel, the first block with a hit winning.
+    static_assert(K % 8 == 0, "K must be a multiple of 8");
+    constexpr int NB = K / 8;
     constexpr float c1 = 1.f - K * EPS_W;
-    float mx = o[0];
+    float m4[4], v4[4];
 #pragma unroll
-    for (int k = 1; k < K; k++) mx = fmaxf(mx, o[k]);
-    float mv = o[K];
+    for (int q = 0; q < 4; q++) {
+        m4[q] = o[q];
+        v4[q] = o[K + q];
+    }
 #pragma unroll
-    for (int k = 1; k <= K; k++) mv = fmaxf(mv, o[K + k]);
-    float se = 0.f;
+    for (int k = 4; k < K; k++) m4[k & 3] = fmaxf(m4[k & 3], o[k]);
+#pragma unroll
+    for (int k = 4; k <= K; k++) v4[k & 3] = fmaxf(v4[k & 3], o[K + k]);
+    const float mx = fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3]));
+    const float mv = fmaxf(fmaxf(v4[0], v4[1]), fmaxf(v4[2], v4[3]));
+    float s4[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < K; k++) {
         o[k] = __expf(o[k] - mx);
-        se += o[k];
+        s4[k & 3] += o[k];
     }
-    const float cw = __fdividef(c1, se);
+    const float cw = __fdividef(c1, (s4[0] + s4[1]) + (s4[2] + s4[3]));
 #pragma unroll
     for (int k = 0; k < K; k++) o[k] = fmaf(cw, o[k], EPS_W);   // bin widths
 #pragma unroll
     for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);   // vertex heights (unnormalised)
-    float Z = 0.f;
+    float seg[K];
+    float EB[NB], PB[NB];
 #pragma unroll
-    for (int k = 0; k < K; k++) Z = fmaf(0.5f * (o[K + k] + o[K + k + 1]), o[k], Z);
-    const float t = DIR == 0 ? x : x * Z;
-    float E = 0.f, P = 0.f, Wb = o[K - 1], ub = o[2 * K - 1], ub1 = o[2 * K], Eb = 0.f, Pb = 0.f;
-    bool found = false;
+    for (int b = 0; b < NB; b++) {
+        EB[b] = 0.f;
+        PB[b] = 0.f;
+    }
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        const float W = o[k];
-        const float seg = 0.5f * (o[K + k] + o[K + k + 1]) * W;
-        const bool here = !found && (k == K - 1 || (DIR == 0 ? (t < E + W) : (t < P + seg)));
-        if (here) {
-            Wb = W;
-            ub = o[K + k];
-            ub1 = o[K + k + 1];
-            Eb = E;
-            Pb = P;
-            found = true;
+        seg[k] = 0.5f * (o[K + k] + o[K + k + 1]) * o[k];
+        EB[k >> 3] += o[k];
+        PB[k >> 3] += seg[k];
+    }
+    float Es[NB], Ps[NB];
+    Es[0] = 0.f;
+    Ps[0] = 0.f;
+#pragma unroll
+    for (int b = 1; b < NB; b++) {
+        Es[b] = Es[b - 1] + EB[b - 1];
+        Ps[b] = Ps[b - 1] + PB[b - 1];
+    }
+    const float Z = Ps[NB - 1] + PB[NB - 1];
+    const float t = DIR == 0 ? x : x * Z;
+    // per-block search
+    float bW[NB], bu[NB], bu1[NB], bE[NB], bP[NB];
+    bool bf[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) {
+        float E = Es[b], P = Ps[b];
+        bool f = false;
+        const int kl = 8 * b + 7;   // default: last bin of the block
+        float cW = o[kl], cu = o[K + kl], cu1 = o[K + kl + 1], cE = Es[b] + EB[b] - o[kl],
+              cP = Ps[b] + PB[b] - seg[kl];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int k = 8 * b + q;
+            const bool here = !f && (DIR == 0 ? (t < E + o[k]) : (t < P + seg[k]));
+            cW = here ? o[k] : cW;
+            cu = here ? o[K + k] : cu;
+            cu1 = here ? o[K + k + 1] : cu1;
+            cE = here ? E : cE;
+            cP = here ? P : cP;
+            f = f || here;
+            E += o[k];
+            P += seg[k];
         }
-        E += W;
-        P += seg;
+        bW[b] = cW; bu[b] = cu; bu1[b] = cu1; bE[b] = cE; bP[b] = cP; bf[b] = f;
+    }
+    float Wb = bW[NB - 1], ub = bu[NB - 1], ub1 = bu1[NB - 1], Eb = bE[NB - 1], Pb = bP[NB - 1];
+#pragma unroll
+    for (int b = NB - 2; b >= 0; b--) {   // the first block with a hit wins
+        Wb = bf[b] ? bW[b] : Wb;
+        ub = bf[b] ? bu[b] : ub;
+        ub1 = bf[b] ? bu1[b] : ub1;
+        Eb = bf[b] ? bE[b] : Eb;
+        Pb = bf[b] ? bP[b] : Pb;
     }
     float al, xo;
     if (DIR == 0) {
@@ -971,13 +1017,17 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     umma::bulk_g2s(umma::smem_u32(sW3) + off, (const uint8_t *)(mirror + y.mU3) + off, sz, bar_w);
                 }
             }
-            for (int i = tid; i < FH * dA; i += FNT) sW1[i] = theta[y.oW1 + i];
+            for (int i = tid; i < FH * 8; i += FNT) {   // W1 padded to 8 columns: [128][8]
+                const int c = i >> 3, a = i & 7;
+                sW1[i] = a < dA ? theta[y.oW1 + c * dA + a] : 0.f;
+            }
             for (int i = tid; i < FH; i += FNT) {
                 sb1[i] = theta[y.ob1 + i];
                 sb2[i] = theta[y.ob2 + i];
             }
             for (int i = tid; i < y.dB * NR; i += FNT) sb3[i] = theta[y.ob3 + i];
-            if (!umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
+            // one thread waits on the mbarrier; the others park at the CTA barrier
+            if (tid == 0 && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
             ph_w ^= 1;
             __syncthreads();
             if (abort_flag) { aborted = true; break; }
@@ -995,12 +1045,29 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     float xa[8];
 #pragma unroll
                     for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? Zs[r * zst + y.A[a]] : 0.f;
+                    const bool wide = dA > 4;
+#pragma unroll 2
                     for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 8) {
                         float v[8];
+                        const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
+                        const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
+                        v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
+                        v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
 #pragma unroll
                         for (int q = 0; q < 8; q++) {
-                            float acc = sb1[c0 + q];
-                            for (int a = 0; a < dA; a++) acc = fmaf(sW1[(c0 + q) * dA + a], xa[a], acc);
+                            const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
+                            float acc = v[q];
+                            acc = fmaf(w0.x, xa[0], acc);
+                            acc = fmaf(w0.y, xa[1], acc);
+                            acc = fmaf(w0.z, xa[2], acc);
+                            acc = fmaf(w0.w, xa[3], acc);
+                            if (wide) {
+                                const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
+                                acc = fmaf(w1.x, xa[4], acc);
+                                acc = fmaf(w1.y, xa[5], acc);
+                                acc = fmaf(w1.z, xa[6], acc);
+                                acc = fmaf(w1.w, xa[7], acc);
+                            }
                             v[q] = fmaxf(acc, 0.f);
                         }
                         uint4 pk;
@@ -1019,8 +1086,9 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     umma::gemm_128xN(tmem, umma::smem_u32(sA), umma::smem_u32(sW2), FH, FH, FH, 0);
                     umma::mma_commit(bar_h);
                 }
-                if (!umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
+                if (tid == 0 && !umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
                 ph_h ^= 1;
+                __syncthreads();
                 umma::fence_after_sync();
                 // ---- H2 epilogue: TMEM -> +b2, relu -> A operand
                 for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
@@ -1030,10 +1098,12 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     for (int q8 = 0; q8 < 32; q8 += 8) {
                         uint4 pk;
                         const int c = c0 + q8;
-                        pk.x = pack_bf16(fmaxf(v[q8 + 0] + sb2[c + 0], 0.f), fmaxf(v[q8 + 1] + sb2[c + 1], 0.f));
-                        pk.y = pack_bf16(fmaxf(v[q8 + 2] + sb2[c + 2], 0.f), fmaxf(v[q8 + 3] + sb2[c + 3], 0.f));
-                        pk.z = pack_bf16(fmaxf(v[q8 + 4] + sb2[c + 4], 0.f), fmaxf(v[q8 + 5] + sb2[c + 5], 0.f));
-                        pk.w = pack_bf16(fmaxf(v[q8 + 6] + sb2[c + 6], 0.f), fmaxf(v[q8 + 7] + sb2[c + 7], 0.f));
+                        const float4 bl = *reinterpret_cast<const float4 *>(sb2 + c);
+                        const float4 bh = *reinterpret_cast<const float4 *>(sb2 + c + 4);
+                        pk.x = pack_bf16(fmaxf(v[q8 + 0] + bl.x, 0.f), fmaxf(v[q8 + 1] + bl.y, 0.f));
+                        pk.y = pack_bf16(fmaxf(v[q8 + 2] + bl.z, 0.f), fmaxf(v[q8 + 3] + bl.w, 0.f));
+                        pk.z = pack_bf16(fmaxf(v[q8 + 4] + bh.x, 0.f), fmaxf(v[q8 + 5] + bh.y, 0.f));
+                        pk.w = pack_bf16(fmaxf(v[q8 + 6] + bh.z, 0.f), fmaxf(v[q8 + 7] + bh.w, 0.f));
                         *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(FH, r, c)) = pk;
                     }
                 }
@@ -1058,10 +1128,14 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                 }
                 for (int gi = 0; gi < ngroups; gi++) {
                     const int buf = gi & 1;
-                    bool ok;
-                    if (buf == 0) { ok = umma::mbar_wait(bar_o0, ph_o0); ph_o0 ^= 1; }
-                    else { ok = umma::mbar_wait(bar_o0 + 8u, ph_o1); ph_o1 ^= 1; }
-                    if (!ok) abort_flag = 1;
+                    if (tid == 0) {
+                        const bool okw = buf == 0 ? umma::mbar_wait(bar_o0, ph_o0) : umma::mbar_wait(bar_o0 + 8u, ph_o1);
+                        if (!okw) abort_flag = 1;
+                    }
+                    if (buf == 0) ph_o0 ^= 1;
+                    else ph_o1 ^= 1;
+                    __syncthreads();
+                    const bool ok = abort_flag == 0;
                     umma::fence_after_sync();
                     const int j = 2 * gi + h;
                     if (ok && j < y.dB) {
@@ -1184,10 +1258,19 @@ static int flow_pass_umma_k(const FlowGeom &g, const vg_flow *fl, int dir, int64
                             float *zout, float *logdet, float *zl, cudaStream_t st, int *rc)
 {
     const size_t limit = VG_FLOW_SMEM_MAX;
-    int ST = UST_MAX;
-    while (ST > 1 && umma_plan(g, ST).total > limit) ST--;
+    int STmax = UST_MAX;
+    while (STmax > 1 && umma_plan(g, STmax).total > limit) STmax--;
+    if (umma_plan(g, STmax).total > limit) return 0;
+    // super-tile size: as large as shared memory allows (weights are fetched
+    // once per layer and super-tile), but small enough that the static
+    // round-robin over CTAs ends within one super-tile of balance
+    const int64_t nsub_total = (n + FROWS - 1) / FROWS;
+    const int64_t G = vg_num_sms();
+    const int64_t rounds = (nsub_total + G * STmax - 1) / (G * STmax);
+    int ST = (int)((nsub_total + G * rounds - 1) / (G * rounds));
+    if (ST < 1) ST = 1;
+    if (ST > STmax) ST = STmax;
     const UmmaPlan pl = umma_plan(g, ST);
-    if (pl.total > limit) return 0;
     size_t smem = pl.total < 120 * 1024 ? 120 * 1024 : pl.total;   // one CTA per SM (TMEM: 512 columns)
     const void *k = dir == 0 ? (const void *)flow_pass_umma_kernel<K, 0> : (const void *)flow_pass_umma_kernel<K, 1>;
     if ((*rc = set_smem(k, smem))) return 1;

@@ -61,6 +61,8 @@ class FlowIntegrator(object):
         lr: Adam learning rate.
         plain_itn: iterations of plain vegas+ before the flow starts.
         kl_itn: first flow iterations trained with KL weights (then chi^2).
+        train_itn: flow iterations that train the flow; later ones only
+            sample with it (None: train on every flow iteration).
         grace: first flow iterations that are not judged.
         patience: judged flow iterations that may lose in a row.
         gate: 'eval' (variance per evaluation) or 'time' (variance x seconds
@@ -70,8 +72,8 @@ class FlowIntegrator(object):
     """
 
     def __init__(self, limits, nlayers=6, K=32, train_batch=1 << 15, train_steps=4, lr=1e-3,
-                 plain_itn=10, kl_itn=10, grace=10, patience=3, gate='eval', flow_seed=0,
-                 device=None, **kargs):
+                 plain_itn=10, kl_itn=10, train_itn=None, grace=10, patience=3, gate='eval',
+                 flow_seed=0, device=None, **kargs):
         kargs.setdefault('precision', 'fp32')
         if kargs['precision'] != 'fp32':
             raise ValueError('the flow path computes in FP32 (precision="fp32")')
@@ -83,6 +85,7 @@ class FlowIntegrator(object):
         self.train_steps = int(train_steps)
         self.plain_itn = int(plain_itn)
         self.kl_itn = int(kl_itn)
+        self.train_itn = None if train_itn is None else int(train_itn)
         self.grace = int(grace)
         self.patience = int(patience)
         if gate not in ('eval', 'time'):
@@ -207,7 +210,8 @@ class FlowIntegrator(object):
             t0 = time.perf_counter()
             if use_flow:
                 self._flow_nit += 1
-                mean, var, neval = self._flow_iteration(fcn, train)
+                tr = train and (self.train_itn is None or self._flow_nit <= self.train_itn)
+                mean, var, neval = self._flow_iteration(fcn, tr)
             else:
                 mean, var, neval = self._plain_iteration(fcn)
             sec = time.perf_counter() - t0
