@@ -49,6 +49,11 @@ def parse():
     ap.add_argument('--no-tta', action='store_true')
     ap.add_argument('--device-loop-only', action='store_true',
                     help='run only the device-resident iteration loop (for profilers)')
+    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch'],
+                    help='with --device-loop-only: which kernel family to run (for profilers): '
+                         'ridge = the fused vegas+ iteration, flow = the flow sampling pass '
+                         '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals')
+    ap.add_argument('--no-batch', action='store_true', help='skip the batched many-integral line')
     return ap.parse_args()
 
 
@@ -107,6 +112,80 @@ class ClockSampler(object):
 
 
 # --------------------------------------------------------------- GPU arm
+def profile_case(args, dev):
+    """Short device loops of one kernel family, for ncu captures."""
+    import torch
+    if args.case == 'flow':
+        from vegas_gb300.flow import Flow
+        fl = Flow(8, seed=1, device=dev)
+        g = torch.Generator(device=dev).manual_seed(0)
+        fl.theta.add_(0.05 * torch.randn(fl.theta.shape, device=dev, generator=g))  # non-uniform splines
+        fl.refresh()
+        u = torch.rand(1 << 18, 8, device=dev, generator=g)
+        for _ in range(args.warmup + args.steps):
+            fl.sample(u)
+    elif args.case == 'batch':
+        from vegas_gb300.batch import BatchIntegrator
+        fs, nevals, _ = batch_workload(256)
+        B = BatchIntegrator(fs, nevals, nitn=2, nwarm=1, seed=99, device=dev, variant=0)
+        for _ in range(args.warmup + args.steps):
+            B.launch()
+    torch.cuda.synchronize()
+
+
+def batch_workload(njobs=4096, seed=2024):
+    """The batched workload: Lorentzian products, dim ~ U{3..9}, centres
+    U[0.2,0.8]^d, widths log-U[0.01,0.1], neval log-U[1e4,1e6] (seeded)."""
+    import numpy as np
+    import vegas_gb300 as vg
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(3, 10, njobs)
+    fs = []
+    for d in dims:
+        c = rng.uniform(0.2, 0.8, int(d))
+        w = np.exp(rng.uniform(np.log(0.01), np.log(0.1), int(d)))
+        fs.append(vg.LorentzianProduct(c, w))
+    nevals = np.exp(rng.uniform(np.log(1e4), np.log(1e6), njobs)).astype(np.int64)
+    return fs, nevals, dims
+
+
+def batched_line(dev, reps=2):
+    """4096 integrals x (8 + 8) iterations in one persistent launch per
+    replay of a CUDA graph; evals/s over the whole job and the pulls against
+    the closed form."""
+    import numpy as np
+    import torch
+    from vegas_gb300.batch import BatchIntegrator
+    fs, nevals, dims = batch_workload()
+    t0 = time.perf_counter()
+    B = BatchIntegrator(fs, nevals, nitn=16, nwarm=8, seed=99, device=dev)
+    t_setup = time.perf_counter() - t0
+    B.capture()
+    B._graph.replay()                     # warm-up replay (adapts the maps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        B._graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3 / reps
+    res = B.results()
+    exact = np.array([f.exact(int(d)) for f, d in zip(fs, dims)])
+    pulls = (res[:, 0] - exact) / res[:, 1]
+    return {
+        'workload': '4096 Lorentzian-product integrals, dim U{3..9}, centres U[0.2,0.8]^d, widths '
+                    'log-U[0.01,0.1], neval log-U[1e4,1e6] per integral, nitn 8+8, one persistent '
+                    'kernel per 16 iterations replayed from a CUDA graph, FP32 eval + FP64 sums',
+        'evals_per_launch': B.evaluations(), 'seconds_per_launch': secs,
+        'value': B.evaluations() / secs, 'unit': 'evals/s', 'variant': B.variant,
+        'autotune_seconds': {str(k): v for k, v in getattr(B, 'tuning', {}).items()},
+        'setup_seconds': t_setup, 'integrals': len(fs),
+        'pull_rms': float(np.sqrt(np.mean(pulls ** 2))), 'pull_max_abs': float(np.max(np.abs(pulls))),
+        'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
+    }
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -122,6 +201,9 @@ def gpu_arm(args):
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     L = N.load()
+    if args.device_loop_only and args.case != 'ridge':
+        profile_case(args, dev)
+        return
 
     def barrier():
         if world > 1:
@@ -219,6 +301,9 @@ def gpu_arm(args):
             'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
         if rank == 0:
             tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
+    batched = None
+    if not args.no_batch and rank == 0:
+        batched = batched_line(dev)
     if world > 1:
         dist.destroy_process_group()
     if rank != 0:
@@ -241,6 +326,7 @@ def gpu_arm(args):
                                     % ex2_per_launch},
         'clocks': clk,
         'time_to_1e-4': tta,
+        'batched': batched,
     }
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)

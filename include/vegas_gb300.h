@@ -251,6 +251,20 @@ int vg_flow_density(const vg_flow *fl, int64_t n, const float *z, float *zhat, f
  * (and the loss into fl->loss): forward and backward kernels, BF16 MMAs. */
 int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const float *w, void *work,
                  size_t work_bytes, void *stream);
+/*
+ * Training batch for the flow from one iteration's samples: m samples drawn
+ * uniformly (Philox keyed by seed, step) from the n samples of the
+ * iteration; zs[m,dim] = z of the drawn samples, ws[m] = their weights
+ * normalised to mean 1: (|f_i| wgt_i)^2 neval_h[hc_i] (chi2 != 0: variance
+ * loss) or |f_i| wgt_i (KL), where f is the integrand seen by the
+ * stratification, wgt the sampler's weight and hc the hypercube.  scratch:
+ * device doubles [m + 1].  Two kernels, no host synchronisation.
+ */
+int vg_flow_train_batch(int64_t n, int64_t m, uint64_t seed, uint32_t step, int dim, const float *z,
+                        const float *f, const double *wgt, const int64_t *hc, const int32_t *neval_h,
+                        int chi2, float *zs, float *ws, double *scratch, void *stream);
+/* grad = 0, loss = 0 (before accumulating a new gradient). */
+int vg_flow_zero_grad(const vg_flow *fl, void *stream);
 /* Adam step on theta with gradient grad*scale (clipped at +-clip), then refresh. */
 int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta1, float beta2, float eps,
                  int step, float clip, void *stream);
@@ -264,15 +278,48 @@ int vg_flow_set_path(int legacy);
 
 /*
  * Built-in integrand at given points (FP32): f[i] = vol * f(lo + width * z_i)
- * * exp(-logdet[i]) with z[n,dim] on the unit cube, vol = prod(width),
+ * * jac[i] * exp(-logdet[i]) with z[n,dim], vol = prod(width), jac and
  * logdet optional (NULL).  The evaluation step of the flow path, where the
- * points come from vg_sample + vg_flow_sample instead of the fused kernel.
- * Replaces the integrand call of Integrator.__call__ (_vegas.pyx:2126-2129)
- * for the built-in integrands.  lo, width: host arrays [dim].
+ * points come from the sampler, the flow and the map instead of the fused
+ * kernel.  Replaces the integrand call of Integrator.__call__
+ * (_vegas.pyx:2126-2129) for the built-in integrands.  lo, width: host
+ * arrays [dim].
  */
 int vg_eval_points(int kind, const double *params, int nparams, int dim, int64_t n,
                    const float *z, const double *lo, const double *width, const float *logdet,
-                   float *f, void *stream);
+                   const float *jac, float *f, void *stream);
+/* out[i] = f[i] * jac[i] * exp(-logdet[i]) for integrand values computed by
+ * the caller (jac, logdet optional). */
+int vg_weight_points(int64_t n, const float *f, const float *jac, const float *logdet, float *out,
+                     void *stream);
+
+/* ----------------------------------------------- many integrals, one launch */
+/*
+ * Batched vegas+ (no counterpart in the reference, which integrates one
+ * integrand per Integrator call): njobs independent integrals -- each
+ * described by its own vg_integrator (dimension <= 16, FP32, its own device
+ * grid, inc, sigf, training histogram, stats and workspace) and built-in
+ * integrand parameters (Lorentzian products: params + j*ldp, nparams[j]
+ * values) -- run nitn iterations each in ONE persistent kernel: one CTA per
+ * integral at a time, integrals taken from a queue in the order `order`
+ * (device int[njobs], e.g. largest first).  Each iteration is the same
+ * allocation / fused evaluation + reduction / adapt as vg_fused_iteration;
+ * out (device double[njobs][nitn][2]) receives every iteration's mean and
+ * variance, res (device double[njobs][4]) the weighted average over the
+ * iterations after the first nwarm (mean, sdev, chi2, dof).  stats->sum_sigf
+ * of each integral must hold its starting value (nhcube for a fresh one).
+ * vg_batch_prepare copies the job table (vg_batch_table_bytes) to the device
+ * and returns the launch's dynamic shared memory and grid for the tile
+ * variant (0 .. vg_batch_variants()-1); vg_batch_launch neither allocates
+ * nor synchronises, so it can be captured in a CUDA graph.
+ */
+int vg_batch_variants(void);
+size_t vg_batch_table_bytes(int njobs);
+int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
+                     const int *nparams, int nitn, double *out, double *res, int variant, void *table,
+                     size_t table_bytes, size_t *smem, int *grid, void *stream);
+int vg_batch_launch(const void *table, int njobs, int nitn, int nwarm, uint32_t itn0, const int *order,
+                    unsigned int *queue, size_t smem, int grid, int variant, void *stream);
 
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */

@@ -157,7 +157,14 @@ SIGNATURES = {
                            ctypes.c_float, I32, ctypes.c_float, P]),
     'vg_flow_status': (I32, [P, I32]),
     'vg_flow_set_path': (I32, [I32]),
-    'vg_eval_points': (I32, [I32, P, I32, I32, I64, P, P, P, P, P, P]),
+    'vg_batch_variants': (I32, []),
+    'vg_batch_table_bytes': (SZ, [I32]),
+    'vg_batch_prepare': (I32, [P, I32, I32, P, I32, P, I32, P, P, I32, P, SZ, P, P, P]),
+    'vg_batch_launch': (I32, [P, I32, I32, I32, U32, P, P, SZ, I32, I32, P]),
+    'vg_eval_points': (I32, [I32, P, I32, I32, I64, P, P, P, P, P, P, P]),
+    'vg_weight_points': (I32, [I64, P, P, P, P, P]),
+    'vg_flow_zero_grad': (I32, [P, P]),
+    'vg_flow_train_batch': (I32, [I64, I64, U64, U32, I32, P, P, P, P, P, I32, P, P, P, P]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),

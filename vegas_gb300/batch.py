@@ -1,0 +1,246 @@
+"""Many independent vegas+ integrals in one persistent GPU launch.
+
+No counterpart in the reference (one ``Integrator`` call integrates one
+integrand).  ``BatchIntegrator`` holds the state of every integral -- the
+same per-integral state an ``Integrator`` has (AdaptiveMap grid, strata and
+their sigf, training histogram, iteration record) -- in a few device arenas,
+and runs ``nitn`` vegas+ iterations of all of them in one kernel
+(``vg_batch_launch``), optionally replayed from a CUDA graph.  The tile
+shape of that kernel is picked by a small autotuner that times each variant
+on a sample of the integrals.
+"""
+import ctypes
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .adaptive_map import _device
+from .integrands import LorentzianProduct
+from .integrator import strata
+
+_LDP = 32   # parameters per integral in the packed table (Lorentzian: 2*dim <= 32)
+
+
+def _align(n, a=256):
+    return (n + a - 1) // a * a
+
+
+class BatchIntegrator(object):
+    """vegas+ on many integrals of Lorentzian products over unit cubes.
+
+    Args:
+        integrands: list of ``LorentzianProduct`` (dimension <= 16 each).
+        nevals: evaluations per iteration of each integral.
+        nitn, nwarm: iterations per launch and warm-up iterations excluded
+            from the weighted average (the reference's ``nitn`` of an adapt
+            call followed by a final call).
+        alpha, beta, seed: as ``Integrator``; integral j uses Philox stream j.
+        variant: tile variant of the kernel (None: autotune).
+    """
+
+    def __init__(self, integrands, nevals, nitn=16, nwarm=8, alpha=0.5, beta=0.75, seed=1,
+                 variant=None, device=None, neval_frac=0.75, max_neval_hcube=50000):
+        self.device = _device(device)
+        self.integrands = list(integrands)
+        self.njobs = len(self.integrands)
+        if self.njobs < 1:
+            raise ValueError('no integrands')
+        for f in self.integrands:
+            if not isinstance(f, LorentzianProduct):
+                raise NotImplementedError('batched launch: LorentzianProduct integrands only')
+        self.nitn, self.nwarm = int(nitn), int(nwarm)
+        if not 0 <= self.nwarm < self.nitn:
+            raise ValueError('need 0 <= nwarm < nitn')
+        self.alpha, self.beta, self.seed = float(alpha), float(beta), int(seed)
+        self.neval_frac, self.max_neval_hcube = float(neval_frac), int(max_neval_hcube)
+        self.dims = np.array([len(f.c) for f in self.integrands], np.int64)
+        if self.dims.max() > 16:
+            raise NotImplementedError('batched launch: dimension <= 16')
+        self._layout(np.asarray(nevals, np.int64))
+        self._itn = 0
+        self.variant = None
+        self._graph = None
+        if variant is None:
+            variant = self.autotune()
+        self.set_variant(variant)
+
+    # ------------------------------------------------------------- layout
+    def _layout(self, nevals):
+        L = N.load()
+        nj = self.njobs
+        self.its = (N.VgIntegrator * nj)()
+        sizes = []
+        self.nstrat, self.ninc, self.nhcube, self.neval = [], [], [], []
+        for j in range(nj):
+            d = int(self.dims[j])
+            sz = strata(d, 0, int(nevals[j]), True, np.zeros(d, np.int64), self.neval_frac, self.beta)
+            it = self.its[j]
+            it.dim = d
+            it.precision = N.VG_F32
+            H = int(np.prod(sz['nstrat']))
+            it.nhcube = H
+            K = int(sz['ninc'].max())
+            for k in range(d):
+                it.nstrat[k] = int(sz['nstrat'][k])
+                it.ninc[k] = int(sz['ninc'][k])
+            it.ldg, it.ldi = K + 1, K
+            it.neval = sz['neval']
+            it.neval_frac = self.neval_frac
+            it.min_neval_hcube = sz['min_neval_hcube']
+            it.max_neval_hcube = self.max_neval_hcube
+            it.alpha, it.beta = self.alpha, self.beta
+            it.adapt = 1
+            it.adapt_to_errors = 0
+            it.seed = self.seed & ((1 << 64) - 1)
+            it.stream_id = j
+            it.tile = 0
+            work = int(L.vg_workspace_bytes(ctypes.byref(it), 0))
+            sizes.append((d * (K + 1) * 8, d * K * 8, H * 8, d * K * 8, d * K * 8,
+                          ctypes.sizeof(N.VgStats), work))
+            self.nstrat.append(sz['nstrat'])
+            self.ninc.append(sz['ninc'])
+            self.nhcube.append(H)
+            self.neval.append(sz['neval'])
+        offs = []
+        o = 0
+        for s in sizes:
+            row = []
+            for b in s:
+                row.append(o)
+                o = _align(o + b)
+            offs.append(row)
+        self.arena = torch.zeros(o, dtype=torch.uint8, device=self.device)
+        base = self.arena.data_ptr()
+        host_init = []
+        for j in range(nj):
+            it = self.its[j]
+            og, oi, osg, osf, onf, ost, ow = offs[j]
+            it.grid, it.inc, it.sigf = base + og, base + oi, base + osg
+            it.sum_f, it.n_f, it.stats = base + osf, base + onf, base + ost
+            it.work, it.work_bytes = base + ow, sizes[j][6]
+            host_init.append((j, og, oi, osg, ost))
+        # initial state: uniform grids, sigf = 1, sum_sigf = nhcube
+        arena = self.arena
+        for j, og, oi, osg, ost in host_init:
+            d, K = int(self.dims[j]), int(self.its[j].ldi)
+            g = np.zeros((d, K + 1))
+            inc = np.zeros((d, K))
+            for k in range(d):
+                nk = int(self.ninc[j][k])
+                g[k, :nk + 1] = np.linspace(0.0, 1.0, nk + 1)
+                inc[k, :nk] = np.diff(g[k, :nk + 1])
+            arena[og:og + g.nbytes].copy_(torch.from_numpy(g.view(np.uint8).reshape(-1)))
+            arena[oi:oi + inc.nbytes].copy_(torch.from_numpy(inc.view(np.uint8).reshape(-1)))
+            H = self.nhcube[j]
+            arena[osg:osg + 8 * H].view(torch.float64).fill_(1.0)
+            st = N.VgStats()
+            st.sum_sigf = float(H)
+            arena[ost:ost + ctypes.sizeof(st)].copy_(
+                torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8))
+        self._stats_off = [h[4] for h in host_init]
+        # integrand parameters, outputs, job table, queue order
+        self.params = np.zeros((nj, _LDP))
+        self.nparams = np.zeros(nj, np.int32)
+        for j, f in enumerate(self.integrands):
+            p = f.params(int(self.dims[j]))
+            self.params[j, :len(p)] = p
+            self.nparams[j] = len(p)
+        self.out = torch.zeros((nj, self.nitn, 2), dtype=torch.float64, device=self.device)
+        self.res = torch.zeros((nj, 4), dtype=torch.float64, device=self.device)
+        self.table = torch.empty(int(L.vg_batch_table_bytes(nj)), dtype=torch.uint8, device=self.device)
+        cost = np.array([self.neval[j] * (1 + self.dims[j]) for j in range(nj)])
+        self.order = torch.tensor(np.argsort(-cost, kind='stable').astype(np.int32), device=self.device)
+        self.queue = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+    # ----------------------------------------------------------- launching
+    def set_variant(self, variant):
+        L = N.load()
+        smem = ctypes.c_size_t(0)
+        grid = ctypes.c_int(0)
+        N.check(L.vg_batch_prepare(ctypes.cast(self.its, ctypes.c_void_p), self.njobs, N.VG_F_LORENTZ,
+                                   self.params.ctypes.data_as(ctypes.c_void_p), _LDP,
+                                   self.nparams.ctypes.data_as(ctypes.c_void_p), self.nitn,
+                                   N.ptr(self.out), N.ptr(self.res), int(variant), N.ptr(self.table),
+                                   self.table.numel(), ctypes.byref(smem), ctypes.byref(grid),
+                                   N.stream_ptr(self.device)))
+        self.variant = int(variant)
+        self.smem = smem.value
+        self.grid = grid.value
+        self._graph = None
+
+    def launch(self):
+        """One persistent kernel: nitn iterations of every integral (asynchronous)."""
+        L = N.load()
+        N.check(L.vg_batch_launch(N.ptr(self.table), self.njobs, self.nitn, self.nwarm,
+                                  (self._itn + 1) & 0xffffffff, N.ptr(self.order), N.ptr(self.queue),
+                                  self.smem, self.grid, self.variant, N.stream_ptr(self.device)))
+        self._itn += self.nitn
+
+    def capture(self):
+        """Capture one launch in a CUDA graph (replayed by ``run(graph=True)``).
+        The iteration counter of a replayed graph is fixed at capture; every
+        replay continues from the state the previous one left."""
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.launch()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        self._graph = g
+        return g
+
+    def run(self, graph=False):
+        """Run nitn iterations of every integral; returns results (see results())."""
+        if graph:
+            if self._graph is None:
+                self.capture()
+            self._graph.replay()
+        else:
+            self.launch()
+        return self.results()
+
+    def results(self):
+        """Per integral: mean, sdev, chi2, dof of the weighted average over the
+        iterations after the warm-up ones (numpy [njobs, 4])."""
+        return self.res.cpu().numpy()
+
+    def iterations(self):
+        """Every iteration's (mean, variance) (numpy [njobs, nitn, 2])."""
+        return self.out.cpu().numpy()
+
+    def evaluations(self):
+        """Evaluations of the last launch summed over integrals and iterations."""
+        return int(sum(self.neval)) * self.nitn
+
+    # ------------------------------------------------------------ autotune
+    def autotune(self, sample=256, reps=2):
+        """Time every tile variant of the batched kernel on a sample of the
+        integrals (fresh copies, one launch each after a warm-up launch) and
+        return the fastest."""
+        L = N.load()
+        nv = int(L.vg_batch_variants())
+        rng = np.random.default_rng(12345)
+        idx = np.sort(rng.choice(self.njobs, size=min(sample, self.njobs), replace=False))
+        best, best_t = 0, float('inf')
+        self.tuning = {}
+        for v in range(nv):
+            probe = BatchIntegrator([self.integrands[i] for i in idx], [self.neval[i] for i in idx],
+                                    nitn=2, nwarm=1, alpha=self.alpha, beta=self.beta,
+                                    seed=self.seed, variant=v, device=self.device,
+                                    neval_frac=self.neval_frac, max_neval_hcube=self.max_neval_hcube)
+            probe.launch()
+            torch.cuda.synchronize(self.device)
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                probe.launch()
+            torch.cuda.synchronize(self.device)
+            t = (time.perf_counter() - t0) / reps
+            self.tuning[v] = t
+            if t < best_t:
+                best, best_t = v, t
+            del probe
+        return best

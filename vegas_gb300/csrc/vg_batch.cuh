@@ -1,0 +1,292 @@
+// vg_batch.cuh -- many independent vegas+ integrals in one persistent launch.
+//
+// One CTA runs one integral at a time, all of its iterations back to back:
+// allocation of evaluations to hypercubes (pyx:1692-1706), the fused tile
+// body of the single-integral kernel over all of the integral's tiles
+// (sampling, map, integrand, two-pass per-hypercube reduction, training
+// histogram), the merge of hypercubes cut by tile boundaries and the
+// iteration sums (finalize), AdaptiveMap.adapt (pyx:467-594), and at the end
+// the weighted average over the iterations after the warm-up ones
+// (RAvg.add, pyx:2392-2410) -- all in FP64 where the single-integral path
+// is.  CTAs take integrals from an atomic queue in an order given by the
+// host (largest first), so nothing crosses CTAs and the launch needs no
+// grid-wide synchronisation.
+#pragma once
+#include "vg_adapt.cuh"
+#include "vg_tile.cuh"
+
+namespace vgbatch {
+using namespace vg;
+
+struct BatchJob {
+    IterArgs a;                  // per-integral arguments (its own workspace)
+    vgadapt::AdaptArgs ad;       // adapt: grid -> scratch grid of the workspace
+    double *out;                 // [nitn][2] iteration mean, variance
+    double *res;                 // [4] weighted mean, sdev, chi2, dof
+    int dimb;                    // dimension bucket: 4, 8 or 16
+    int adapt;                   // adapt the map after each iteration
+};
+
+constexpr int APER = 4;          // hypercubes per thread and pass of the allocation
+
+// Allocation of one iteration by one CTA: neval_h, offsets, tile heads,
+// totals in the integral's stats (the three allocation kernels' work).
+static __device__ __noinline__ void cta_alloc(const IterArgs &a, int64_t *scan)
+{
+    const int tid = threadIdx.x;
+    vg_stats *st = a.stats;
+    const double sum_sigf = st->sum_sigf;
+    const double nsf = (a.beta > 0 && sum_sigf > 0)
+                           ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
+                           : 0.0;
+    const int64_t mx = a.max_neval_hcube > a.min_neval_hcube ? a.max_neval_hcube : a.min_neval_hcube;
+    const int64_t avg = (int64_t)((double)a.neval / (double)a.H);
+    int64_t run = 0, mxn = 0;
+    for (int64_t base = 0; base < a.H; base += (int64_t)NT * APER) {
+        int64_t loc[APER];
+        int64_t s = 0;
+#pragma unroll
+        for (int k = 0; k < APER; k++) {
+            const int64_t h = base + (int64_t)tid * APER + k;
+            int64_t n = 0;
+            if (h < a.H) {
+                if (a.adaptive_alloc) {
+                    n = (int64_t)__dmul_rn(a.sigf[h], nsf) + a.min_neval_hcube;
+                    if (n > mx) n = mx;
+                } else {
+                    n = avg;
+                }
+                mxn = n > mxn ? n : mxn;
+            }
+            loc[k] = n;
+            s += n;
+        }
+        scan[tid] = s;
+        __syncthreads();
+        for (int off = 1; off < NT; off <<= 1) {
+            const int64_t add = tid >= off ? scan[tid - off] : 0;
+            __syncthreads();
+            scan[tid] += add;
+            __syncthreads();
+        }
+        int64_t off = run + scan[tid] - s;
+        const int64_t total = scan[NT - 1];
+#pragma unroll
+        for (int k = 0; k < APER; k++) {
+            const int64_t h = base + (int64_t)tid * APER + k;
+            if (h >= a.H) break;
+            const int64_t n = loc[k];
+            a.neval_h[h] = (int32_t)n;
+            a.offsets[h] = off;
+            for (int64_t tt = (off + BASE_TILE - 1) / BASE_TILE; tt * BASE_TILE < off + n; tt++)
+                if (tt < a.ntiles_cap) a.tile_h0[tt] = h;
+            off += n;
+        }
+        run += total;
+        __syncthreads();
+    }
+    // block maximum of the counts
+    scan[tid] = mxn;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+        if (tid < o) scan[tid] = scan[tid + o] > scan[tid] ? scan[tid + o] : scan[tid];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const int64_t N = run;
+        int64_t ntiles = (N + BASE_TILE - 1) / BASE_TILE;
+        a.offsets[a.H] = N;
+        st->neval = N;
+        st->neval_sigf = nsf;
+        st->range_lo = a.min_neval_hcube;
+        st->range_hi = a.adaptive_alloc ? (scan[0] > a.min_neval_hcube ? scan[0] : a.min_neval_hcube)
+                                        : a.min_neval_hcube;
+        if (N > a.ncap || ntiles + 1 > a.ntiles_cap) {
+            st->status = VG_ERR_MEMORY;
+            ntiles = 0;
+        } else {
+            st->status = VG_OK;
+            a.tile_h0[ntiles] = a.H;
+        }
+        st->ntiles = ntiles;
+        st->nan_seen = 0;
+        *a.counter = 0ull;
+    }
+    __syncthreads();
+}
+
+// Iteration sums of one integral by one CTA: the tile body's partial sums
+// (parts[0]) plus the Chan et al. merge of every hypercube cut by tile
+// boundaries (the finalize kernels' work); sum_sigf and the constant-integrand
+// reset (pyx:2209-2215).
+static __device__ __noinline__ void cta_finalize(const IterArgs &a, VgKSum *red, int *flag)
+{
+    const int tid = threadIdx.x;
+    vg_stats *st = a.stats;
+    const int64_t N = st->neval;
+    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
+    VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
+    if (tid == 0 && ntiles > 0) {
+        const TilePart p = a.parts[0];
+        cm = p.mean;
+        cv = p.var;
+        cs = p.sigf;
+    }
+    for (int64_t t = tid; t < ntiles; t += NT) {
+        const TileRec r = a.recs[2 * t + 1];
+        if (r.h < 0) continue;
+        double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
+        for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+            const TileRec q = a.recs[2 * t2];
+            if (q.h != r.h) break;
+            const double n2 = n + q.n;
+            const double delta = q.S / q.n - Sx / n;
+            Q = Q + q.Q + delta * delta * (n * q.n / n2);
+            Sx += q.S;
+            D += q.D;
+            n = n2;
+            if (!q.spans) break;
+        }
+        const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
+        cm.add(__dadd_rn(Sx, D));
+        cv.add(vh);
+        if (a.adaptive) {
+            const double sg = vg_pow_fast(fabs(vh), a.beta_half);
+            a.sigf[r.h] = sg;
+            cs.add(sg);
+        }
+    }
+    const VgKSum M = vg_block_ksum<NT>(cm, red);
+    const VgKSum V = vg_block_ksum<NT>(cv, red);
+    const VgKSum Sg = vg_block_ksum<NT>(cs, red);
+    if (tid == 0) {
+        st->mean = M.value();
+        st->var = V.value();
+        st->sigf_reset = 0;
+        *flag = 0;
+        if (a.adaptive) {
+            const double ss = Sg.value();
+            if (ss > 0) {
+                st->sum_sigf = ss;
+            } else {
+                st->sum_sigf = (double)a.H;
+                st->sigf_reset = 1;
+                *flag = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (*flag)
+        for (int64_t h = tid; h < a.H; h += NT) a.sigf[h] = 1.0;
+    __syncthreads();
+}
+
+// End of iteration: adapt the map (one axis after another), copy the new
+// grid back, clear the training histogram (vg_end_iteration's work).
+static __device__ __noinline__ void cta_adapt(const BatchJob &J, const IterArgs &a, unsigned char *smem)
+{
+    const int tid = threadIdx.x;
+    const vgadapt::AdaptArgs &ad = J.ad;
+    double *avg = (double *)smem;
+    double *tmp = avg + ad.max_old;
+    double *part = tmp + ad.max_old;
+    for (int i = tid; i < ad.max_old; i += NT) avg[i] = 1.0;
+    __syncthreads();
+    for (int d = 0; d < ad.dim; d++) vgadapt::adapt_axis<NT>(ad, d, avg, tmp, part);
+    __syncthreads();
+    for (int d = 0; d < ad.dim; d++) {
+        const int K = ad.old_ninc[d];
+        double *g = const_cast<double *>(ad.grid) + d * ad.ldg;
+        double *inc = const_cast<double *>(ad.inc) + d * ad.ldi;
+        for (int i = tid; i <= K; i += NT) g[i] = ad.new_grid[d * ad.ldg_new + i];
+        for (int i = tid; i < K; i += NT) {
+            inc[i] = ad.new_inc[d * ad.ldi_new + i];
+            a.sum_f[d * a.ldi + i] = 0.0;
+            a.n_f[d * a.ldi + i] = 0ull;
+        }
+    }
+    __syncthreads();
+}
+
+// Weighted average of iterations [nwarm, nitn) (RAvg, pyx:2392-2410):
+// mean = sum(m/v)/sum(1/v), sdev = sum(1/v)^-1/2, chi2 = sum((m-mean)^2/v).
+static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nwarm)
+{
+    if (threadIdx.x != 0) return;
+    double sw = 0.0, swm = 0.0;
+    int cnt = 0;
+    for (int i = nwarm; i < nitn; i++) {
+        const double m = J.out[2 * i], v = J.out[2 * i + 1];
+        if (v > 0) {
+            sw += 1.0 / v;
+            swm += m / v;
+        }
+        cnt++;
+    }
+    const double mean = sw > 0 ? swm / sw : 0.0;
+    double chi2 = 0.0;
+    for (int i = nwarm; i < nitn; i++) {
+        const double m = J.out[2 * i], v = J.out[2 * i + 1];
+        if (v > 0) chi2 += (m - mean) * (m - mean) / v;
+    }
+    J.res[0] = mean;
+    J.res[1] = sw > 0 ? 1.0 / sqrt(sw) : 0.0;
+    J.res[2] = chi2;
+    J.res[3] = (double)(cnt > 0 ? cnt - 1 : 0);
+}
+
+// The persistent kernel: S4, S8, S16 are the samples per thread of the
+// dimension buckets and MINB the CTAs per SM it is compiled for (the tile
+// shape and occupancy the autotuner picks).
+template <int KIND, int S4, int S8, int S16, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restrict__ jobs,
+                                                   const VgParams *__restrict__ params,
+                                                   const int *__restrict__ order, int njobs, int nitn,
+                                                   int nwarm, uint32_t itn0, unsigned int *queue)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ IterArgs sa;
+    __shared__ int64_t scan[NT];
+    __shared__ VgKSum red[NT / 32 + 2];
+    __shared__ int s_q, s_flag;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_q = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();
+        if (q >= njobs) break;
+        const int j = order[q];
+        const BatchJob &J = jobs[j];
+        {
+            const int nw = (int)(sizeof(IterArgs) / 4);
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&J.a);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
+            for (int i = tid; i < nw; i += NT) dst[i] = src[i];
+        }
+        __syncthreads();
+        const int dimb = J.dimb;
+        for (int it = 0; it < nitn; it++) {
+            if (tid == 0) sa.itn = itn0 + (uint32_t)it;
+            __syncthreads();
+            cta_alloc(sa, scan);
+            if (sa.stats->ntiles > 0) {
+                if (dimb == 4) tile_body<float, MODE_FUSED, KIND, 4, S4>(sa, params[j], smem, 0, 1, 0);
+                else if (dimb == 8) tile_body<float, MODE_FUSED, KIND, 8, S8>(sa, params[j], smem, 0, 1, 0);
+                else tile_body<float, MODE_FUSED, KIND, 16, S16>(sa, params[j], smem, 0, 1, 0);
+            }
+            __syncthreads();
+            cta_finalize(sa, red, &s_flag);
+            if (tid == 0) {
+                J.out[2 * it] = sa.stats->mean;
+                J.out[2 * it + 1] = sa.stats->var;
+            }
+            if (J.adapt) cta_adapt(J, sa, smem);
+            __syncthreads();
+        }
+        cta_ravg(J, nitn, nwarm);
+        __syncthreads();
+    }
+}
+
+}  // namespace vgbatch

@@ -1195,6 +1195,48 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
     if (warp == 0) umma::tmem_dealloc(tmem, 512);
 }
 
+// ------------------------------------------------------- training batch
+// Draw m of the iteration's n samples (Philox: counter (i, step, 0, 0x7f00),
+// key = seed; index = high 32 bits of word x times n), gather their z and
+// form the raw weights in FP64; the block sums accumulate into scratch[m].
+__global__ void train_gather_kernel(int64_t n, int64_t m, uint64_t seed, uint32_t step, int dim,
+                                    const float *__restrict__ z, const float *__restrict__ f,
+                                    const double *__restrict__ wgt, const int64_t *__restrict__ hc,
+                                    const int32_t *__restrict__ nh, int chi2, float *__restrict__ zs,
+                                    double *__restrict__ wraw)
+{
+    __shared__ double red[32];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double w = 0.0;
+    if (i < m) {
+        const VgU4 r = vg_philox((uint32_t)i, (uint32_t)(i >> 32), step, 0x7f00u, (uint32_t)seed,
+                                 (uint32_t)(seed >> 32));
+        const int64_t idx = (int64_t)(((uint64_t)r.x * (uint64_t)n) >> 32);
+        for (int d = 0; d < dim; d++) zs[i * dim + d] = z[idx * dim + d];
+        const double fw = fabs((double)f[idx]) * wgt[idx];
+        w = chi2 ? fw * fw * (double)nh[hc[idx]] : fw;
+        wraw[i] = w;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) w += __shfl_down_sync(0xffffffffu, w, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (threadIdx.x == 0) atomicAdd(wraw + m, v);
+    }
+}
+
+// Weights normalised to mean 1 (FP32 for the backward).
+__global__ void train_norm_kernel(int64_t m, const double *__restrict__ wraw, float *__restrict__ ws)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const double s = wraw[m];
+    if (i < m) ws[i] = s > 0 ? (float)(wraw[i] * ((double)m / s)) : 1.f;
+}
+
 int geom_of(FlowGeom &g, const vg_flow *fl) { return make_geom(g, fl->dim, fl->nlayers, fl->K, fl->hidden); }
 
 int set_smem(const void *kern, size_t bytes)
@@ -1431,5 +1473,35 @@ extern "C" int vg_flow_status(int *status, int reset)
         VG_CUDA_CHECK(cudaMemcpyToSymbol(g_flow_status, &z, sizeof(int)));
     }
     *status = v;
+    return VG_OK;
+}
+
+extern "C" int vg_flow_train_batch(int64_t n, int64_t m, uint64_t seed, uint32_t step, int dim, const float *z,
+                                   const float *f, const double *wgt, const int64_t *hc, const int32_t *neval_h,
+                                   int chi2, float *zs, float *ws, double *scratch, void *stream)
+{
+    vg_clear_error();
+    if (n < 1 || m < 1 || n >= ((int64_t)1 << 32)) return vg_fail(VG_ERR_VALUE, "training batch sizes");
+    if (dim < 1 || dim > FMAXD) return vg_fail(VG_ERR_UNSUPPORTED, "flow dim %d", dim);
+    if (chi2 && (hc == nullptr || neval_h == nullptr)) return vg_fail(VG_ERR_VALUE, "chi2 weights need hc, neval_h");
+    cudaStream_t st = (cudaStream_t)stream;
+    VG_CUDA_CHECK(cudaMemsetAsync(scratch + m, 0, sizeof(double), st));
+    const unsigned nb = (unsigned)((m + 255) / 256);
+    train_gather_kernel<<<nb, 256, 0, st>>>(n, m, seed, step, dim, z, f, wgt, hc, neval_h, chi2, zs, scratch);
+    VG_LAUNCH_CHECK();
+    train_norm_kernel<<<nb, 256, 0, st>>>(m, scratch, ws);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
+extern "C" int vg_flow_zero_grad(const vg_flow *fl, void *stream)
+{
+    vg_clear_error();
+    FlowGeom g;
+    int rc = geom_of(g, fl);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    VG_CUDA_CHECK(cudaMemsetAsync(fl->grad, 0, sizeof(float) * (size_t)g.nparams, st));
+    VG_CUDA_CHECK(cudaMemsetAsync(fl->loss, 0, sizeof(double), st));
     return VG_OK;
 }

@@ -411,6 +411,19 @@ int finalize_launch(IterArgs &a, cudaStream_t st, int fast)
 int launch_points(IterArgs &a, int f64, cudaStream_t st);
 int launch_reduce(IterArgs &a, int f64, cudaStream_t st);
 int launch_fused(IterArgs &a, int kind, const VgParams &P, int tab_len, int f64, cudaStream_t st);
+
+int fill_iter_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *u)
+{
+    return fill_args(a, it, itn, u);
+}
+
+void scratch_grid(const vg_integrator *it, double **new_grid, double **new_inc)
+{
+    WorkLayout L = layout(it, neval_cap(it));
+    char *w = (char *)it->work;
+    *new_grid = (double *)(w + L.newgrid);
+    *new_inc = (double *)(w + L.newinc);
+}
 }  // namespace vg
 
 // ====================================================================== ABI

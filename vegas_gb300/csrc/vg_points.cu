@@ -4,7 +4,8 @@
 // calls the user's integrand on its batch of points (_vegas.pyx:2126-2129);
 // this is the same call for the built-in synthetic integrands.
 //
-//   f[i] = vol * f(lo + width * z_i) * exp(-logdet[i])     (logdet optional)
+//   f[i] = vol * f(lo + width * z_i) * jac[i] * exp(-logdet[i])
+// (jac and logdet optional)
 //
 // z is FP32 [n, dim] on the unit cube; the evaluation is FP32 as in the fused
 // kernels (vg_integrands.cuh).  HBM-bound for cheap integrands: reads 4*dim
@@ -24,6 +25,7 @@ struct PointsArgs {
     float vol;
     const float *z;
     const float *logdet;
+    const float *jac;
     float *f;
 };
 
@@ -42,6 +44,7 @@ __global__ void __launch_bounds__(256) points_kernel(PointsArgs a, VgParams P)
         for (int d = 0; d < DIMB; d++)
             x[d] = d < dim ? fmaf(a.width[d], a.z[i * dim + d], a.lo[d]) : 0.f;
         float v = a.vol * vg_eval_f32<KIND, DIMB>(k, tab, a.tab_len, dim, x);
+        if (a.jac != nullptr) v *= a.jac[i];
         if (a.logdet != nullptr) v *= __expf(-a.logdet[i]);
         a.f[i] = v;
     }
@@ -62,11 +65,38 @@ int launch_points(const PointsArgs &a, const VgParams &P, cudaStream_t st)
     return VG_OK;
 }
 
+__global__ void weight_kernel(int64_t n, const float *__restrict__ f, const float *__restrict__ jac,
+                              const float *__restrict__ logdet, float *__restrict__ out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float v = f[i];
+        if (jac != nullptr) v *= jac[i];
+        if (logdet != nullptr) v *= __expf(-logdet[i]);
+        out[i] = v;
+    }
+}
+
 }  // namespace
+
+// out[i] = f[i] * jac[i] * exp(-logdet[i]) for integrand values computed
+// elsewhere (a torch integrand on the flow path); jac, logdet optional.
+extern "C" int vg_weight_points(int64_t n, const float *f, const float *jac, const float *logdet, float *out,
+                                void *stream)
+{
+    vg_clear_error();
+    if (n <= 0) return VG_OK;
+    int64_t nb = (n + 255) / 256;
+    const int64_t cap = (int64_t)vg_num_sms() * 16;
+    if (nb > cap) nb = cap;
+    weight_kernel<<<(unsigned)nb, 256, 0, (cudaStream_t)stream>>>(n, f, jac, logdet, out);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
 
 extern "C" int vg_eval_points(int kind, const double *params, int nparams, int dim, int64_t n,
                               const float *z, const double *lo, const double *width,
-                              const float *logdet, float *f, void *stream)
+                              const float *logdet, const float *jac, float *f, void *stream)
 {
     vg_clear_error();
     if (dim < 1 || dim > VG_MAX_DIM) return vg_fail(VG_ERR_VALUE, "dim %d out of range", dim);
@@ -90,6 +120,7 @@ extern "C" int vg_eval_points(int kind, const double *params, int nparams, int d
     a.vol = (float)vol;
     a.z = z;
     a.logdet = logdet;
+    a.jac = jac;
     a.f = f;
     cudaStream_t st = (cudaStream_t)stream;
     switch (kind) {

@@ -276,10 +276,15 @@ __device__ __forceinline__ double vg_div(double a, double b)
 }
 
 // ------------------------------------------------------------------ kernel
+// The work of one CTA: reduction modes take tiles first, first + stride, ...
+// (static, deterministic); evaluation-only modes take tiles from the atomic
+// counter.  The CTA's partial sums go to a.parts[part_slot].  Called by the
+// grid-wide tile_kernel (first = blockIdx.x, stride = gridDim.x) and by the
+// batched kernel, where one CTA runs a whole integral (0, 1, 0).
 template <typename T, int MODE, int KIND, int DIMB, int S>
-__global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
+__device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm, unsigned char *smem,
+                                          int64_t first, int64_t stride, int64_t part_slot)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
     typedef typename GridEntry<T>::type GE;
     constexpr int TT = NT * S;
     constexpr int KSUB = TT / BASE_TILE;   // base tiles per tile
@@ -345,7 +350,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
     int nan_local = 0;
     // per-thread running sums over every hypercube this thread finalises
     double acc_m = 0.0, acc_v = 0.0, acc_s = 0.0;
-    int64_t next_static = blockIdx.x;
+    int64_t next_static = first;
 
     for (;;) {
         __syncthreads();
@@ -354,7 +359,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
             // reduction modes: fixed tile -> CTA assignment, so the per-CTA
             // partial sums (and hence the result) are deterministic
             tile = next_static;
-            next_static += gridDim.x;
+            next_static += stride;
         } else {
             // evaluation-only modes: dynamic tiles for load balance
             if (tid == 0) s_tile = (int64_t)atomicAdd(a.counter, 1ull);
@@ -703,7 +708,7 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
             p.mean = m;
             p.var = v;
             p.sigf = sg;
-            a.parts[blockIdx.x] = p;
+            a.parts[part_slot] = p;
         }
         if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
         if (use_bins && a.hist_smem) {
@@ -720,6 +725,13 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
             }
         }
     }
+}
+
+template <typename T, int MODE, int KIND, int DIMB, int S>
+__global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    tile_body<T, MODE, KIND, DIMB, S>(a, prm, smem, blockIdx.x, gridDim.x, blockIdx.x);
 }
 
 // ---------------------------------------------------------------- launcher
@@ -773,5 +785,8 @@ int launch_dim(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st);
 
 int finalize_launch(IterArgs &a, cudaStream_t st, int fast);
 int launch_reduce(IterArgs &a, int f64, cudaStream_t st);
+// IterArgs of one integral (pointers into its workspace) and its adapt scratch grid
+int fill_iter_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *u);
+void scratch_grid(const vg_integrator *it, double **new_grid, double **new_inc);
 
 }  // namespace vg

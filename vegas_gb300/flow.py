@@ -101,6 +101,17 @@ class Flow(object):
         N.check(L.vg_flow_grad(ctypes.byref(st), n, N.ptr(z), N.ptr(w), N.ptr(self._work),
                                self._work.numel(), N.stream_ptr(self.device)))
 
+    def train_step_normalized(self, z, w, lr=None, clip=10.0):
+        """One Adam step on -sum_i w_i log q(z_i) / m with weights already
+        normalised to mean 1 (vg_flow_train_batch); only library kernels run."""
+        m = z.shape[0]
+        N.check(N.load().vg_flow_zero_grad(ctypes.byref(self._struct()), N.stream_ptr(self.device)))
+        self.accumulate_grad(z, w)
+        self.step_count += 1
+        N.check(N.load().vg_flow_adam(ctypes.byref(self._struct()), 1.0 / m,
+                                      self.lr if lr is None else lr, 0.9, 0.999, 1e-8,
+                                      self.step_count, clip, N.stream_ptr(self.device)))
+
     def train_step(self, z, w, lr=None, clip=10.0):
         """One Adam step on the loss -sum_i w_i log q(z_i) / sum_i w_i.
 

@@ -100,8 +100,9 @@ class FlowIntegrator(object):
         self._nit = 0
         self._flow_nit = 0
         self.history = []            # per iteration: dict(flow, mean, sdev, neval, score, seconds)
-        self._gen = torch.Generator(device=self.device)
-        self._gen.manual_seed(int(self.vegas.seed) & 0x7fffffff)
+        self._tseed = (int(self.vegas.seed) * 0x9E3779B97F4A7C15 + 0x632BE5AB) & ((1 << 64) - 1)
+        self._tstep = 0
+        self._zs = self._ws = self._scr = None
 
     @property
     def plain_score(self):
@@ -126,18 +127,17 @@ class FlowIntegrator(object):
         self.flow_on = True
         self.losing = 0
 
-    def _feff(self, fcn, x, jac, ld):
-        """f(x) * jac * exp(-ld) (FP32 [n]); x in the integration box."""
+    def _feff(self, fcn, x, jac, ld, out):
+        """out[:n] = f(x) * jac * exp(-ld) (FP32); x in the integration box."""
         n = x.shape[0]
-        lw = ld - torch.log(jac)
+        L = N.load()
+        stream = N.stream_ptr(self.device)
         if isinstance(fcn, BuiltinIntegrand):
             p = fcn.params(self.dim)
-            out = torch.empty(n, dtype=torch.float32, device=self.device)
-            N.check(N.load().vg_eval_points(int(fcn.kind), N.dbl_array(p), len(p), self.dim, n,
-                                            N.ptr(x), N.dbl_array([0.0] * self.dim),
-                                            N.dbl_array([1.0] * self.dim), N.ptr(lw), N.ptr(out),
-                                            N.stream_ptr(self.device)))
-            return out
+            N.check(L.vg_eval_points(int(fcn.kind), N.dbl_array(p), len(p), self.dim, n, N.ptr(x),
+                                     N.dbl_array([0.0] * self.dim), N.dbl_array([1.0] * self.dim),
+                                     N.ptr(ld), N.ptr(jac), N.ptr(out), stream))
+            return
         ft = getattr(fcn, 'fcntype', 'scalar')
         if ft == 'rbatch':
             f = fcn(x.t())
@@ -145,8 +145,11 @@ class FlowIntegrator(object):
             f = fcn(x)
         else:
             raise ValueError('the flow path needs a batch integrand (lbatchintegrand / rbatchintegrand)')
-        f = torch.as_tensor(f, device=self.device).reshape(n).to(torch.float32)
-        return f * torch.exp(-lw)
+        f = torch.as_tensor(f, device=self.device).reshape(n)
+        if f.dtype != torch.float32:
+            f = f.to(torch.float32)
+        f = f.contiguous()
+        N.check(L.vg_weight_points(n, N.ptr(f), N.ptr(jac), N.ptr(ld), N.ptr(out), stream))
 
     def _flow_iteration(self, fcn, train):
         s = self.strat
@@ -163,18 +166,24 @@ class FlowIntegrator(object):
         x = torch.empty_like(yp)
         jac = torch.empty(n, dtype=torch.float32, device=self.device)
         self.map.map(yp, x, jac)
-        f = torch.zeros(ncap, dtype=torch.float32, device=self.device)
-        f[:n] = self._feff(fcn, x, jac, ld)
+        f = torch.empty(ncap, dtype=torch.float32, device=self.device)
+        self._feff(fcn, x, jac, ld, f)
         N.check(L.vg_reduce(ctypes.byref(it), itn_word, None, N.ptr(f), N.VG_F32, stream))
         if train and self.train_steps > 0:
-            nh = s._work[:4 * s.nhcube].view(torch.int32)
             m = min(self.train_batch, n)
-            chi2 = self._flow_nit > self.kl_itn
+            if self._zs is None or self._zs.shape[0] != m:
+                self._zs = torch.empty((m, self.dim), dtype=torch.float32, device=self.device)
+                self._ws = torch.empty(m, dtype=torch.float32, device=self.device)
+                self._scr = torch.empty(m + 1, dtype=torch.float64, device=self.device)
+            nh = s._work[:4 * s.nhcube].view(torch.int32)
+            chi2 = 1 if self._flow_nit > self.kl_itn else 0
             for _ in range(self.train_steps):
-                idx = torch.randint(0, n, (m,), device=self.device, generator=self._gen)
-                fw = f[idx].double().abs() * wgt[idx]          # |f_eff| / (H n_h)
-                w = fw * fw * nh[hc[idx]].double() if chi2 else fw
-                self.flow.train_step(yp[idx], w.float())
+                self._tstep += 1
+                N.check(L.vg_flow_train_batch(n, m, self._tseed, self._tstep & 0xffffffff, self.dim,
+                                              N.ptr(yp), N.ptr(f), N.ptr(wgt), N.ptr(hc), N.ptr(nh),
+                                              chi2, N.ptr(self._zs), N.ptr(self._ws), N.ptr(self._scr),
+                                              stream))
+                self.flow.train_step_normalized(self._zs, self._ws)
         N.check(L.vg_end_iteration(ctypes.byref(it), stream))
         st = s._read_stats()
         if st.status != 0:

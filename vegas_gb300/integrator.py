@@ -261,7 +261,7 @@ class Integrator(object):
         it.adapt = int(self.adapt)
         it.adapt_to_errors = int(self.adapt_to_errors)
         it.seed = int(self.seed) & ((1 << 64) - 1)
-        it.stream_id = 0
+        it.stream_id = getattr(self, '_stream_id', 0)   # Philox stream (0; batched integrals use their index)
         it.tile = 0
         L = N.load()
         ncap = L.vg_neval_cap(ctypes.byref(it))
