@@ -299,27 +299,33 @@ int vg_weight_points(int64_t n, const float *f, const float *jac, const float *l
  * integrand per Integrator call): njobs independent integrals -- each
  * described by its own vg_integrator (dimension <= 16, FP32, its own device
  * grid, inc, sigf, training histogram, stats and workspace) and built-in
- * integrand parameters (Lorentzian products: params + j*ldp, nparams[j]
- * values) -- run nitn iterations each in ONE persistent kernel: one CTA per
- * integral at a time, integrals taken from a queue in the order `order`
- * (device int[njobs], e.g. largest first).  Each iteration is the same
- * allocation / fused evaluation + reduction / adapt as vg_fused_iteration;
- * out (device double[njobs][nitn][2]) receives every iteration's mean and
- * variance, res (device double[njobs][4]) the weighted average over the
- * iterations after the first nwarm (mean, sdev, chi2, dof).  stats->sum_sigf
- * of each integral must hold its starting value (nhcube for a fresh one).
- * vg_batch_prepare copies the job table (vg_batch_table_bytes) to the device
- * and returns the launch's dynamic shared memory and grid for the tile
- * variant (0 .. vg_batch_variants()-1); vg_batch_launch neither allocates
- * nor synchronises, so it can be captured in a CUDA graph.
+ * integrand parameters (kind VG_F_LORENTZ or VG_F_LATTICE; params + j*ldp,
+ * nparams[j] values) -- run nitn iterations each in ONE persistent kernel.
+ * Queue mode (group <= 1): one CTA per integral at a time, integrals taken
+ * from a queue in the order `order` (device int[njobs], e.g. largest
+ * first).  Group mode (group = G >= 2, njobs*G <= the co-resident CTAs
+ * vg_batch_prepare reports): a cooperative launch in which G CTAs share
+ * each integral's tiles (sync: device uint[njobs] barrier counters).  Each
+ * iteration is the same allocation / fused evaluation + reduction / adapt
+ * as vg_fused_iteration; out (device double[njobs][nitn][2]) receives every
+ * iteration's mean and variance, res (device double[njobs][4]) the weighted
+ * average over the iterations after the first nwarm (mean, sdev, chi2, dof).
+ * stats->sum_sigf of each integral must hold its starting value (nhcube for
+ * a fresh one).  status (device int) becomes VG_ERR_TIMEOUT if a bounded
+ * group barrier gave up.  vg_batch_prepare copies the job table
+ * (vg_batch_table_bytes) to the device and returns the launch's dynamic
+ * shared memory and co-resident grid for the tile variant (0 ..
+ * vg_batch_variants()-1); vg_batch_launch neither allocates nor
+ * synchronises, so it can be captured in a CUDA graph.
  */
 int vg_batch_variants(void);
 size_t vg_batch_table_bytes(int njobs);
 int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
-                     const int *nparams, int nitn, double *out, double *res, int variant, void *table,
-                     size_t table_bytes, size_t *smem, int *grid, void *stream);
-int vg_batch_launch(const void *table, int njobs, int nitn, int nwarm, uint32_t itn0, const int *order,
-                    unsigned int *queue, size_t smem, int grid, int variant, void *stream);
+                     const int *nparams, int nitn, double *out, double *res, unsigned int *sync, int variant,
+                     void *table, size_t table_bytes, size_t *smem, int *grid, void *stream);
+int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm, uint32_t itn0, const int *order,
+                    unsigned int *queue, unsigned int *sync, int group, int *status, size_t smem, int grid,
+                    int variant, void *stream);
 
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */

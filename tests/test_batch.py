@@ -74,3 +74,36 @@ def test_batch_accuracy_and_graph_replay():
     pulls2 = (res2[:, 0] - exact) / res2[:, 1]
     assert np.max(np.abs(pulls2)) < 5
     assert np.median(res2[:, 1]) <= np.median(res[:, 1]) * 1.5
+
+
+@pytest.mark.gpu
+def test_batch_group_mode_matches_queue_mode():
+    """Cooperative groups of CTAs per integral give the queue mode's first
+    iteration (same samples) and the closed-form answers."""
+    from vegas_gb300.batch import BatchIntegrator
+    rng = np.random.default_rng(21)
+    dims, nevals = [4, 6, 8], [200000, 300000, 100000]
+    fs = [_lorentz(rng, d) for d in dims]
+    A = BatchIntegrator(fs, nevals, nitn=6, nwarm=2, seed=8, variant=0, group=1)
+    B = BatchIntegrator(fs, nevals, nitn=6, nwarm=2, seed=8, variant=0, group=2)
+    ra, rb = A.run(), B.run()
+    oa, ob = A.iterations(), B.iterations()
+    assert np.allclose(oa[:, 0, 0], ob[:, 0, 0], rtol=1e-6, atol=0)
+    exact = np.array([f.exact(d) for f, d in zip(fs, dims)])
+    for r in (ra, rb):
+        assert np.max(np.abs((r[:, 0] - exact) / r[:, 1])) < 5
+
+
+@pytest.mark.gpu
+def test_batch_lattice_scan_against_transfer_matrix():
+    """A small lambda scan of the periodic lattice action (dim 4 on
+    [-5, 5]^4) in group mode, against the FP64 transfer-matrix value."""
+    from vegas_gb300.batch import BatchIntegrator
+    lams = np.exp(np.linspace(np.log(0.01), np.log(1.0), 8))
+    fs = [vg.LatticeAction(0.5, float(l)) for l in lams]
+    B = BatchIntegrator(fs, [200000] * len(fs), nitn=12, nwarm=6, seed=3, dims=[4] * len(fs),
+                        limits=(-5.0, 5.0))
+    res = B.run()
+    exact = np.array([f.exact(4) for f in fs])
+    pulls = (res[:, 0] - exact) / res[:, 1]
+    assert np.max(np.abs(pulls)) < 5, pulls

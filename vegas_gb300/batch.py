@@ -18,10 +18,11 @@ import torch
 
 from . import _native as N
 from .adaptive_map import _device
-from .integrands import LorentzianProduct
+from .integrands import LatticeAction, LorentzianProduct
 from .integrator import strata
 
 _LDP = 32   # parameters per integral in the packed table (Lorentzian: 2*dim <= 32)
+_KINDS = {LorentzianProduct: N.VG_F_LORENTZ, LatticeAction: N.VG_F_LATTICE}
 
 
 def _align(n, a=256):
@@ -29,11 +30,16 @@ def _align(n, a=256):
 
 
 class BatchIntegrator(object):
-    """vegas+ on many integrals of Lorentzian products over unit cubes.
+    """vegas+ on many integrals of one built-in integrand family.
 
     Args:
-        integrands: list of ``LorentzianProduct`` (dimension <= 16 each).
+        integrands: list of ``LorentzianProduct`` (over the unit cube) or of
+            ``LatticeAction`` (over ``limits``), dimension <= 16 each.
         nevals: evaluations per iteration of each integral.
+        dims: dimension of each integral (needed for ``LatticeAction``).
+        limits: (lo, hi) of every axis (default (0, 1)).
+        group: CTAs per integral (None: as many as fit when every integral
+            gets at least two, else 1 = one CTA per integral from a queue).
         nitn, nwarm: iterations per launch and warm-up iterations excluded
             from the weighted average (the reference's ``nitn`` of an adapt
             call followed by a final call).
@@ -42,21 +48,27 @@ class BatchIntegrator(object):
     """
 
     def __init__(self, integrands, nevals, nitn=16, nwarm=8, alpha=0.5, beta=0.75, seed=1,
-                 variant=None, device=None, neval_frac=0.75, max_neval_hcube=50000):
+                 variant=None, device=None, neval_frac=0.75, max_neval_hcube=50000, dims=None,
+                 limits=(0.0, 1.0), group=None):
         self.device = _device(device)
         self.integrands = list(integrands)
         self.njobs = len(self.integrands)
         if self.njobs < 1:
             raise ValueError('no integrands')
-        for f in self.integrands:
-            if not isinstance(f, LorentzianProduct):
-                raise NotImplementedError('batched launch: LorentzianProduct integrands only')
+        kinds = {_KINDS.get(type(f)) for f in self.integrands}
+        if None in kinds or len(kinds) != 1:
+            raise NotImplementedError('batched launch: one family of LorentzianProduct or LatticeAction')
+        self.kind = kinds.pop()
+        self.limits = (float(limits[0]), float(limits[1]))
+        self.group_req = group
         self.nitn, self.nwarm = int(nitn), int(nwarm)
         if not 0 <= self.nwarm < self.nitn:
             raise ValueError('need 0 <= nwarm < nitn')
         self.alpha, self.beta, self.seed = float(alpha), float(beta), int(seed)
         self.neval_frac, self.max_neval_hcube = float(neval_frac), int(max_neval_hcube)
-        self.dims = np.array([len(f.c) for f in self.integrands], np.int64)
+        if dims is None:
+            dims = [len(f.c) for f in self.integrands]
+        self.dims = np.array(dims, np.int64)
         if self.dims.max() > 16:
             raise NotImplementedError('batched launch: dimension <= 16')
         self._layout(np.asarray(nevals, np.int64))
@@ -130,7 +142,7 @@ class BatchIntegrator(object):
             inc = np.zeros((d, K))
             for k in range(d):
                 nk = int(self.ninc[j][k])
-                g[k, :nk + 1] = np.linspace(0.0, 1.0, nk + 1)
+                g[k, :nk + 1] = np.linspace(self.limits[0], self.limits[1], nk + 1)
                 inc[k, :nk] = np.diff(g[k, :nk + 1])
             arena[og:og + g.nbytes].copy_(torch.from_numpy(g.view(np.uint8).reshape(-1)))
             arena[oi:oi + inc.nbytes].copy_(torch.from_numpy(inc.view(np.uint8).reshape(-1)))
@@ -154,29 +166,38 @@ class BatchIntegrator(object):
         cost = np.array([self.neval[j] * (1 + self.dims[j]) for j in range(nj)])
         self.order = torch.tensor(np.argsort(-cost, kind='stable').astype(np.int32), device=self.device)
         self.queue = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.sync = torch.zeros(nj, dtype=torch.int32, device=self.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
 
     # ----------------------------------------------------------- launching
     def set_variant(self, variant):
         L = N.load()
         smem = ctypes.c_size_t(0)
         grid = ctypes.c_int(0)
-        N.check(L.vg_batch_prepare(ctypes.cast(self.its, ctypes.c_void_p), self.njobs, N.VG_F_LORENTZ,
+        N.check(L.vg_batch_prepare(ctypes.cast(self.its, ctypes.c_void_p), self.njobs, self.kind,
                                    self.params.ctypes.data_as(ctypes.c_void_p), _LDP,
                                    self.nparams.ctypes.data_as(ctypes.c_void_p), self.nitn,
-                                   N.ptr(self.out), N.ptr(self.res), int(variant), N.ptr(self.table),
+                                   N.ptr(self.out), N.ptr(self.res), N.ptr(self.sync), int(variant),
+                                   N.ptr(self.table),
                                    self.table.numel(), ctypes.byref(smem), ctypes.byref(grid),
                                    N.stream_ptr(self.device)))
         self.variant = int(variant)
         self.smem = smem.value
         self.grid = grid.value
+        if self.group_req is None:
+            g = self.grid // self.njobs
+            self.group = g if g >= 2 else 1
+        else:
+            self.group = int(self.group_req)
         self._graph = None
 
     def launch(self):
         """One persistent kernel: nitn iterations of every integral (asynchronous)."""
         L = N.load()
-        N.check(L.vg_batch_launch(N.ptr(self.table), self.njobs, self.nitn, self.nwarm,
+        N.check(L.vg_batch_launch(N.ptr(self.table), self.njobs, self.kind, self.nitn, self.nwarm,
                                   (self._itn + 1) & 0xffffffff, N.ptr(self.order), N.ptr(self.queue),
-                                  self.smem, self.grid, self.variant, N.stream_ptr(self.device)))
+                                  N.ptr(self.sync), self.group, N.ptr(self.status), self.smem,
+                                  self.grid, self.variant, N.stream_ptr(self.device)))
         self._itn += self.nitn
 
     def capture(self):
@@ -206,6 +227,9 @@ class BatchIntegrator(object):
     def results(self):
         """Per integral: mean, sdev, chi2, dof of the weighted average over the
         iterations after the warm-up ones (numpy [njobs, 4])."""
+        if int(self.status.item()) != 0:
+            raise N.VegasError('batched launch: a group barrier timed out (status %d)'
+                               % int(self.status.item()))
         return self.res.cpu().numpy()
 
     def iterations(self):
@@ -228,10 +252,16 @@ class BatchIntegrator(object):
         best, best_t = 0, float('inf')
         self.tuning = {}
         for v in range(nv):
-            probe = BatchIntegrator([self.integrands[i] for i in idx], [self.neval[i] for i in idx],
-                                    nitn=2, nwarm=1, alpha=self.alpha, beta=self.beta,
-                                    seed=self.seed, variant=v, device=self.device,
-                                    neval_frac=self.neval_frac, max_neval_hcube=self.max_neval_hcube)
+            try:
+                probe = BatchIntegrator([self.integrands[i] for i in idx], [self.neval[i] for i in idx],
+                                        nitn=2, nwarm=1, alpha=self.alpha, beta=self.beta,
+                                        seed=self.seed, variant=v, device=self.device,
+                                        neval_frac=self.neval_frac,
+                                        max_neval_hcube=self.max_neval_hcube,
+                                        dims=[int(self.dims[i]) for i in idx], limits=self.limits,
+                                        group=self.group_req)
+            except (ValueError, MemoryError, NotImplementedError, N.VegasError):
+                continue   # variant unavailable for this family / size
             probe.launch()
             torch.cuda.synchronize(self.device)
             t0 = time.perf_counter()

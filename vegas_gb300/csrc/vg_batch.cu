@@ -16,15 +16,15 @@
 int vg_build_params(int kind, int dim, const double *params, int nparams, VgParams *Pp, int *tab_len_out);
 
 namespace vgbatch {
-int launch_k442(const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, cudaStream_t);
-int launch_k221(const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, cudaStream_t);
-int launch_k222(const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, cudaStream_t);
-int occupancy_k442(size_t, int *);
-int occupancy_k221(size_t, int *);
-int occupancy_k222(size_t, int *);
+int launch_k442(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
+                int, int, int *, cudaStream_t);
+int launch_k221(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
+                int, int, int *, cudaStream_t);
+int launch_k222(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
+                int, int, int *, cudaStream_t);
+int occupancy_k442(int, size_t, int *);
+int occupancy_k221(int, size_t, int *);
+int occupancy_k222(int, size_t, int *);
 }  // namespace vgbatch
 
 namespace {
@@ -59,12 +59,14 @@ extern "C" size_t vg_batch_table_bytes(int njobs)
 }
 
 extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
-                                const int *nparams, int nitn, double *out, double *res, int variant, void *table,
-                                size_t table_bytes, size_t *smem_out, int *grid_out, void *stream)
+                                const int *nparams, int nitn, double *out, double *res, unsigned int *sync,
+                                int variant, void *table, size_t table_bytes, size_t *smem_out, int *grid_out,
+                                void *stream)
 {
     vg_clear_error();
     if (njobs < 1) return vg_fail(VG_ERR_VALUE, "no integrals");
-    if (kind != VG_F_LORENTZ) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: Lorentzian products only");
+    if (kind != VG_F_LORENTZ && kind != VG_F_LATTICE)
+        return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: Lorentzian products and the lattice action only");
     if (variant < 0 || variant >= NVARIANTS) return vg_fail(VG_ERR_VALUE, "variant %d", variant);
     if (nitn < 1) return vg_fail(VG_ERR_VALUE, "nitn < 1");
     if (table_bytes < vg_batch_table_bytes(njobs)) return vg_fail(VG_ERR_VALUE, "job table too small");
@@ -135,6 +137,7 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
         }
         J.out = out + (size_t)j * 2 * nitn;
         J.res = res + (size_t)j * 4;
+        J.sync = sync != nullptr ? sync + j : nullptr;
         smem_max = need > smem_max ? need : smem_max;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -145,9 +148,9 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
     VG_CUDA_CHECK(cudaStreamSynchronize(st));   // the host staging buffers go out of scope
     int per_sm = 0, rc = 0;
     switch (kernel_of(variant)) {
-    case 0: rc = occupancy_k442(smem_max, &per_sm); break;
-    case 1: rc = occupancy_k221(smem_max, &per_sm); break;
-    default: rc = occupancy_k222(smem_max, &per_sm); break;
+    case 0: rc = occupancy_k442(kind, smem_max, &per_sm); break;
+    case 1: rc = occupancy_k221(kind, smem_max, &per_sm); break;
+    default: rc = occupancy_k222(kind, smem_max, &per_sm); break;
     }
     if (rc) return rc;
     if (per_sm < 1) return vg_fail(VG_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
@@ -156,8 +159,9 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
     return VG_OK;
 }
 
-extern "C" int vg_batch_launch(const void *table, int njobs, int nitn, int nwarm, uint32_t itn0, const int *order,
-                               unsigned int *queue, size_t smem, int grid, int variant, void *stream)
+extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm, uint32_t itn0,
+                               const int *order, unsigned int *queue, unsigned int *sync, int group, int *status,
+                               size_t smem, int grid, int variant, void *stream)
 {
     vg_clear_error();
     if (variant < 0 || variant >= NVARIANTS) return vg_fail(VG_ERR_VALUE, "variant %d", variant);
@@ -165,11 +169,20 @@ extern "C" int vg_batch_launch(const void *table, int njobs, int nitn, int nwarm
     cudaStream_t st = (cudaStream_t)stream;
     const BatchJob *jobs = (const BatchJob *)table;
     const VgParams *prm = (const VgParams *)((const char *)table + table_jobs_bytes(njobs));
-    int g = grid < njobs ? grid : njobs;
+    int g;
+    if (group > 1) {   // njobs groups of `group` co-resident CTAs
+        if ((int64_t)njobs * group > grid)
+            return vg_fail(VG_ERR_VALUE, "group launch needs njobs*group <= %d co-resident CTAs", grid);
+        if (sync == nullptr) return vg_fail(VG_ERR_VALUE, "group launch needs the sync counters");
+        g = njobs * group;
+        VG_CUDA_CHECK(cudaMemsetAsync(sync, 0, sizeof(unsigned int) * (size_t)njobs, st));
+    } else {
+        g = grid < njobs ? grid : njobs;
+    }
     VG_CUDA_CHECK(cudaMemsetAsync(queue, 0, sizeof(unsigned int), st));
     switch (kernel_of(variant)) {
-    case 0: return launch_k442(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, st);
-    case 1: return launch_k221(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, st);
-    default: return launch_k222(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, st);
+    case 0: return launch_k442(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
+    case 1: return launch_k221(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
+    default: return launch_k222(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
     }
 }

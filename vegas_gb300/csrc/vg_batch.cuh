@@ -23,9 +23,38 @@ struct BatchJob {
     vgadapt::AdaptArgs ad;       // adapt: grid -> scratch grid of the workspace
     double *out;                 // [nitn][2] iteration mean, variance
     double *res;                 // [4] weighted mean, sdev, chi2, dof
+    unsigned int *sync;          // group barrier counter (group mode)
     int dimb;                    // dimension bucket: 4, 8 or 16
     int adapt;                   // adapt the map after each iteration
 };
+
+// Barrier of the G CTAs working on one integral (group mode; the launch is
+// cooperative, so they are co-resident).  Thread 0 releases this CTA's
+// writes, arrives, and waits (bounded) until all G arrived `round` times.
+// Returns false when the wait gave up.
+__device__ __forceinline__ bool group_barrier(unsigned int *ctr, unsigned int target)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        int ok = 0;
+        for (uint32_t i = 0; i < (1u << 26); i++) {
+            unsigned int v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+            if (v >= target) {
+                ok = 1;
+                break;
+            }
+            __nanosleep(256);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
 
 constexpr int APER = 4;          // hypercubes per thread and pass of the allocation
 
@@ -119,15 +148,15 @@ static __device__ __noinline__ void cta_alloc(const IterArgs &a, int64_t *scan)
 // (parts[0]) plus the Chan et al. merge of every hypercube cut by tile
 // boundaries (the finalize kernels' work); sum_sigf and the constant-integrand
 // reset (pyx:2209-2215).
-static __device__ __noinline__ void cta_finalize(const IterArgs &a, VgKSum *red, int *flag)
+static __device__ __noinline__ void cta_finalize(const IterArgs &a, int ngroup, VgKSum *red, int *flag)
 {
     const int tid = threadIdx.x;
     vg_stats *st = a.stats;
     const int64_t N = st->neval;
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
-    if (tid == 0 && ntiles > 0) {
-        const TilePart p = a.parts[0];
+    if (tid < ngroup && ntiles > 0) {   // the partial sums of each CTA of the group
+        const TilePart p = a.parts[tid];
         cm = p.mean;
         cv = p.var;
         cs = p.sigf;
@@ -238,11 +267,18 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
 // The persistent kernel: S4, S8, S16 are the samples per thread of the
 // dimension buckets and MINB the CTAs per SM it is compiled for (the tile
 // shape and occupancy the autotuner picks).
+//
+// Queue mode (group <= 1): each CTA takes whole integrals from the queue.
+// Group mode (group = G >= 2, cooperative launch): CTA c works on integral
+// order[c / G] as rank c % G; rank 0 allocates, finalizes and adapts, all G
+// ranks share the tiles (rank r takes tiles r, r + G, ...), with two group
+// barriers per iteration.
 template <int KIND, int S4, int S8, int S16, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restrict__ jobs,
                                                    const VgParams *__restrict__ params,
                                                    const int *__restrict__ order, int njobs, int nitn,
-                                                   int nwarm, uint32_t itn0, unsigned int *queue)
+                                                   int nwarm, uint32_t itn0, unsigned int *queue,
+                                                   int group, int *status)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ IterArgs sa;
@@ -250,11 +286,21 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
     __shared__ VgKSum red[NT / 32 + 2];
     __shared__ int s_q, s_flag;
     const int tid = threadIdx.x;
+    const int G = group > 1 ? group : 1;
+    const int rank = G > 1 ? (int)(blockIdx.x % G) : 0;
+    bool first = true;
     for (;;) {
-        if (tid == 0) s_q = (int)atomicAdd(queue, 1u);
-        __syncthreads();
-        const int q = s_q;
-        __syncthreads();
+        int q;
+        if (G > 1) {
+            if (!first) break;
+            q = (int)(blockIdx.x / G);
+        } else {
+            if (tid == 0) s_q = (int)atomicAdd(queue, 1u);
+            __syncthreads();
+            q = s_q;
+            __syncthreads();
+        }
+        first = false;
         if (q >= njobs) break;
         const int j = order[q];
         const BatchJob &J = jobs[j];
@@ -266,25 +312,35 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
         }
         __syncthreads();
         const int dimb = J.dimb;
-        for (int it = 0; it < nitn; it++) {
+        unsigned int rounds = 0;
+        bool ok = true;
+        for (int it = 0; it < nitn && ok; it++) {
             if (tid == 0) sa.itn = itn0 + (uint32_t)it;
             __syncthreads();
-            cta_alloc(sa, scan);
+            if (rank == 0) cta_alloc(sa, scan);
+            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
             if (sa.stats->ntiles > 0) {
-                if (dimb == 4) tile_body<float, MODE_FUSED, KIND, 4, S4>(sa, params[j], smem, 0, 1, 0);
-                else if (dimb == 8) tile_body<float, MODE_FUSED, KIND, 8, S8>(sa, params[j], smem, 0, 1, 0);
-                else tile_body<float, MODE_FUSED, KIND, 16, S16>(sa, params[j], smem, 0, 1, 0);
+                if (dimb == 4) tile_body<float, MODE_FUSED, KIND, 4, S4>(sa, params[j], smem, rank, G, rank);
+                else if (dimb == 8) tile_body<float, MODE_FUSED, KIND, 8, S8>(sa, params[j], smem, rank, G, rank);
+                else tile_body<float, MODE_FUSED, KIND, 16, S16>(sa, params[j], smem, rank, G, rank);
             }
             __syncthreads();
-            cta_finalize(sa, red, &s_flag);
-            if (tid == 0) {
-                J.out[2 * it] = sa.stats->mean;
-                J.out[2 * it + 1] = sa.stats->var;
+            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
+            if (rank == 0) {
+                cta_finalize(sa, G, red, &s_flag);
+                if (tid == 0) {
+                    J.out[2 * it] = sa.stats->mean;
+                    J.out[2 * it + 1] = sa.stats->var;
+                }
+                if (J.adapt) cta_adapt(J, sa, smem);
             }
-            if (J.adapt) cta_adapt(J, sa, smem);
             __syncthreads();
         }
-        cta_ravg(J, nitn, nwarm);
+        if (!ok) {
+            if (tid == 0) atomicExch(status, VG_ERR_TIMEOUT);
+            break;
+        }
+        if (rank == 0) cta_ravg(J, nitn, nwarm);
         __syncthreads();
     }
 }

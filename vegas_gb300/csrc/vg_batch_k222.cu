@@ -1,22 +1,48 @@
 // vg_batch_k222.cu -- batched-kernel instantiation: 2 / 2 / 2 samples per
-// thread in the dimension buckets 4 / 8 / 16 (Lorentzian products), compiled for two CTAs per SM.
+// thread in the dimension buckets 4 / 8 / 16 (Lorentzian products and the lattice action), compiled for two CTAs per SM.
 #include "vg_batch.cuh"
 
 namespace vgbatch {
-int launch_k222(const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn, int nwarm,
-                uint32_t itn0, unsigned int *queue, size_t smem, int grid, cudaStream_t st)
+template <int KIND>
+static int launch_kind(const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn, int nwarm,
+                       uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group, int *status,
+                       cudaStream_t st)
 {
-    auto k = batch_kernel<VG_F_LORENTZ, 2, 2, 2, 2>;
-    k<<<grid, NT, smem, st>>>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue);
+    auto k = batch_kernel<KIND, 2, 2, 2, 2>;
+    if (group > 1) {   // co-resident groups: cooperative launch
+        void *args[] = {(void *)&jobs, (void *)&prm, (void *)&order, (void *)&njobs, (void *)&nitn, (void *)&nwarm,
+                        (void *)&itn0, (void *)&queue, (void *)&group, (void *)&status};
+        VG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)k, dim3((unsigned)grid), dim3(NT), args, smem, st));
+        return VG_OK;
+    }
+    k<<<grid, NT, smem, st>>>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, group, status);
     VG_LAUNCH_CHECK();
     return VG_OK;
 }
-// sets the kernel's shared-memory attribute (outside any stream capture)
-int occupancy_k222(size_t smem, int *per_sm)
+
+template <int KIND>
+static int occupancy_kind(size_t smem, int *per_sm)
 {
-    VG_CUDA_CHECK(cudaFuncSetAttribute(batch_kernel<VG_F_LORENTZ, 2, 2, 2, 2>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, batch_kernel<VG_F_LORENTZ, 2, 2, 2, 2>, NT, smem));
+    auto k = batch_kernel<KIND, 2, 2, 2, 2>;
+    VG_CUDA_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, NT, smem));
     return VG_OK;
+}
+
+int launch_k222(int kind, const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn, int nwarm,
+                uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group, int *status, cudaStream_t st)
+{
+    if (kind == VG_F_LATTICE)
+        return launch_kind<VG_F_LATTICE>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group,
+                                         status, st);
+    return launch_kind<VG_F_LORENTZ>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status,
+                                     st);
+}
+
+// sets the kernel's shared-memory attribute (outside any stream capture)
+int occupancy_k222(int kind, size_t smem, int *per_sm)
+{
+    if (kind == VG_F_LATTICE) return occupancy_kind<VG_F_LATTICE>(smem, per_sm);
+    return occupancy_kind<VG_F_LORENTZ>(smem, per_sm);
 }
 }  // namespace vgbatch

@@ -200,6 +200,21 @@ class LatticeAction(BuiltinIntegrand):
         S = ((xn - x) ** 2 / (2 * self.a) + self.a * (x ** 2 / 2 + self.lam * x ** 4)).sum(dim=1)
         return torch.exp(-S)
 
+    def exact(self, dim, lo=-5.0, hi=5.0, nodes=400):
+        """Integral over [lo, hi]^dim in FP64 by the transfer matrix: the
+        periodic chain integrates to Tr(T^dim) with T(x, y) =
+        exp(-(x-y)^2/(2a) - a (V(x) + V(y))/2), V = x^2/2 + lam x^4, here
+        discretised by Gauss-Legendre quadrature (nodes points) and summed
+        over the eigenvalues of the symmetric quadrature matrix."""
+        t, wq = np.polynomial.legendre.leggauss(int(nodes))
+        x = 0.5 * (hi - lo) * t + 0.5 * (hi + lo)
+        wq = 0.5 * (hi - lo) * wq
+        V = x ** 2 / 2 + self.lam * x ** 4
+        T = np.exp(-(x[:, None] - x[None, :]) ** 2 / (2 * self.a) - self.a * (V[:, None] + V[None, :]) / 2)
+        sw = np.sqrt(wq)
+        ev = np.linalg.eigvalsh(sw[:, None] * T * sw[None, :])
+        return float(np.sum(ev ** int(dim)))
+
 
 class Constant(BuiltinIntegrand):
     kind = N.VG_F_CONST
