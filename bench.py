@@ -186,6 +186,47 @@ def batched_line(dev, reps=2):
     }
 
 
+def lattice_line(dev, reps=2):
+    """64 couplings lambda log-spaced in [0.01, 1] of the dim-16 periodic
+    lattice action on [-5, 5]^16 (a = 0.5), 1e7 evaluations per lambda and
+    iteration, nitn 8+8, in one launch (cooperative groups of CTAs per
+    lambda); errors against the FP64 transfer-matrix value."""
+    import numpy as np
+    import torch
+    import vegas_gb300 as vg
+    from vegas_gb300.batch import BatchIntegrator
+    lams = np.exp(np.linspace(np.log(0.01), np.log(1.0), 64))
+    fs = [vg.LatticeAction(0.5, float(l)) for l in lams]
+    t0 = time.perf_counter()
+    B = BatchIntegrator(fs, [10 ** 7] * 64, nitn=16, nwarm=8, seed=7, dims=[16] * 64,
+                        limits=(-5.0, 5.0), device=dev)
+    t_setup = time.perf_counter() - t0
+    B.run()                               # warm-up launch (adapts the maps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        B.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3 / reps
+    res = B.results()
+    exact = np.array([f.exact(16) for f in fs])
+    pulls = (res[:, 0] - exact) / res[:, 1]
+    return {
+        'workload': 'dim-16 periodic lattice action exp(-sum[(x_{i+1}-x_i)^2/(2a) + a(x_i^2/2 + '
+                    'lambda x_i^4)]), a=0.5, x in [-5,5]^16, 64 lambda log-spaced in [0.01,1], '
+                    '1e7 evals/itn per lambda, nitn 8+8, one cooperative launch, FP32 eval, FP64 RAvg',
+        'evals_per_launch': B.evaluations(), 'seconds_per_launch': secs,
+        'value': B.evaluations() / secs, 'unit': 'evals/s', 'variant': B.variant,
+        'ctas_per_lambda': B.group, 'setup_seconds': t_setup,
+        'pull_rms': float(np.sqrt(np.mean(pulls ** 2))), 'pull_max_abs': float(np.max(np.abs(pulls))),
+        'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
+        'oracle': 'transfer matrix, 400-node Gauss-Legendre, FP64 (LatticeAction.exact)',
+        'fp32_vs_fp64_oracle_max_rel_dev': float(np.max(np.abs(res[:, 0] / exact - 1))),
+    }
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -301,9 +342,10 @@ def gpu_arm(args):
             'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
         if rank == 0:
             tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
-    batched = None
+    batched = lattice = None
     if not args.no_batch and rank == 0:
         batched = batched_line(dev)
+        lattice = lattice_line(dev)
     if world > 1:
         dist.destroy_process_group()
     if rank != 0:
@@ -327,6 +369,7 @@ def gpu_arm(args):
         'clocks': clk,
         'time_to_1e-4': tta,
         'batched': batched,
+        'lattice_scan': lattice,
     }
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)
