@@ -227,6 +227,24 @@ def lattice_line(dev, reps=2):
     }
 
 
+def max_over_ranks(value, world, device=None):
+    """Largest value over the ranks of the job (the timing rule of the
+    benchmark: a step lasts as long as its slowest replica)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(base, rank):
+    """Seed of a replica: replicas are independent vegas+ runs (own Philox
+    key, stream = rank); nothing is exchanged on the data path."""
+    return (int(base) + 7919 * int(rank)) & ((1 << 63) - 1)
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -254,7 +272,7 @@ def gpu_arm(args):
     f = vg.Ridge(M=RIDGE_M, s=RIDGE_S)
     exact = f.exact(DIM)
     # -------- device loop (inputs resident; value, roofline)
-    integ = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=1234 + 7919 * rank, device=dev)
+    integ = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=replica_seed(1234, rank), device=dev)
     it, ncap = integ._struct()
     it.stream_id = rank
     stream = N.stream_ptr(dev)
@@ -299,11 +317,7 @@ def gpu_arm(args):
     kern_ms = [evs[k][1].elapsed_time(evs[k][2]) for k in range(args.steps)]
     st = integ._read_stats()
     neval_step = int(st.neval)
-    t_total = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
+    t_total = max_over_ranks(sum(step_ms) / 1e3, world, dev)
     value = world * neval_step * args.steps / t_total
     # -------- roofline of the fused kernel: SFU-bound (one ex2 per Gaussian term)
     kern_s = statistics.median(kern_ms) / 1e3
@@ -311,7 +325,7 @@ def gpu_arm(args):
     achieved = ex2_per_launch / kern_s / 1e9
     peak = measure_ex2_peak(L, dev)
     # -------- e2e through the public API
-    integ2 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=99 + rank, device=dev)
+    integ2 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=replica_seed(99, rank), device=dev)
     for _ in range(args.warmup):
         integ2(f, nitn=1)
     barrier()
@@ -321,16 +335,12 @@ def gpu_arm(args):
         r = integ2(f, nitn=1)
         ne2 += integ2.last_neval
     barrier()
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
     e2e = world * ne2 / t_e2e
     # -------- time to 1e-4 relative error (plain vegas+, public API, fresh map)
     tta = None
     if not args.no_tta:
-        integ3 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=4242 + rank, device=dev)
+        integ3 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=replica_seed(4242, rank), device=dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         r3 = integ3(f, nitn=5000, rtol=1e-4)

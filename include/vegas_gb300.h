@@ -215,6 +215,20 @@ int vg_end_iteration(const vg_integrator *it, void *stream);
 int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const double *u, int kind,
                          const double *params, int nparams, void *stream);
 
+/*
+ * Array-valued integrands (reference Integrator.__call__ with fcn_size s > 1,
+ * _vegas.pyx:2136-2197): after vg_reduce has run on component 0 (sigf and
+ * the training histogram use it only), the iteration's mean[s] and
+ * (co)variance var[s*s] of all components: f[n, s] (FP32 or FP64, row-major),
+ * wgt[n] the sampler's weights (vg_sample).  correlate != 0: full covariance
+ * with the reference's EPSILON rule (s <= 6); else the diagonal (s <= 16).
+ * work: vg_reduce_array_work_bytes(s, correlate) device bytes.
+ */
+int vg_reduce_array(const vg_integrator *it, const void *f, int f_dtype, int s, int correlate,
+                    const double *wgt, double *mean, double *var, void *work, size_t work_bytes,
+                    void *stream);
+size_t vg_reduce_array_work_bytes(int s, int correlate);
+
 /* ------------------------------------------------------ learned proposal */
 /*
  * Coupling-layer normalising flow with piecewise-quadratic transforms on the

@@ -1,0 +1,91 @@
+"""Array-valued integrands (reference fcn_size s > 1, _vegas.pyx:2136-2197).
+
+GPU: the per-hypercube (co)variance kernel against a numpy restatement of
+the reference loops on the same samples, FP64 (1e-12 relative); an
+Integrator run returning an RAvgArray of the integrand's shape whose
+components agree with their exact values (5 sigma), correlated and not."""
+import numpy as np
+import pytest
+import torch
+
+import vegas_gb300 as vg
+from vegas_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+EPSILON = 2.220446049250313e-16 * 1e4   # _vegas.pyx:36
+
+
+def _ref_array_reduce(wgt, fx, hc, correlate):
+    """pyx:2140-2193 restated in numpy (per hypercube, sample order)."""
+    s = fx.shape[1]
+    mean = np.zeros(s)
+    var = np.zeros((s, s))
+    for h in np.unique(hc):
+        idx = np.nonzero(hc == h)[0]
+        n = len(idx)
+        wf = wgt[idx, None] * fx[idx]
+        sum_wf = wf.sum(axis=0)
+        m = sum_wf / n
+        sum_dwf = np.zeros(s)
+        sum_dwf2 = np.zeros((s, s))
+        for j in range(n):
+            dwf = wf[j] - m
+            for c in range(s):
+                if abs(dwf[c]) < EPSILON * abs(m[c]):
+                    sum_dwf2[c, c] += (EPSILON * abs(m[c])) ** 2
+                    dwf[c] = 0.0
+                else:
+                    sum_dwf2[c, c] += dwf[c] ** 2
+                sum_dwf[c] += dwf[c]
+                if correlate:
+                    for t in range(c):
+                        sum_dwf2[c, t] += dwf[c] * dwf[t]
+        mean += sum_wf + sum_dwf
+        for c in range(s):
+            for t in range(c + 1 if correlate else 1):
+                tt = t if correlate else c
+                var[c, tt] += (n * sum_dwf2[c, tt] - sum_dwf[c] * sum_dwf[tt]) / (n - 1.)
+    if correlate:
+        var = np.tril(var) + np.tril(var, -1).T
+    return mean, var
+
+
+@vg.lbatchintegrand
+def _f3(x):
+    g = torch.exp(-20.0 * ((x - 0.45) ** 2).sum(dim=1))
+    return torch.stack([g, x[:, 0] * g, x[:, 1] * x[:, 2] * g], dim=1)
+
+
+@pytest.mark.parametrize('correlate', [True, False])
+def test_array_reduction_matches_reference_loops(correlate):
+    I = vg.Integrator(3 * [[0, 1]], neval=3000, precision='fp64', seed=5,
+                      correlate_integrals=correlate)
+    it, ncap = I._struct()
+    I._allocate(it)
+    n = int(I._read_stats().neval)
+    x, _, w, hc = I._points(it, ncap, 1, None, want_hc=True)
+    f = _f3(x[:n])
+    fbuf = torch.zeros((ncap, 3), dtype=torch.float64, device=x.device)
+    fbuf[:n] = f
+    mean, var = I._reduce_array(it, fbuf, N.VG_F64, w)
+    rm, rv = _ref_array_reduce(w[:n].cpu().numpy(), f.cpu().numpy(), hc[:n].cpu().numpy(), correlate)
+    np.testing.assert_allclose(mean, rm, rtol=1e-12)
+    np.testing.assert_allclose(var, rv, rtol=1e-11, atol=1e-300)
+
+
+def test_array_integrand_results():
+    for correlate in (True, False):
+        I = vg.Integrator(3 * [[0, 1]], neval=20000, seed=9, correlate_integrals=correlate)
+        I(_f3, nitn=6)
+        r = I(_f3, nitn=8)
+        assert isinstance(r, vg.RAvgArray) and r.shape == (3,)
+        # exact values by a fine FP64 tensor-product midpoint rule
+        m = 200
+        g1 = (np.arange(m) + 0.5) / m
+        e1 = np.exp(-20.0 * (g1 - 0.45) ** 2) / m
+        ex = np.array([e1.sum() ** 3, (g1 * e1).sum() * e1.sum() ** 2, (g1 * e1).sum() ** 2 * e1.sum()])
+        for k in range(3):
+            assert abs(r[k].mean - ex[k]) < 5 * r[k].sdev, (k, r[k], ex[k])
+        if correlate:
+            c = vg._gvar.corr(r[0], r[1])
+            assert 0.0 < c <= 1.0

@@ -1,0 +1,51 @@
+"""Flow-augmented vegas+ (FlowIntegrator) on the GPU.
+
+* gain: on the non-separable 8-d mixture of 4 Gaussians, the trained flow's
+  variance per evaluation beats plain vegas+ (same evaluations per
+  iteration, plain vegas+ given the same number of iterations) by >= 5x;
+* unbiasedness: the flow iterations' weighted average agrees with the exact
+  integral within 5 sigma (every sample carries the flow's exact logdet);
+* gate: on an integrand plain vegas+ integrates exactly (a constant), the
+  flow cannot win and is switched off, after which plain vegas+ continues.
+"""
+import numpy as np
+import pytest
+import torch
+
+import vegas_gb300 as vg
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixture(dim=8, seed=4):
+    rng = np.random.default_rng(seed)
+    return vg.GaussianMixture(rng.uniform(0.15, 0.85, (4, dim)), sigma=0.03)
+
+
+def test_flow_beats_plain_vegas_on_mixture():
+    from vegas_gb300.flow_vegas import FlowIntegrator
+    f = _mixture()
+    exact = f.exact(8)
+    neval = 1 << 18
+    plain = vg.Integrator(8 * [[0, 1]], neval=neval, seed=11)
+    plain(f, nitn=50)
+    rp = plain(f, nitn=10)
+    v_plain = np.median([r.sdev ** 2 for r in rp.itn_results]) * plain.last_neval
+    F = FlowIntegrator(8 * [[0, 1]], neval=neval, seed=11, plain_itn=10, kl_itn=10, train_itn=40,
+                       grace=1000, train_steps=6, train_batch=1 << 15)
+    F(f, nitn=50)                      # 10 plain + 40 training flow iterations
+    rf = F(f, nitn=10)                 # frozen flow
+    assert F.flow_on
+    v_flow = np.median([h['sdev'] ** 2 * h['neval'] for h in F.history[-10:]])
+    assert v_flow * 5 <= v_plain, (v_flow, v_plain)
+    assert abs(rf.mean - exact) < 5 * rf.sdev, (rf.mean, rf.sdev, exact)
+
+
+def test_flow_switched_off_when_plain_vegas_wins():
+    from vegas_gb300.flow_vegas import FlowIntegrator
+    F = FlowIntegrator(4 * [[0, 1]], neval=20000, seed=3, plain_itn=4, kl_itn=2, grace=2, patience=2,
+                       train_steps=1, train_batch=4096)
+    r = F(vg.Constant(2.0), nitn=14)
+    assert F.flow_dead and not F.flow_on
+    assert abs(r.mean - 2.0) < 1e-6
+    assert not F.history[-1]['flow']

@@ -404,10 +404,35 @@ class Integrator(object):
             f = torch.as_tensor(np.asarray(f, dtype=float), device=self.device)
         f = f.to(self.device)
         if f.dim() > 1:
-            if f[0].numel() != 1:
-                raise NotImplementedError('array-valued integrands are not supported yet')
-            f = f.reshape(f.shape[0])
+            f = f.reshape(f.shape[0], -1)   # [n, s], s = size of one integrand value
         return f
+
+    def _fshape(self, fcn, kind, x1, s):
+        """Shape of one integrand value (s components; the reference takes it
+        from a sample evaluation, pyx:3068-3082)."""
+        if s == 1:
+            return ()
+        if kind == 'lbatch':
+            out = fcn(x1)
+        elif kind == 'rbatch':
+            out = fcn(x1.t())
+        else:
+            return (s,)
+        shp = tuple(torch.as_tensor(out).shape)
+        return shp[1:] if kind == 'lbatch' else shp[:-1]
+
+    def _reduce_array(self, it, f, fdt, w):
+        """Mean and (co)variance of every component of an array integrand."""
+        L = N.load()
+        s = int(f.shape[1])
+        corr = 1 if self.correlate_integrals else 0
+        need = int(L.vg_reduce_array_work_bytes(s, corr))
+        work = torch.empty(need, dtype=torch.uint8, device=self.device)
+        mean = torch.empty(s, dtype=torch.float64, device=self.device)
+        var = torch.empty((s, s), dtype=torch.float64, device=self.device)
+        N.check(L.vg_reduce_array(ctypes.byref(it), N.ptr(f), fdt, s, corr, N.ptr(w), N.ptr(mean),
+                                  N.ptr(var), N.ptr(work), need, N.stream_ptr(self.device)))
+        return mean.cpu().numpy(), var.cpu().numpy()
 
     def __call__(self, fcn, save=None, saveall=None, **kargs):
         """Integrate ``fcn``; returns an :class:`RAvg` (pyx:1912-2230)."""
@@ -420,7 +445,9 @@ class Integrator(object):
         L = N.load()
         stream = N.stream_ptr(self.device)
         dt = torch.float64 if self.precision == 'fp64' else torch.float32
+        fshape = None
         for itn in range(self.nitn):
+            arr = None
             if self.analyzer is not None:
                 self.analyzer.begin(itn, self)
             it, ncap = self._struct()
@@ -442,8 +469,8 @@ class Integrator(object):
                     N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, N.ptr(u),
                                                  int(fcn.kind), N.dbl_array(p), len(p), stream))
                 else:
-                    x, _, _, _ = self._points(it, ncap, itn_word, u)
-                    f = torch.empty(ncap, dtype=dt, device=self.device)
+                    x, _, w, _ = self._points(it, ncap, itn_word, u)
+                    f = None
                     nb = max(1, int(self.min_neval_batch))
                     for lo in range(0, n, nb):
                         hi = min(n, lo + nb)
@@ -451,11 +478,20 @@ class Integrator(object):
                         if fb.shape[0] != hi - lo:
                             raise ValueError('integrand returned %d values for %d points'
                                              % (fb.shape[0], hi - lo))
-                        f[lo:hi] = fb.to(dt)
+                        if f is None:
+                            s_f = 1 if fb.dim() == 1 else int(fb.shape[1])
+                            if fshape is None:
+                                fshape = self._fshape(fcn, kind, x[:1], s_f)
+                            f = torch.empty((ncap, s_f) if s_f > 1 else ncap, dtype=dt,
+                                            device=self.device)
+                        f[lo:hi] = fb.to(dt) if f.dim() == 1 else fb.reshape(hi - lo, -1).to(dt)
                     if bool(torch.isnan(f[:n]).any()):
                         raise ValueError('integrand evaluates to nan')
-                    N.check(L.vg_reduce(ctypes.byref(it), itn_word, N.ptr(u), N.ptr(f),
-                                        N.VG_F64 if dt == torch.float64 else N.VG_F32, stream))
+                    fdt = N.VG_F64 if dt == torch.float64 else N.VG_F32
+                    f0 = f if f.dim() == 1 else f[:, 0].contiguous()
+                    N.check(L.vg_reduce(ctypes.byref(it), itn_word, N.ptr(u), N.ptr(f0), fdt, stream))
+                    if f.dim() > 1:
+                        arr = self._reduce_array(it, f, fdt, w)
             # adapt the map on the device before reading the iteration record
             N.check(L.vg_end_iteration(ctypes.byref(it), stream))
             st = self._read_stats()
@@ -469,7 +505,19 @@ class Integrator(object):
             self.neval_hcube_range = np.array([st.range_lo, st.range_hi])
             if self.beta > 0 and self.adapt and self.nhcube > 1:
                 self.sum_sigf = float(st.sum_sigf)
-            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            if arr is not None:
+                # array-valued integrand: RAvgArray of the integrand's shape
+                # (VegasIntegrand.format_result, pyx:3127-3147)
+                if not isinstance(result, RAvgArray):
+                    result = RAvgArray(fshape, weighted=self.adapt)
+                mean_a, var_a = arr
+                if self.correlate_integrals:
+                    g = gv.gvar(mean_a, var_a)
+                else:
+                    g = gv.gvar(mean_a, np.sqrt(np.clip(np.diag(var_a), 0.0, None)))
+                result.add(np.asarray(g, dtype=object).reshape(fshape))
+            else:
+                result.add(gv.gvar(st.mean, st.var ** 0.5))
             result.sum_neval += self.last_neval
             if self.analyzer is not None:
                 self.analyzer.end(result.itn_results[-1], result)
