@@ -245,6 +245,57 @@ def replica_seed(base, rank):
     return (int(base) + 7919 * int(rank)) & ((1 << 63) - 1)
 
 
+def config1_line(dev, nitn=20):
+    """The CPU-sized workload: dim 4, f = (100/pi)^2 exp(-100 sum (x-1/2)^2),
+    neval 1e4/itn, FP64 throughout.  Latency per iteration through the public
+    API (host round trip per iteration) and for iterations captured in a CUDA
+    graph (allocation, fused evaluation + reduction, adapt; the iteration
+    record copied on the device)."""
+    import ctypes
+    import torch
+    import vegas_gb300 as vg
+    from vegas_gb300 import _native as N
+    L = N.load()
+    f = vg.Gaussian(a=100.0, c=0.5, dim=4)
+    integ = vg.Integrator(4 * [[0, 1]], neval=10000, precision='fp64', seed=31, device=dev)
+    integ(f, nitn=3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = integ(f, nitn=nitn)
+    torch.cuda.synchronize()
+    t_api = (time.perf_counter() - t0) / nitn
+    # CUDA graph of nitn iterations; sum_sigf carries over in the device record
+    g_int = vg.Integrator(4 * [[0, 1]], neval=10000, precision='fp64', seed=32, device=dev)
+    it, ncap = g_int._struct()
+    g_int._put_sum_sigf()
+    params = N.dbl_array(f.params(4))
+    recs = torch.empty((nitn, ctypes.sizeof(N.VgStats)), dtype=torch.uint8, device=dev)
+    s = torch.cuda.Stream(device=dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            sp = N.stream_ptr(dev)
+            for k in range(nitn):
+                N.check(L.vg_allocate(ctypes.byref(it), sp))
+                N.check(L.vg_fused_iteration(ctypes.byref(it), k + 1, None, f.kind, params, 3, sp))
+                N.check(L.vg_end_iteration(ctypes.byref(it), sp))
+                recs[k].copy_(g_int._stats)
+    torch.cuda.current_stream(dev).wait_stream(s)
+    graph.replay()                         # warm-up replay
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    t_graph = e0.elapsed_time(e1) / 1e3 / nitn
+    return {'workload': 'dim 4, (100/pi)^2 exp(-100 sum (x-1/2)^2), neval 1e4/itn, ninc 1000, '
+                        'alpha 0.5, beta 0.75, FP64 throughout',
+            'seconds_per_iteration_api': t_api, 'seconds_per_iteration_graph': t_graph,
+            'result': str(r), 'exact': f.exact(4)}
+
+
 def gpu_arm(args):
     import numpy as np
     import torch
@@ -352,7 +403,9 @@ def gpu_arm(args):
             'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
         if rank == 0:
             tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
-    batched = lattice = None
+    batched = lattice = small = None
+    if rank == 0:
+        small = config1_line(dev)
     if not args.no_batch and rank == 0:
         batched = batched_line(dev)
         lattice = lattice_line(dev)
@@ -380,6 +433,7 @@ def gpu_arm(args):
         'time_to_1e-4': tta,
         'batched': batched,
         'lattice_scan': lattice,
+        'small_fp64': small,
     }
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)
@@ -503,9 +557,18 @@ def cpu_baseline(iters=2, kind='port'):
         out = st.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=5, itn=k + 1, nthreads=cores)
         ne += out['neval']
     dt = time.perf_counter() - t0
+    # the CPU-sized workload (dim 4 Gaussian, neval 1e4, FP64): seconds per
+    # iteration of the reference algorithm on one core
+    st1 = O.State(4 * [[0, 1]], 10000)
+    p1 = [100.0, 0.5, (100.0 / 3.141592653589793) ** 2]
+    t1 = time.perf_counter()
+    for k in range(20):
+        st1.iterate(O.F_GAUSS, p1, seed=5, itn=k + 1, nthreads=1)
+    t1 = (time.perf_counter() - t1) / 20
     return {'value': ne / dt, 'unit': 'evals/s', 'cores': cores, 'kind': kind,
             'sample': '%d full iterations of the workload (neval=1e6 each), FP64, %d threads'
-                      % (iters, cores)}
+                      % (iters, cores),
+            'small_fp64_seconds_per_iteration_1core': t1}
 
 
 def reference_arm(args):

@@ -341,6 +341,11 @@ int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm,
                     unsigned int *queue, unsigned int *sync, int group, int *status, size_t smem, int grid,
                     int variant, void *stream);
 
+/* Instrumentation: while set (device counter, NULL = off), the FP32 ridge
+ * adds the number of Gaussian terms it evaluates -- the ones that can be
+ * nonzero in FP32; the rest are exactly zero and skipped. */
+int vg_set_term_counter(unsigned long long *count);
+
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);

@@ -191,6 +191,22 @@ __device__ __forceinline__ VgKSum vg_block_ksum(VgKSum v, VgKSum *smem /* NT/32 
     return v;
 }
 
+// Float-float (double-single) accumulation: (h, l) += x with Knuth's
+// TwoSum (error-free in h, the rounding error carried in l).  The FP32 mode
+// accumulates a thread's few samples this way (about 2^-48 relative, close
+// to FP64) before the per-hypercube sums continue in FP64.  __fadd_rn /
+// __fsub_rn keep the compiler from reassociating or contracting.
+__device__ __forceinline__ void vg_ff_add(float &h, float &l, float x)
+{
+    const float s = __fadd_rn(h, x);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    h = s;
+    l = __fadd_rn(l, e);
+}
+
+__device__ __forceinline__ double vg_ff_value(float h, float l) { return (double)h + (double)l; }
+
 #define VG_CUDA_CHECK(expr)                                                                  \
     do {                                                                                     \
         cudaError_t _e = (expr);                                                             \

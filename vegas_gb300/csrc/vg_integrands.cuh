@@ -16,6 +16,7 @@
 struct VgParams {
     int n;
     float fc[8];                 // FP32 constants, precomputed on the host (vg_prepare_f32_host)
+    unsigned long long *term_count;   // optional: Gaussian terms evaluated (ridge, FP32)
     double p[VG_MAX_PARAMS];
 };
 
@@ -212,8 +213,28 @@ __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *
         const float E0 = -k.c[0] * R;
         const float w = m * k.c[1];
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-        int j = 0;
-        for (; j + 4 <= nterm; j += 4) {
+        // terms with E0 - (w - v_j)^2 < -127 are exactly zero (ex2.approx.ftz
+        // flushes them): evaluate the window of the others only, aligned to
+        // the 4-way accumulator pattern -- the sum is bit-identical
+        int j = 0, jend = nterm & ~3;
+        {
+            const float rad2 = E0 + 127.f;
+            if (rad2 <= 0.f) {
+                jend = 0;
+            } else {
+                const float delta = sqrtf(rad2) * 1.0001f + 1e-3f;
+                const float rc = 1.f / k.c[4];
+                int jlo = (int)floorf((w - delta) * rc - 0.5f) - 1;
+                int jhi = (int)ceilf((w + delta) * rc - 0.5f) + 1;
+                jlo = jlo < 0 ? 0 : jlo;
+                jhi = jhi > nterm - 1 ? nterm - 1 : jhi;
+                j = jlo & ~3;
+                const int je = (jhi & ~3) + 4;
+                jend = je < jend ? je : jend;
+                if (j > jend) j = jend;
+            }
+        }
+        for (; j + 4 <= jend; j += 4) {
             float4 v = *reinterpret_cast<const float4 *>(tab + j);
             float d0 = w - v.x, d1 = w - v.y, d2 = w - v.z, d3 = w - v.w;
             a0 += vg_ex2(fmaf(-d0, d0, E0));
@@ -221,7 +242,7 @@ __device__ __forceinline__ float vg_eval_f32(const VgF32Consts &k, const float *
             a2 += vg_ex2(fmaf(-d2, d2, E0));
             a3 += vg_ex2(fmaf(-d3, d3, E0));
         }
-        for (; j < nterm; j++) {
+        for (j = nterm & ~3; j < nterm; j++) {
             float d0 = w - tab[j];
             a0 += vg_ex2(fmaf(-d0, d0, E0));
         }

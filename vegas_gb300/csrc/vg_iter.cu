@@ -493,6 +493,16 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
+static unsigned long long *g_term_count = nullptr;
+
+// Instrumentation: while set, the FP32 ridge adds the number of Gaussian
+// terms it evaluates to *count (device); NULL turns it off.
+extern "C" int vg_set_term_counter(unsigned long long *count)
+{
+    g_term_count = count;
+    return VG_OK;
+}
+
 // Validate the parameters of a built-in integrand and fill P (including its
 // host-precomputed FP32 constants); tab_len = length of its per-CTA table.
 int vg_build_params(int kind, int dim, const double *params, int nparams, VgParams *Pp, int *tab_len_out)
@@ -524,6 +534,7 @@ int vg_build_params(int kind, int dim, const double *params, int nparams, VgPara
     }
     if (nparams < need) return vg_fail(VG_ERR_VALUE, "integrand needs %d parameters", need);
     vg_prepare_f32_host(P, kind, dim);
+    P.term_count = (kind == VG_F_RIDGE) ? g_term_count : nullptr;
     *tab_len_out = tab_len;
     return VG_OK;
 }

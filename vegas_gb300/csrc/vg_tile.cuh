@@ -200,12 +200,12 @@ template <typename T, int KIND, int DIMB, int S>
 struct BatchEval {
     static __device__ __forceinline__ void run(const VgParams &prm, const VgF32Consts &kc,
                                                const float *tab, int nterm, int dim,
-                                               const T (&x)[S][DIMB], double (&f)[S])
+                                               const T (&x)[S][DIMB], T (&f)[S])
     {
 #pragma unroll
         for (int k = 0; k < S; k++) {
-            if (sizeof(T) == 8) f[k] = vg_eval_f64<KIND, DIMB>(prm, dim, (const double *)x[k]);
-            else f[k] = (double)vg_eval_f32<KIND, DIMB>(kc, tab, nterm, dim, (const float *)x[k]);
+            if (sizeof(T) == 8) f[k] = (T)vg_eval_f64<KIND, DIMB>(prm, dim, (const double *)x[k]);
+            else f[k] = (T)vg_eval_f32<KIND, DIMB>(kc, tab, nterm, dim, (const float *)x[k]);
         }
     }
 };
@@ -216,7 +216,7 @@ template <int DIMB, int S>
 struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
     static __device__ __forceinline__ void run(const VgParams &prm, const VgF32Consts &kc,
                                                const float *tab, int nterm, int dim,
-                                               const float (&x)[S][DIMB], double (&f)[S])
+                                               const float (&x)[S][DIMB], float (&f)[S])
     {
         float E0[S], w[S], a0[S], a1[S];
 #pragma unroll
@@ -240,8 +240,32 @@ struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
         }
         const float4 *t4 = reinterpret_cast<const float4 *>(tab);
         const int n4 = nterm >> 2;
+        // Window of groups of 4 terms that can be nonzero for one of the S
+        // samples: a term with E0 - (w - v_j)^2 < -127 is exactly zero
+        // (ex2.approx.ftz flushes it), so skipping whole groups of such terms
+        // leaves every accumulator -- and f -- bit-identical.
+        int qlo = n4, qhi = 0;
+        const float rc = 1.f / kc.c[4];
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            const float rad2 = E0[k] + 127.f;
+            if (rad2 > 0.f) {
+                const float delta = sqrtf(rad2) * 1.0001f + 1e-3f;
+                int jlo = (int)floorf((w[k] - delta) * rc - 0.5f) - 1;
+                int jhi = (int)ceilf((w[k] + delta) * rc - 0.5f) + 1;
+                jlo = jlo < 0 ? 0 : jlo;
+                jhi = jhi > nterm - 1 ? nterm - 1 : jhi;
+                qlo = min(qlo, jlo >> 2);
+                qhi = max(qhi, min(n4, (jhi >> 2) + 1));
+            }
+        }
+        if (prm.term_count != nullptr) {   // instrumentation: terms evaluated
+            const unsigned int nt = qhi > qlo ? (unsigned int)(4 * S * (qhi - qlo)) : 0u;
+            const unsigned int tot = __reduce_add_sync(0xffffffffu, nt);
+            if ((threadIdx.x & 31) == 0) atomicAdd(prm.term_count, (unsigned long long)tot);
+        }
 #pragma unroll 2
-        for (int q = 0; q < n4; q++) {
+        for (int q = qlo; q < qhi; q++) {
             const float4 v = t4[q];
 #pragma unroll
             for (int k = 0; k < S; k++) {
@@ -260,7 +284,7 @@ struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
             }
         }
 #pragma unroll
-        for (int k = 0; k < S; k++) f[k] = (double)(kc.c[2] * (a0[k] + a1[k]));
+        for (int k = 0; k < S; k++) f[k] = kc.c[2] * (a0[k] + a1[k]);
     }
 };
 
@@ -417,7 +441,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             }
         }
         T xs[S][DIMB];
-        double wg[S];
+        T wg[S];   // sampler weight (FP32 in the FP32 mode)
         int lhs[S];
         int cur = lh;
 #pragma unroll
@@ -492,8 +516,8 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                             (unsigned short)((yd > (T)0 && yd < (T)1 && iy < K) ? iy : 0xffff);
                 }
                 // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
-                if (sizeof(T) == 8) wg[k] = __dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
-                else wg[k] = (double)((float)jac * (dv_yf / (float)nh));
+                if (sizeof(T) == 8) wg[k] = (T)__dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
+                else wg[k] = (T)((float)jac * (dv_yf / (float)nh));
                 if (MODE == MODE_POINTS) {
                     T *xo = (T *)a.x_out;
 #pragma unroll
@@ -505,14 +529,14 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                         for (int d = 0; d < DIMB; d++)
                             if (d < dim) yo[ig * dim + d] = yv[d];
                     }
-                    if (a.wgt_out) a.wgt_out[ig] = wg[k];
+                    if (a.wgt_out) a.wgt_out[ig] = (double)wg[k];
                     if (a.hc_out) a.hc_out[ig] = h0 + cur;
                 }
             }
         }
         if (MODE == MODE_POINTS) continue;
 
-        double fv[S];
+        T fv[S];
         if (MODE == MODE_FUSED || MODE == MODE_EVAL) {
             BatchEval<T, KIND, DIMB, S>::run(prm, kc, itab, a.tab_len, dim, xs, fv);
             if (MODE == MODE_EVAL) {
@@ -524,29 +548,29 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         } else {
 #pragma unroll
             for (int k = 0; k < S; k++) {
-                fv[k] = 0.0;
+                fv[k] = (T)0;
                 if (k < nmine) {
                     const int64_t ig = tile_start + li0 + k;
-                    fv[k] = a.f_f64 ? ((const double *)a.f_in)[ig]
-                                    : (double)((const float *)a.f_in)[ig];
+                    fv[k] = a.f_f64 ? (T)((const double *)a.f_in)[ig]
+                                    : (T)((const float *)a.f_in)[ig];
                 }
             }
         }
-        double wf[S];
+        T wf[S];   // wgt * f, pyx:2143 (FP32 in the FP32 mode)
 #pragma unroll
         for (int k = 0; k < S; k++) {
-            wf[k] = 0.0;
+            wf[k] = (T)0;
             if (k >= nmine) continue;
             if (fv[k] != fv[k]) nan_local = 1;
-            double w1;
+            double w1 = 0.0;
             float wf32 = 0.f;
             if (sizeof(T) == 8) {
-                w1 = __dmul_rn(wg[k], fv[k]);   // wgt * f, pyx:2143
+                w1 = __dmul_rn((double)wg[k], (double)fv[k]);
+                wf[k] = (T)w1;
             } else {
                 wf32 = (float)wg[k] * (float)fv[k];
-                w1 = (double)wf32;
+                wf[k] = (T)wf32;
             }
-            wf[k] = w1;
             if (use_bins) {
                 // fdv2 = (wgt*f*neval)^2, pyx:2173; |fdv2| into the bins, pyx:460-463
                 T fd;
@@ -576,10 +600,21 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         const int fk = has ? lhs[0] : 0x7fffffff;
         const int lk = has ? lhs[nmine - 1] : 0x7fffffff;
         double fsum = 0.0, lsum = 0.0;
+        if (sizeof(T) == 8) {
 #pragma unroll
-        for (int k = 0; k < S; k++) {
-            if (k < nmine && lhs[k] == fk) fsum += wf[k];
-            if (k < nmine && lhs[k] == lk) lsum += wf[k];
+            for (int k = 0; k < S; k++) {
+                if (k < nmine && lhs[k] == fk) fsum += (double)wf[k];
+                if (k < nmine && lhs[k] == lk) lsum += (double)wf[k];
+            }
+        } else {   // FP32 mode: float-float over the thread's samples, FP64 from here on
+            float fh = 0.f, fl = 0.f, lh2 = 0.f, ll = 0.f;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                if (k < nmine && lhs[k] == fk) vg_ff_add(fh, fl, (float)wf[k]);
+                if (k < nmine && lhs[k] == lk) vg_ff_add(lh2, ll, (float)wf[k]);
+            }
+            fsum = vg_ff_value(fh, fl);
+            lsum = vg_ff_value(lh2, ll);
         }
         keyF[tid] = fk;
         keyL[tid] = lk;
@@ -602,21 +637,71 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 const int key = lhs[k];
                 int k1 = k;
                 double Sloc = 0.0;
-                while (k1 < nmine && lhs[k1] == key) Sloc += wf[k1++];
+                if (sizeof(T) == 8) {
+                    while (k1 < nmine && lhs[k1] == key) Sloc += (double)wf[k1++];
+                } else {
+                    float sh = 0.f, sl = 0.f;
+                    while (k1 < nmine && lhs[k1] == key) vg_ff_add(sh, sl, (float)wf[k1++]);
+                    Sloc = vg_ff_value(sh, sl);
+                }
                 const int nin = win_off[key + 1] - win_off[key];
                 const bool is_first = (key == fk), is_last = (key == lk);
                 const double Sseg = (is_first || is_last) ? seg_S[key] : Sloc;
                 const double m = vg_div<T>(Sseg, (double)nin);
                 const double thr = __dmul_rn(VG_EPSILON, fabs(m));
                 double Dr = 0.0, Qr = 0.0;
-                for (int q = k; q < k1; q++) {
-                    const double dwf = __dsub_rn(wf[q], m);
-                    if (fabs(dwf) < thr) {
-                        Qr = __dadd_rn(Qr, __dmul_rn(thr, thr));
-                    } else {
-                        Qr = __dadd_rn(Qr, __dmul_rn(dwf, dwf));
-                        Dr = __dadd_rn(Dr, dwf);
+                if (sizeof(T) == 8) {
+                    for (int q = k; q < k1; q++) {
+                        const double dwf = __dsub_rn((double)wf[q], m);
+                        if (fabs(dwf) < thr) {
+                            Qr = __dadd_rn(Qr, __dmul_rn(thr, thr));
+                        } else {
+                            Qr = __dadd_rn(Qr, __dmul_rn(dwf, dwf));
+                            Dr = __dadd_rn(Dr, dwf);
+                        }
                     }
+                } else {
+                    // FP32 mode: deviations about m as float-float (m split
+                    // into m_hi + m_lo), their squares by TwoProd, sums as
+                    // float-float; the EPSILON guard counted and added in FP64
+                    const float m_hi = (float)m;
+                    const float m_lo = (float)(m - (double)m_hi);
+                    const float thr_f = (float)thr;
+                    float dh_s = 0.f, dl_s = 0.f, qh = 0.f, ql = 0.f;
+                    int nguard = 0;
+                    double Qbig = 0.0;
+                    for (int q = k; q < k1; q++) {
+                        float e0;
+                        {   // TwoSum(wf, -m_hi) then subtract m_lo
+                            const float x = (float)wf[q];
+                            const float s0 = __fsub_rn(x, m_hi);
+                            const float bb = __fsub_rn(s0, x);
+                            e0 = __fadd_rn(__fsub_rn(x, __fsub_rn(s0, bb)), __fsub_rn(-m_hi, bb));
+                            e0 = __fsub_rn(e0, m_lo);
+                            const float d = __fadd_rn(s0, e0);   // renormalise (fast TwoSum)
+                            e0 = __fsub_rn(e0, __fsub_rn(d, s0));
+                            if (fabsf(d) < thr_f) {   // |dwf| < EPSILON |mean|, pyx:2156
+                                nguard++;
+                                continue;
+                            }
+                            if (fabsf(d) > 1e18f) {   // squares beyond the float range: FP64
+                                const double dd = (double)d + (double)e0;
+                                Qbig = __dadd_rn(Qbig, __dmul_rn(dd, dd));
+                                vg_ff_add(dh_s, dl_s, d);
+                                dl_s = __fadd_rn(dl_s, e0);
+                                continue;
+                            }
+                            const float p = __fmul_rn(d, d);
+                            const float pe = __fadd_rn(fmaf(d, d, -p), __fmul_rn(2.f * d, e0));
+                            vg_ff_add(qh, ql, p);
+                            ql = __fadd_rn(ql, pe);
+                            vg_ff_add(dh_s, dl_s, d);
+                            dl_s = __fadd_rn(dl_s, e0);
+                        }
+                    }
+                    Dr = vg_ff_value(dh_s, dl_s);
+                    Qr = __dadd_rn(__dadd_rn(vg_ff_value(qh, ql), Qbig),
+                                   __dmul_rn((double)nguard, __dmul_rn(thr, thr)));
                 }
                 if (is_first) dq_first = make_double2(Dr, Qr);
                 if (is_last) dq_last = make_double2(Dr, Qr);
