@@ -373,7 +373,18 @@ def gpu_arm(args):
     # -------- roofline of the fused kernel: SFU-bound (one ex2 per Gaussian term)
     kern_s = statistics.median(kern_ms) / 1e3
     ex2_per_launch = neval_step * RIDGE_M
-    achieved = ex2_per_launch / kern_s / 1e9
+    # Gaussian terms the kernel evaluates: those that can be nonzero in FP32
+    # (the others are exactly zero and skipped); counted in one extra,
+    # untimed iteration
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    N.check(L.vg_set_term_counter(N.ptr(cnt)))
+    params_c = N.dbl_array(f.params(DIM))   # rebuilt so the counter is attached
+    N.check(L.vg_allocate(ctypes.byref(it), stream))
+    N.check(L.vg_fused_iteration(ctypes.byref(it), itn, None, f.kind, params_c, 2, stream))
+    N.check(L.vg_set_term_counter(None))
+    torch.cuda.synchronize()
+    executed = int(cnt.item())
+    achieved = executed / kern_s / 1e9
     peak = measure_ex2_peak(L, dev)
     # -------- e2e through the public API
     integ2 = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=replica_seed(99, rank), device=dev)
@@ -426,9 +437,12 @@ def gpu_arm(args):
         'gpu_launches': 6 * args.steps,
         'roofline': {'bound': 'sfu', 'achieved': achieved, 'peak': peak, 'unit': 'Gex2/s',
                      'frac': achieved / peak, 'traffic': None,
-                     'kernel': 'tile_kernel<float, FUSED, RIDGE> (+finalize)',
-                     'algorithmic': '1 ex2 per Gaussian term: neval*M = %d per launch'
-                                    % ex2_per_launch},
+                     'kernel': 'ridge iteration: tile_kernel EVAL + REDUCE + finalize (CUDA events)',
+                     'algorithmic': 'ex2 evaluated per launch: %d (the terms that can be nonzero '
+                                    'in FP32; all M=1000 terms per evaluation = %d, the rest are '
+                                    'exactly zero and skipped)' % (executed, ex2_per_launch),
+                     'frac_all_terms': ex2_per_launch / kern_s / 1e9 / peak,
+                     'peak_source': 'MUFU ex2 probe kernel on this GPU (vg_probe_mufu_ex2)'},
         'clocks': clk,
         'time_to_1e-4': tta,
         'batched': batched,

@@ -146,6 +146,10 @@ int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const do
 /* AdaptiveMap.map, pyx:310-360: y[n,dim] -> x[n,dim], jac[n] (dtype VG_F32/VG_F64). */
 int vg_map(int dim, const int64_t *ninc, const double *grid, const double *inc, int64_t ldg,
            int64_t ldi, int64_t n, const void *y, void *x, void *jac, int dtype, void *stream);
+/* AdaptiveMap.jac1d (_vegas.pyx:265-295): out[n, dim] = dx[d]/dy[d] at y[n, dim]
+ * (dtype VG_F32 / VG_F64 for y and out). */
+int vg_jac1d(int dim, const int64_t *ninc, const double *inc, int64_t ldi, int64_t n, const void *y,
+             void *out, int dtype, void *stream);
 
 /* AdaptiveMap.add_training_data, pyx:421-464 (accumulates into sum_f / n_f). */
 int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, int64_t n, const void *y,

@@ -89,3 +89,40 @@ def test_array_integrand_results():
         if correlate:
             c = vg._gvar.corr(r[0], r[1])
             assert 0.0 < c <= 1.0
+
+
+def test_uses_jac_like_reference():
+    """uses_jac=True: the integrand receives dx/dy per direction (reference
+    test_vegas.py test_uses_jac: the integral of 1/prod(jac) over the map's
+    range is 1 for any map), for scalar, lbatch and rbatch integrands and
+    scalar / array results."""
+    import numpy as np
+    integ = vg.Integrator(2 * [[0, 2.]], precision='fp64', seed=3)
+
+    def check(f, array=False):
+        r = integ(f, nitn=1, neval=10, uses_jac=True)
+        ans = r[0, 0] if array else r
+        assert abs(ans.mean - 1.0) < 1e-10, ans
+
+    check(lambda x, jac: 1. / np.prod(jac))
+    check(lambda x, jac: [[1. / np.prod(jac)]], array=True)
+
+    @vg.rbatchintegrand
+    def fr(x, jac):
+        return 1. / torch.prod(jac, dim=0)
+    check(fr)
+
+    @vg.rbatchintegrand
+    def fr2(x, jac):
+        return (1. / torch.prod(jac, dim=0))[None, None, :]
+    check(fr2, array=True)
+
+    @vg.lbatchintegrand
+    def fl(x, jac):
+        return 1. / torch.prod(jac, dim=-1)
+    check(fl)
+
+    @vg.lbatchintegrand
+    def fl2(x, jac):
+        return (1. / torch.prod(jac, dim=-1))[:, None, None]
+    check(fl2, array=True)

@@ -229,13 +229,15 @@ class AdaptiveMap(object):
         ya = y if is_t else np.asarray(y, float)
         shape = tuple(ya.shape)
         yt, _ = self._as_device(ya.reshape(-1, shape[-1]))
-        yt = yt.to(torch.float64)
-        K = torch.as_tensor(self._ninc, dtype=torch.float64, device=self.device)
-        iy = torch.floor(yt * K).to(torch.int64)
-        iy = torch.minimum(iy, torch.as_tensor(self._ninc - 1, device=self.device))
-        idx = iy.t().contiguous()
-        incv = torch.gather(self._inc, 1, idx).t()
-        out = (incv * K).reshape(shape)
+        if yt.dtype not in (torch.float32, torch.float64):
+            yt = yt.to(torch.float64)
+        yt = yt.contiguous()
+        out = torch.empty_like(yt)
+        L = N.load()
+        N.check(L.vg_jac1d(self.dim, self._geom(), N.ptr(self._inc), self._inc.shape[1], yt.shape[0],
+                           N.ptr(yt), N.ptr(out), N.VG_F64 if yt.dtype == torch.float64 else N.VG_F32,
+                           N.stream_ptr(self.device)))
+        out = out.reshape(shape)
         return out if is_t else out.cpu().numpy()
 
     def jac(self, y):

@@ -170,6 +170,46 @@ extern "C" int vg_make_uniform(int dim, const int64_t *ninc, const double *xl, c
     return VG_OK;
 }
 
+namespace {
+// AdaptiveMap.jac1d (pyx:265-295): dx[d]/dy[d] = inc[d][iy] * ninc[d],
+// iy = floor(y ninc) (inc[ninc-1] at y = 1).
+template <typename T>
+__global__ void jac1d_kernel(MapGeom g, const double *__restrict__ inc, int64_t ldi, int64_t n,
+                             const T *__restrict__ y, T *__restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int d = 0; d < g.dim; d++) {
+        const int K = g.ninc[d];
+        int64_t iy;
+        if (sizeof(T) == 8) iy = (int64_t)floor(__dmul_rn((double)y[i * g.dim + d], (double)K));
+        else iy = (int64_t)floorf((float)y[i * g.dim + d] * (float)K);
+        if (iy >= K) iy = K - 1;
+        if (iy < 0) iy = 0;
+        out[i * g.dim + d] = (T)__dmul_rn(inc[d * ldi + iy], (double)K);
+    }
+}
+}  // namespace
+
+extern "C" int vg_jac1d(int dim, const int64_t *ninc, const double *inc, int64_t ldi, int64_t n,
+                        const void *y, void *out, int dtype, void *stream)
+{
+    vg_clear_error();
+    MapGeom g;
+    int rc = fill_geom(g, dim, ninc);
+    if (rc) return rc;
+    if (n <= 0) return VG_OK;
+    const int64_t nb = (n + 255) / 256;
+    if (dtype == VG_F64)
+        jac1d_kernel<double><<<(unsigned)nb, 256, 0, (cudaStream_t)stream>>>(g, inc, ldi, n, (const double *)y,
+                                                                              (double *)out);
+    else
+        jac1d_kernel<float><<<(unsigned)nb, 256, 0, (cudaStream_t)stream>>>(g, inc, ldi, n, (const float *)y,
+                                                                             (float *)out);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
 extern "C" int vg_map(int dim, const int64_t *ninc, const double *grid, const double *inc,
                       int64_t ldg, int64_t ldi, int64_t n, const void *y, void *x, void *jac,
                       int dtype, void *stream)

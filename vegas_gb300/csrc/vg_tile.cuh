@@ -195,6 +195,83 @@ __device__ __forceinline__ double2 seg_scan(int flag, double2 v, double2 *P, dou
     return v;
 }
 
+// (ah, al) += (bh, bl) in float-float (TwoSum of the heads, tails added,
+// renormalised).  Used by the FP32 mode's reduction within a tile.
+__device__ __forceinline__ void ff_add_pair(float &ah, float &al, float bh, float bl)
+{
+    const float s = __fadd_rn(ah, bh);
+    const float bb = __fsub_rn(s, ah);
+    float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    ah = __fadd_rn(s, e);
+    al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
+// Inclusive segmented scan over the NT threads of float-float values:
+// (x, y) is one float-float number, and with K == 2 (z, w) a second one.
+template <int K>
+__device__ __forceinline__ float4 seg_scan_ff(int flag, float4 v, float4 *P, float4 *wsum, int *wflag)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int f = flag;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float ux = __shfl_up_sync(0xffffffffu, v.x, off);
+        const float uy = __shfl_up_sync(0xffffffffu, v.y, off);
+        float uz = 0.f, uw = 0.f;
+        if (K == 2) {
+            uz = __shfl_up_sync(0xffffffffu, v.z, off);
+            uw = __shfl_up_sync(0xffffffffu, v.w, off);
+        }
+        const int uf = __shfl_up_sync(0xffffffffu, f, off);
+        if (lane >= off) {
+            if (!f) {
+                ff_add_pair(v.x, v.y, ux, uy);
+                if (K == 2) ff_add_pair(v.z, v.w, uz, uw);
+            }
+            f |= uf;
+        }
+    }
+    if (lane == 31) {
+        wsum[w] = v;
+        wflag[w] = f;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const int NW = NT / 32;
+        float4 x = lane < NW ? wsum[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        int g = lane < NW ? wflag[lane] : 1;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float ux = __shfl_up_sync(0xffffffffu, x.x, off);
+            const float uy = __shfl_up_sync(0xffffffffu, x.y, off);
+            float uz = 0.f, uw = 0.f;
+            if (K == 2) {
+                uz = __shfl_up_sync(0xffffffffu, x.z, off);
+                uw = __shfl_up_sync(0xffffffffu, x.w, off);
+            }
+            const int ug = __shfl_up_sync(0xffffffffu, g, off);
+            if (lane >= off) {
+                if (!g) {
+                    ff_add_pair(x.x, x.y, ux, uy);
+                    if (K == 2) ff_add_pair(x.z, x.w, uz, uw);
+                }
+                g |= ug;
+            }
+        }
+        if (lane < NW) wsum[lane] = x;
+    }
+    __syncthreads();
+    if (w > 0 && !f) {
+        const float4 c = wsum[w - 1];
+        ff_add_pair(v.x, v.y, c.x, c.y);
+        if (K == 2) ff_add_pair(v.z, v.w, c.z, c.w);
+    }
+    P[threadIdx.x] = v;
+    __syncthreads();
+    return v;
+}
+
 // ------------------------------------------------- integrand, batched over S
 template <typename T, int KIND, int DIMB, int S>
 struct BatchEval {
@@ -595,26 +672,161 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             }
         }
 
+        if constexpr (sizeof(T) == 4) {
+        // ---- FP32 mode: the tile's reduction in float-float (TwoSum/TwoProd,
+        // about 2^-48 relative), FP64 once per hypercube -- GB300 runs FP64 at
+        // a small fraction of the FP32 rate.  Same two passes as below.
+        const int has = nmine > 0;
+        const int fk = has ? lhs[0] : 0x7fffffff;
+        const int lk = has ? lhs[nmine - 1] : 0x7fffffff;
+        float fh = 0.f, fl = 0.f, lh2 = 0.f, ll = 0.f;
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+            if (k < nmine && lhs[k] == fk) vg_ff_add(fh, fl, (float)wf[k]);
+            if (k < nmine && lhs[k] == lk) vg_ff_add(lh2, ll, (float)wf[k]);
+        }
+        keyF[tid] = fk;
+        keyL[tid] = lk;
+        __syncthreads();
+        const int prevL = tid > 0 ? keyL[tid - 1] : -1;
+        const int nextF = tid < NT - 1 ? keyF[tid + 1] : -2;
+        const int flag = (tid == 0) || (lk != prevL);
+        float4 *Pf = reinterpret_cast<float4 *>(Pv);
+        float4 *wsf = reinterpret_cast<float4 *>(wsum);
+        float2 *segf = reinterpret_cast<float2 *>(seg_S);
+        const float4 Pi = seg_scan_ff<1>(flag, make_float4(lh2, ll, 0.f, 0.f), Pf, wsf, wflag);
+        const int ends_last = has && (lk != nextF);
+        if (has && lk != fk) {
+            float ch = fh, cl = fl;
+            if (tid > 0 && prevL == fk) ff_add_pair(ch, cl, Pf[tid - 1].x, Pf[tid - 1].y);
+            segf[fk] = make_float2(ch, cl);
+        }
+        if (ends_last) segf[lk] = make_float2(Pi.x, Pi.y);
+        __syncthreads();
+        // per hypercube: mean, variance, sigf in FP64 (pyx:2174-2186)
+        auto finish = [&](int64_t h, int nin, double Sx, double Dx, double Qx) {
+            const double nd = (double)nin;
+            const double vh = vg_div<T>(__dsub_rn(__dmul_rn(nd, Qx), __dmul_rn(Dx, Dx)), __dsub_rn(nd, 1.));
+            acc_m += __dadd_rn(Sx, Dx);
+            acc_v += vh;
+            if (a.adaptive) {
+                const double sg = vg_pow_fast(fabs(vh), beta_half);
+                a.sigf[h] = sg;
+                acc_s += sg;
+            }
+        };
+        float4 dq_first = make_float4(0.f, 0.f, 0.f, 0.f), dq_last = dq_first;   // (D, Q) float-float
+        {
+            int k = 0;
+            while (k < nmine) {
+                const int key = lhs[k];
+                int k1 = k;
+                float sh = 0.f, sl = 0.f;
+                while (k1 < nmine && lhs[k1] == key) vg_ff_add(sh, sl, (float)wf[k1++]);
+                const int nin = win_off[key + 1] - win_off[key];
+                const bool is_first = (key == fk), is_last = (key == lk);
+                if (is_first || is_last) {
+                    const float2 t2 = segf[key];
+                    sh = t2.x;
+                    sl = t2.y;
+                }
+                // mean m = S / nin as float-float
+                const float fn = (float)nin;
+                const float rn = 1.f / fn;
+                const float m_hi = sh * rn;
+                const float m_lo = (__fadd_rn(fmaf(-m_hi, fn, sh), sl)) * rn;
+                const float thr_f = (float)VG_EPSILON * fabsf(m_hi);
+                float dh_s = 0.f, dl_s = 0.f, qh = 0.f, ql = 0.f;
+                int nguard = 0;
+                double Qbig = 0.0;
+                for (int q = k; q < k1; q++) {
+                    const float x = (float)wf[q];
+                    const float s0 = __fsub_rn(x, m_hi);   // TwoSum(wf, -m_hi), then - m_lo
+                    const float bb = __fsub_rn(s0, x);
+                    float e0 = __fadd_rn(__fsub_rn(x, __fsub_rn(s0, bb)), __fsub_rn(-m_hi, bb));
+                    e0 = __fsub_rn(e0, m_lo);
+                    const float d = __fadd_rn(s0, e0);
+                    e0 = __fsub_rn(e0, __fsub_rn(d, s0));
+                    if (fabsf(d) < thr_f) {   // |dwf| < EPSILON |mean|, pyx:2156
+                        nguard++;
+                        continue;
+                    }
+                    if (fabsf(d) > 1e18f) {   // squares beyond the float range: FP64
+                        const double dd = (double)d + (double)e0;
+                        Qbig = __dadd_rn(Qbig, __dmul_rn(dd, dd));
+                    } else {
+                        const float p = __fmul_rn(d, d);
+                        const float pe = __fadd_rn(fmaf(d, d, -p), __fmul_rn(2.f * d, e0));
+                        ff_add_pair(qh, ql, p, pe);
+                    }
+                    ff_add_pair(dh_s, dl_s, d, e0);
+                }
+                if (nguard) ff_add_pair(qh, ql, (float)nguard * thr_f * thr_f, 0.f);
+                if (is_first) dq_first = make_float4(dh_s, dl_s, qh, ql);
+                if (is_last) dq_last = make_float4(dh_s, dl_s, qh, ql);
+                if (!is_first && !is_last)   // hypercube wholly inside this thread
+                    finish(h0 + key, nin, vg_ff_value(sh, sl), vg_ff_value(dh_s, dl_s),
+                           __dadd_rn(vg_ff_value(qh, ql), Qbig));
+                else if (Qbig != 0.0) {   // rare: carry the FP64 part through the scan's head
+                    if (is_first) dq_first.z = (float)((double)dq_first.z + Qbig);
+                    else dq_last.z = (float)((double)dq_last.z + Qbig);
+                }
+                k = k1;
+            }
+        }
+        __syncthreads();
+        const float4 Pq = seg_scan_ff<2>(flag, dq_last, Pf, wsf, wflag);
+#pragma unroll
+        for (int which = 0; which < 2; which++) {
+            int key;
+            float4 dq;
+            if (which == 0) {
+                if (!(has && lk != fk)) continue;
+                key = fk;
+                dq = dq_first;
+                if (tid > 0 && prevL == fk) {
+                    const float4 c = Pf[tid - 1];
+                    ff_add_pair(dq.x, dq.y, c.x, c.y);
+                    ff_add_pair(dq.z, dq.w, c.z, c.w);
+                }
+            } else {
+                if (!ends_last) continue;
+                key = lk;
+                dq = Pq;
+            }
+            const int64_t h = h0 + key;
+            const int nin = win_off[key + 1] - win_off[key];
+            const int nh = win_n[key];
+            const float2 sg2 = segf[key];
+            const double Sseg = vg_ff_value(sg2.x, sg2.y);
+            const double Dx = vg_ff_value(dq.x, dq.y), Qx = vg_ff_value(dq.z, dq.w);
+            const int64_t ostart = a.offsets[h];
+            const bool starts_before = ostart < tile_start;
+            const bool ends_after = ostart + nh > tile_start + tile_len;
+            if (!starts_before && !ends_after) {
+                finish(h, nin, Sseg, Dx, Qx);
+            } else {
+                TileRec r;
+                r.h = h;
+                r.n = (double)nin;
+                r.S = Sseg;
+                r.Q = Qx;
+                r.D = Dx;
+                r.spans = (starts_before && ends_after) ? 1 : 0;
+                r.pad = 0;
+                a.recs[2 * tile + (starts_before ? 0 : 1)] = r;
+            }
+        }
+        } else {
         // ---- pass 1: per-run sums of wf; segmented scan across threads
         const int has = nmine > 0;
         const int fk = has ? lhs[0] : 0x7fffffff;
         const int lk = has ? lhs[nmine - 1] : 0x7fffffff;
         double fsum = 0.0, lsum = 0.0;
-        if (sizeof(T) == 8) {
 #pragma unroll
-            for (int k = 0; k < S; k++) {
-                if (k < nmine && lhs[k] == fk) fsum += (double)wf[k];
-                if (k < nmine && lhs[k] == lk) lsum += (double)wf[k];
-            }
-        } else {   // FP32 mode: float-float over the thread's samples, FP64 from here on
-            float fh = 0.f, fl = 0.f, lh2 = 0.f, ll = 0.f;
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                if (k < nmine && lhs[k] == fk) vg_ff_add(fh, fl, (float)wf[k]);
-                if (k < nmine && lhs[k] == lk) vg_ff_add(lh2, ll, (float)wf[k]);
-            }
-            fsum = vg_ff_value(fh, fl);
-            lsum = vg_ff_value(lh2, ll);
+        for (int k = 0; k < S; k++) {
+            if (k < nmine && lhs[k] == fk) fsum += (double)wf[k];
+            if (k < nmine && lhs[k] == lk) lsum += (double)wf[k];
         }
         keyF[tid] = fk;
         keyL[tid] = lk;
@@ -637,71 +849,21 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 const int key = lhs[k];
                 int k1 = k;
                 double Sloc = 0.0;
-                if (sizeof(T) == 8) {
-                    while (k1 < nmine && lhs[k1] == key) Sloc += (double)wf[k1++];
-                } else {
-                    float sh = 0.f, sl = 0.f;
-                    while (k1 < nmine && lhs[k1] == key) vg_ff_add(sh, sl, (float)wf[k1++]);
-                    Sloc = vg_ff_value(sh, sl);
-                }
+                while (k1 < nmine && lhs[k1] == key) Sloc += (double)wf[k1++];
                 const int nin = win_off[key + 1] - win_off[key];
                 const bool is_first = (key == fk), is_last = (key == lk);
                 const double Sseg = (is_first || is_last) ? seg_S[key] : Sloc;
                 const double m = vg_div<T>(Sseg, (double)nin);
                 const double thr = __dmul_rn(VG_EPSILON, fabs(m));
                 double Dr = 0.0, Qr = 0.0;
-                if (sizeof(T) == 8) {
-                    for (int q = k; q < k1; q++) {
-                        const double dwf = __dsub_rn((double)wf[q], m);
-                        if (fabs(dwf) < thr) {
-                            Qr = __dadd_rn(Qr, __dmul_rn(thr, thr));
-                        } else {
-                            Qr = __dadd_rn(Qr, __dmul_rn(dwf, dwf));
-                            Dr = __dadd_rn(Dr, dwf);
-                        }
+                for (int q = k; q < k1; q++) {
+                    const double dwf = __dsub_rn((double)wf[q], m);
+                    if (fabs(dwf) < thr) {
+                        Qr = __dadd_rn(Qr, __dmul_rn(thr, thr));
+                    } else {
+                        Qr = __dadd_rn(Qr, __dmul_rn(dwf, dwf));
+                        Dr = __dadd_rn(Dr, dwf);
                     }
-                } else {
-                    // FP32 mode: deviations about m as float-float (m split
-                    // into m_hi + m_lo), their squares by TwoProd, sums as
-                    // float-float; the EPSILON guard counted and added in FP64
-                    const float m_hi = (float)m;
-                    const float m_lo = (float)(m - (double)m_hi);
-                    const float thr_f = (float)thr;
-                    float dh_s = 0.f, dl_s = 0.f, qh = 0.f, ql = 0.f;
-                    int nguard = 0;
-                    double Qbig = 0.0;
-                    for (int q = k; q < k1; q++) {
-                        float e0;
-                        {   // TwoSum(wf, -m_hi) then subtract m_lo
-                            const float x = (float)wf[q];
-                            const float s0 = __fsub_rn(x, m_hi);
-                            const float bb = __fsub_rn(s0, x);
-                            e0 = __fadd_rn(__fsub_rn(x, __fsub_rn(s0, bb)), __fsub_rn(-m_hi, bb));
-                            e0 = __fsub_rn(e0, m_lo);
-                            const float d = __fadd_rn(s0, e0);   // renormalise (fast TwoSum)
-                            e0 = __fsub_rn(e0, __fsub_rn(d, s0));
-                            if (fabsf(d) < thr_f) {   // |dwf| < EPSILON |mean|, pyx:2156
-                                nguard++;
-                                continue;
-                            }
-                            if (fabsf(d) > 1e18f) {   // squares beyond the float range: FP64
-                                const double dd = (double)d + (double)e0;
-                                Qbig = __dadd_rn(Qbig, __dmul_rn(dd, dd));
-                                vg_ff_add(dh_s, dl_s, d);
-                                dl_s = __fadd_rn(dl_s, e0);
-                                continue;
-                            }
-                            const float p = __fmul_rn(d, d);
-                            const float pe = __fadd_rn(fmaf(d, d, -p), __fmul_rn(2.f * d, e0));
-                            vg_ff_add(qh, ql, p);
-                            ql = __fadd_rn(ql, pe);
-                            vg_ff_add(dh_s, dl_s, d);
-                            dl_s = __fadd_rn(dl_s, e0);
-                        }
-                    }
-                    Dr = vg_ff_value(dh_s, dl_s);
-                    Qr = __dadd_rn(__dadd_rn(vg_ff_value(qh, ql), Qbig),
-                                   __dmul_rn((double)nguard, __dmul_rn(thr, thr)));
                 }
                 if (is_first) dq_first = make_double2(Dr, Qr);
                 if (is_last) dq_last = make_double2(Dr, Qr);
@@ -768,6 +930,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 r.pad = 0;
                 a.recs[2 * tile + (starts_before ? 0 : 1)] = r;
             }
+        }
         }
         if (tid == 0) {   // empty record slots
             const int64_t o0 = a.offsets[h0];

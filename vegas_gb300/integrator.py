@@ -392,14 +392,30 @@ class Integrator(object):
             return 'rbatch'
         return 'scalar'
 
-    def _eval_batch(self, fcn, kind, x):
+    def _eval_batch(self, fcn, kind, x, jac=None):
+        """fcn on a batch; with uses_jac, jac[n, dim] = dx/dy per direction is
+        passed as ``jac=`` (transposed for rbatch, per point for scalar
+        integrands), as in the reference (pyx:2127, 3309-3316)."""
         if kind == 'lbatch':
-            f = fcn(x)
+            f = fcn(x) if jac is None else fcn(x, jac=jac)
         elif kind == 'rbatch':
-            f = fcn(x.t())
+            f = fcn(x.t()) if jac is None else fcn(x.t(), jac=jac.t())
         else:
             xc = x.cpu().numpy()
-            f = np.array([fcn(xi) for xi in xc], dtype=float)
+            if jac is None:
+                f = [fcn(xi) for xi in xc]
+            else:
+                jc = jac.cpu().numpy()
+                f = [fcn(xi, jac=ji) for xi, ji in zip(xc, jc)]
+            f = np.array([np.asarray(fi, dtype=float).reshape(-1) for fi in f], dtype=float)
+            if f.ndim == 2 and f.shape[1] == 1:
+                f = f[:, 0]
+        if kind == 'rbatch' and not isinstance(f, torch.Tensor):
+            f = torch.as_tensor(np.asarray(f, dtype=float), device=self.device)
+        if kind == 'rbatch':
+            f = f.to(self.device)
+            if f.dim() > 1:   # rbatch returns [..., n]: batch index last
+                f = f.reshape(-1, x.shape[0]).t()
         if not isinstance(f, torch.Tensor):
             f = torch.as_tensor(np.asarray(f, dtype=float), device=self.device)
         f = f.to(self.device)
@@ -407,19 +423,18 @@ class Integrator(object):
             f = f.reshape(f.shape[0], -1)   # [n, s], s = size of one integrand value
         return f
 
-    def _fshape(self, fcn, kind, x1, s):
-        """Shape of one integrand value (s components; the reference takes it
-        from a sample evaluation, pyx:3068-3082)."""
-        if s == 1:
-            return ()
+    def _fshape(self, fcn, kind, x1, j1=None):
+        """Shape of one integrand value, from an evaluation at one point (the
+        reference takes it from a sample evaluation, pyx:3068-3082)."""
         if kind == 'lbatch':
-            out = fcn(x1)
-        elif kind == 'rbatch':
-            out = fcn(x1.t())
-        else:
-            return (s,)
-        shp = tuple(torch.as_tensor(out).shape)
-        return shp[1:] if kind == 'lbatch' else shp[:-1]
+            out = fcn(x1) if j1 is None else fcn(x1, jac=j1)
+            return tuple(torch.as_tensor(out).shape)[1:]
+        if kind == 'rbatch':
+            out = fcn(x1.t()) if j1 is None else fcn(x1.t(), jac=j1.t())
+            return tuple(torch.as_tensor(out).shape)[:-1]
+        xc = x1[0].cpu().numpy()
+        out = fcn(xc) if j1 is None else fcn(xc, jac=j1[0].cpu().numpy())
+        return tuple(np.shape(out))
 
     def _reduce_array(self, it, f, fdt, w):
         """Mean and (co)variance of every component of an array integrand."""
@@ -455,6 +470,8 @@ class Integrator(object):
             self._itn += 1
             itn_word = self._itn & 0xffffffff
             u = None
+            if kind == 'builtin' and self.uses_jac:
+                raise ValueError('uses_jac=True needs an integrand that accepts jac=')
             if kind == 'builtin' and self.ran_array_generator is None:
                 p = fcn.params(self.dim)
                 N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, None, int(fcn.kind),
@@ -469,22 +486,26 @@ class Integrator(object):
                     N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, N.ptr(u),
                                                  int(fcn.kind), N.dbl_array(p), len(p), stream))
                 else:
-                    x, _, w, _ = self._points(it, ncap, itn_word, u)
+                    x, yv, w, _ = self._points(it, ncap, itn_word, u, want_y=self.uses_jac)
+                    jac = self.map.jac1d(yv[:n]) if self.uses_jac else None
                     f = None
                     nb = max(1, int(self.min_neval_batch))
                     for lo in range(0, n, nb):
                         hi = min(n, lo + nb)
-                        fb = self._eval_batch(fcn, kind, x[lo:hi])
+                        fb = self._eval_batch(fcn, kind, x[lo:hi],
+                                              None if jac is None else jac[lo:hi])
                         if fb.shape[0] != hi - lo:
                             raise ValueError('integrand returned %d values for %d points'
                                              % (fb.shape[0], hi - lo))
                         if f is None:
-                            s_f = 1 if fb.dim() == 1 else int(fb.shape[1])
                             if fshape is None:
-                                fshape = self._fshape(fcn, kind, x[:1], s_f)
-                            f = torch.empty((ncap, s_f) if s_f > 1 else ncap, dtype=dt,
+                                fshape = self._fshape(fcn, kind, x[:1],
+                                                      None if jac is None else jac[:1])
+                            s_f = int(np.prod(fshape)) if fshape else 1
+                            f = torch.empty((ncap, s_f) if fshape else ncap, dtype=dt,
                                             device=self.device)
-                        f[lo:hi] = fb.to(dt) if f.dim() == 1 else fb.reshape(hi - lo, -1).to(dt)
+                        f[lo:hi] = fb.reshape(hi - lo).to(dt) if f.dim() == 1 \
+                            else fb.reshape(hi - lo, -1).to(dt)
                     if bool(torch.isnan(f[:n]).any()):
                         raise ValueError('integrand evaluates to nan')
                     fdt = N.VG_F64 if dt == torch.float64 else N.VG_F32
