@@ -126,3 +126,43 @@ def test_uses_jac_like_reference():
     def fl2(x, jac):
         return (1. / torch.prod(jac, dim=-1))[:, None, None]
     check(fl2, array=True)
+
+
+def test_dict_integrands_and_uses_jac():
+    """Dictionary-valued integrands give an RAvgDict keyed like the integrand
+    (reference RAvgDict, pyx:2453); uses_jac dict variants of the reference's
+    test_uses_jac."""
+    import numpy as np
+    integ = vg.Integrator(2 * [[0, 2.]], precision='fp64', seed=4)
+    r = integ(lambda x, jac: dict(a=1. / np.prod(jac)), nitn=1, neval=10, uses_jac=True)
+    assert isinstance(r, vg.RAvgDict) and abs(r['a'].mean - 1.0) < 1e-10
+
+    @vg.rbatchintegrand
+    def fr(x, jac):
+        return dict(a=1. / torch.prod(jac, dim=0))
+    r = integ(fr, nitn=1, neval=10, uses_jac=True)
+    assert abs(r['a'].mean - 1.0) < 1e-10
+
+    @vg.lbatchintegrand
+    def fl(x, jac):
+        return dict(a=1. / torch.prod(jac, dim=-1))
+    r = integ(fl, nitn=1, neval=10, uses_jac=True)
+    assert abs(r['a'].mean - 1.0) < 1e-10
+
+    # several keys, scalar and array valued, against exact values
+    @vg.lbatchintegrand
+    def fd(x):
+        g = torch.exp(-5.0 * ((x - 0.5) ** 2).sum(dim=1))
+        return dict(g=g, moments=torch.stack([x[:, 0] * g, x[:, 1] * g], dim=1))
+    I2 = vg.Integrator(2 * [[0, 1]], neval=20000, seed=6)
+    I2(fd, nitn=5)
+    r = I2(fd, nitn=6)
+    m = 400
+    t = (np.arange(m) + 0.5) / m
+    e1 = np.exp(-5.0 * (t - 0.5) ** 2) / m
+    g_ex = e1.sum() ** 2
+    mom_ex = (t * e1).sum() * e1.sum()
+    assert set(r.keys()) == {'g', 'moments'} and r['moments'].shape == (2,)
+    assert abs(r['g'].mean - g_ex) < 5 * r['g'].sdev
+    for k in range(2):
+        assert abs(r['moments'][k].mean - mom_ex) < 5 * r['moments'][k].sdev

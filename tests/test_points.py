@@ -1,7 +1,8 @@
 """Built-in integrands at given points (vg_eval_points, the FP32 evaluation the
 fused kernels share) against their FP64 torch formulas.  FP32 tolerance:
-1e-5 relative to the largest value of the batch (sums of up to 1000
-exponentials).  The ridge evaluates only the terms that can be nonzero in
+3e-5 relative to the largest value of the batch for the ridge (sums of up
+to 1000 exponentials; its FP32 decomposition |x - c 1|^2 = R + dim (m - c)^2
+loses a little more with the dimension), 2e-5 for the others.  The ridge evaluates only the terms that can be nonzero in
 FP32; points near and far from its diagonal check that nothing is lost."""
 import ctypes
 
@@ -42,7 +43,7 @@ def test_ridge_points_vs_fp64(dim):
     got = _eval_points(f, dim, x).double()
     ref = f(x.double())
     scale = float(ref.abs().max())
-    assert float((got - ref).abs().max()) <= 1e-5 * scale
+    assert float((got - ref).abs().max()) <= 3e-5 * scale
     # where the FP32 value is exactly zero (every term flushed), the FP64
     # value is below the FP32 range relative to the batch's scale
     zero = got == 0

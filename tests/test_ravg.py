@@ -64,3 +64,16 @@ def test_correlated_gvar_algebra():
     np.testing.assert_allclose(c, [[1.0, 0.5], [0.5, 2.0]])
     d = x[0] - x[0]
     assert d.sdev == 0.0
+
+
+def test_ravgdict_weighted_average():
+    from vegas_gb300 import RAvgDict
+    r = RAvgDict([('a', ()), ('b', (2,))])
+    r.add({'a': gvar(1.0, 0.1), 'b': [gvar(2.0, 0.2), gvar(3.0, 0.3)]})
+    r.add({'a': gvar(1.2, 0.1), 'b': [gvar(2.2, 0.2), gvar(3.3, 0.3)]})
+    assert abs(r['a'].mean - 1.1) < 1e-12
+    assert abs(r['a'].sdev - 0.1 / 2 ** 0.5) < 1e-12
+    assert r['b'].shape == (2,) and abs(r['b'][1].mean - 3.15) < 1e-12
+    assert r.nitn == 2 and r.dof == 3
+    assert abs(r.chi2 - (0.2 ** 2 / 0.02 + 0.2 ** 2 / 0.08 + 0.3 ** 2 / 0.18)) < 1e-9
+    assert r.converged(0.1, 0) and not r.converged(1e-6, 0)

@@ -10,12 +10,12 @@ from .integrands import (BatchIntegrand, Constant, Gaussian, GaussianMixture, La
                          LBatchIntegrand, LorentzianProduct, RBatchIntegrand, Ridge,
                          batchintegrand, lbatchintegrand, rbatchintegrand)
 from .integrator import Integrator, reporter, strata
-from .ravg import RAvg, RAvgArray
+from .ravg import RAvg, RAvgArray, RAvgDict
 from ._gvar import GVar, gvar
 
 __version__ = '0.1.0'
 
-__all__ = ['AdaptiveMap', 'Integrator', 'RAvg', 'RAvgArray', 'reporter', 'lbatchintegrand',
+__all__ = ['AdaptiveMap', 'Integrator', 'RAvg', 'RAvgArray', 'RAvgDict', 'reporter', 'lbatchintegrand',
            'batchintegrand', 'rbatchintegrand', 'LBatchIntegrand', 'BatchIntegrand',
            'RBatchIntegrand', 'Gaussian', 'Ridge', 'LorentzianProduct', 'GaussianMixture',
            'LatticeAction', 'Constant', 'GVar', 'gvar', 'strata']

@@ -29,7 +29,7 @@ from . import _native as N
 from . import _gvar as gv
 from .adaptive_map import AdaptiveMap, _device
 from .integrands import BuiltinIntegrand
-from .ravg import RAvg, RAvgArray
+from .ravg import RAvg, RAvgArray, RAvgDict
 
 HUGE = 10 ** (sys.float_info.max_10_exp - 50)  # _vegas.pyx:35
 
@@ -392,14 +392,19 @@ class Integrator(object):
             return 'rbatch'
         return 'scalar'
 
-    def _eval_batch(self, fcn, kind, x, jac=None):
+    def _eval_batch(self, fcn, kind, x, jac=None, layout=None):
         """fcn on a batch; with uses_jac, jac[n, dim] = dx/dy per direction is
         passed as ``jac=`` (transposed for rbatch, per point for scalar
         integrands), as in the reference (pyx:2127, 3309-3316)."""
+        n = x.shape[0]
         if kind == 'lbatch':
             f = fcn(x) if jac is None else fcn(x, jac=jac)
+            if layout is not None:
+                return self._flatten_dict(f, kind, n, layout)
         elif kind == 'rbatch':
             f = fcn(x.t()) if jac is None else fcn(x.t(), jac=jac.t())
+            if layout is not None:
+                return self._flatten_dict(f, kind, n, layout)
         else:
             xc = x.cpu().numpy()
             if jac is None:
@@ -407,6 +412,9 @@ class Integrator(object):
             else:
                 jc = jac.cpu().numpy()
                 f = [fcn(xi, jac=ji) for xi, ji in zip(xc, jc)]
+            if layout is not None:
+                f = [np.concatenate([np.asarray(fi[k], dtype=float).reshape(-1) for k, _ in layout])
+                     for fi in f]
             f = np.array([np.asarray(fi, dtype=float).reshape(-1) for fi in f], dtype=float)
             if f.ndim == 2 and f.shape[1] == 1:
                 f = f[:, 0]
@@ -425,16 +433,33 @@ class Integrator(object):
 
     def _fshape(self, fcn, kind, x1, j1=None):
         """Shape of one integrand value, from an evaluation at one point (the
-        reference takes it from a sample evaluation, pyx:3068-3082)."""
+        reference takes it from a sample evaluation, pyx:3068-3082): a tuple
+        for arrays, a list of (key, shape) for dictionary-valued integrands."""
         if kind == 'lbatch':
             out = fcn(x1) if j1 is None else fcn(x1, jac=j1)
+            if hasattr(out, 'keys'):
+                return [(k, tuple(torch.as_tensor(out[k]).shape)[1:]) for k in out]
             return tuple(torch.as_tensor(out).shape)[1:]
         if kind == 'rbatch':
             out = fcn(x1.t()) if j1 is None else fcn(x1.t(), jac=j1.t())
+            if hasattr(out, 'keys'):
+                return [(k, tuple(torch.as_tensor(out[k]).shape)[:-1]) for k in out]
             return tuple(torch.as_tensor(out).shape)[:-1]
         xc = x1[0].cpu().numpy()
         out = fcn(xc) if j1 is None else fcn(xc, jac=j1[0].cpu().numpy())
+        if hasattr(out, 'keys'):
+            return [(k, tuple(np.shape(out[k]))) for k in out]
         return tuple(np.shape(out))
+
+    def _flatten_dict(self, out, kind, n, layout):
+        """[n, s] tensor of a dictionary-valued batch in the layout's key order."""
+        parts = []
+        for k, _ in layout:
+            v = torch.as_tensor(out[k], device=self.device)
+            if kind == 'rbatch':
+                v = v.reshape(-1, n).t()
+            parts.append(v.reshape(n, -1).to(torch.float64))
+        return torch.cat(parts, dim=1)
 
     def _reduce_array(self, it, f, fdt, w):
         """Mean and (co)variance of every component of an array integrand."""
@@ -492,16 +517,20 @@ class Integrator(object):
                     nb = max(1, int(self.min_neval_batch))
                     for lo in range(0, n, nb):
                         hi = min(n, lo + nb)
+                        if fshape is None:
+                            fshape = self._fshape(fcn, kind, x[:1],
+                                                  None if jac is None else jac[:1])
+                        layout = fshape if isinstance(fshape, list) else None
                         fb = self._eval_batch(fcn, kind, x[lo:hi],
-                                              None if jac is None else jac[lo:hi])
+                                              None if jac is None else jac[lo:hi], layout)
                         if fb.shape[0] != hi - lo:
                             raise ValueError('integrand returned %d values for %d points'
                                              % (fb.shape[0], hi - lo))
                         if f is None:
-                            if fshape is None:
-                                fshape = self._fshape(fcn, kind, x[:1],
-                                                      None if jac is None else jac[:1])
-                            s_f = int(np.prod(fshape)) if fshape else 1
+                            if layout is not None:
+                                s_f = int(sum(int(np.prod(sh)) if sh else 1 for _, sh in layout))
+                            else:
+                                s_f = int(np.prod(fshape)) if fshape else 1
                             f = torch.empty((ncap, s_f) if fshape else ncap, dtype=dt,
                                             device=self.device)
                         f[lo:hi] = fb.reshape(hi - lo).to(dt) if f.dim() == 1 \
@@ -527,16 +556,22 @@ class Integrator(object):
             if self.beta > 0 and self.adapt and self.nhcube > 1:
                 self.sum_sigf = float(st.sum_sigf)
             if arr is not None:
-                # array-valued integrand: RAvgArray of the integrand's shape
+                # array- or dictionary-valued integrand: RAvgArray of the
+                # integrand's shape / RAvgDict of its keys
                 # (VegasIntegrand.format_result, pyx:3127-3147)
-                if not isinstance(result, RAvgArray):
-                    result = RAvgArray(fshape, weighted=self.adapt)
                 mean_a, var_a = arr
                 if self.correlate_integrals:
                     g = gv.gvar(mean_a, var_a)
                 else:
                     g = gv.gvar(mean_a, np.sqrt(np.clip(np.diag(var_a), 0.0, None)))
-                result.add(np.asarray(g, dtype=object).reshape(fshape))
+                if isinstance(fshape, list):
+                    if not isinstance(result, RAvgDict):
+                        result = RAvgDict(fshape, weighted=self.adapt)
+                    result.add(np.asarray(g, dtype=object).reshape(-1))
+                else:
+                    if not isinstance(result, RAvgArray):
+                        result = RAvgArray(fshape, weighted=self.adapt)
+                    result.add(np.asarray(g, dtype=object).reshape(fshape))
             else:
                 result.add(gv.gvar(st.mean, st.var ** 0.5))
             result.sum_neval += self.last_neval

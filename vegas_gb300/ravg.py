@@ -290,3 +290,88 @@ def _rebuild_ravgarray(shape, weighted, itn, sum_neval, rescale):
     for r in res:
         out.add(np.asarray(r).reshape(shape))
     return out
+
+
+class RAvgDict(dict):
+    """Running average of dictionary-valued estimates (pyx:2453-2545).
+
+    Keys map to GVars or arrays of GVars; the values share one flat
+    RAvgArray (``rarray``), so correlations between keys are kept.
+    ``layout`` is a list of (key, shape) in the integrand's key order.
+    """
+
+    def __init__(self, layout, weighted=True, sum_neval=0, rescale=True):
+        super(RAvgDict, self).__init__()
+        self.layout = [(k, tuple(s)) for k, s in layout]
+        self.size = int(sum(int(np.prod(s)) if s else 1 for _, s in self.layout))
+        self.rarray = RAvgArray((self.size,), weighted=weighted, rescale=rescale)
+        self.weighted = weighted
+        self.itn_results = []
+        self.sum_neval = sum_neval
+        self._fill()
+
+    def _slices(self):
+        o = 0
+        for k, s in self.layout:
+            n = int(np.prod(s)) if s else 1
+            yield k, s, slice(o, o + n)
+            o += n
+
+    def _fill(self):
+        flat = np.asarray(self.rarray, dtype=object).reshape(-1)
+        for k, s, sl in self._slices():
+            dict.__setitem__(self, k, flat[sl][0] if s == () else flat[sl].reshape(s))
+
+    def unflatten(self, flat):
+        """Dictionary of the flat vector's pieces in this layout."""
+        flat = np.asarray(flat, dtype=object).reshape(-1)
+        out = {}
+        for k, s, sl in self._slices():
+            out[k] = flat[sl][0] if s == () else flat[sl].reshape(s)
+        return out
+
+    def add(self, g):
+        """Add one iteration's estimates: a dict in this layout, or the flat vector."""
+        if isinstance(g, dict):
+            flat = np.concatenate([np.asarray(g[k], dtype=object).reshape(-1) for k, _ in self.layout])
+        else:
+            flat = np.asarray(g, dtype=object).reshape(-1)
+        self.itn_results.append(self.unflatten(flat))
+        self.rarray.add(flat)
+        self._fill()
+
+    def extend(self, ravg):
+        for r in ravg.itn_results:
+            self.add(r)
+        self.sum_neval += ravg.sum_neval
+
+    @property
+    def buf(self):
+        return np.asarray(self.rarray, dtype=object).reshape(-1)
+
+    @property
+    def chi2(self):
+        return self.rarray.chi2
+
+    @property
+    def dof(self):
+        return self.rarray.dof
+
+    @property
+    def Q(self):
+        return self.rarray.Q
+
+    @property
+    def nitn(self):
+        return len(self.itn_results)
+
+    @property
+    def avg_neval(self):
+        return self.sum_neval / self.nitn if self.nitn > 0 else 0
+
+    def converged(self, rtol, atol):
+        b = self.buf
+        return bool(np.all(gv.sdev(b) < atol + rtol * np.abs(gv.mean(b))))
+
+    def summary(self, extended=False, weighted=None, rescale=None):
+        return self.rarray.summary(extended=False, weighted=weighted, rescale=rescale)
