@@ -110,7 +110,7 @@ struct GridEntry<double> {
 };
 
 struct SmemPlan {
-    size_t table, hsum, hcnt, bins, win_off, win_n, seg_S, keyF, keyL, P, red, itab, total;
+    size_t table, hsum, hcnt, bins, win_off, win_n, win_w, seg_S, keyF, keyL, P, red, itab, total;
 };
 
 template <typename T>
@@ -130,6 +130,7 @@ __host__ __device__ inline SmemPlan smem_plan(int dim, int maxK, int Ttile, int 
     if (bins_smem) o = (o + sizeof(unsigned short) * (size_t)Ttile * dim + 15) & ~(size_t)15;
     p.win_off = o; o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
     p.win_n = o;   o = (o + sizeof(int) * (Ttile + 2) + 15) & ~(size_t)15;
+    p.win_w = o;   o = (o + sizeof(float) * (Ttile + 2) + 15) & ~(size_t)15;
     p.seg_S = o;   if (need_red) o = (o + sizeof(double) * (Ttile + 2) + 15) & ~(size_t)15;
     p.keyF = o;    if (need_red) o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
     p.keyL = o;    if (need_red) o = (o + sizeof(int) * NT + 15) & ~(size_t)15;
@@ -401,6 +402,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     unsigned short *sbins = (unsigned short *)(smem + sp.bins);
     int *win_off = (int *)(smem + sp.win_off);
     int *win_n = (int *)(smem + sp.win_n);
+    float *win_w = (float *)(smem + sp.win_w);   // FP32 mode: dv_y / neval_h of the window's hypercubes
     double *seg_S = (double *)(smem + sp.seg_S);
     int *keyF = (int *)(smem + sp.keyF);
     int *keyL = (int *)(smem + sp.keyL);
@@ -448,6 +450,12 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     const double dv_y = a.dv_y;
     const float dv_yf = (float)a.dv_y;
     const double beta_half = a.beta_half;
+    float Kf[DIMB], rstrat[DIMB];   // FP32 mode: per-axis constants
+#pragma unroll
+    for (int d = 0; d < DIMB; d++) {
+        Kf[d] = d < dim ? (float)a.ninc[d] : 1.f;
+        rstrat[d] = d < dim ? 1.f / (float)a.nstrat[d] : 1.f;
+    }
     int nan_local = 0;
     // per-thread running sums over every hypercube this thread finalises
     double acc_m = 0.0, acc_v = 0.0, acc_s = 0.0;
@@ -485,7 +493,10 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             int64_t o = (h <= a.H) ? a.offsets[h] : N;
             int64_t r = o - tile_start;
             win_off[k] = (int)(r < 0 ? 0 : (r > tile_len ? tile_len : r));
-            if (k < nwin) win_n[k] = a.neval_h[h];
+            if (k < nwin) {
+                win_n[k] = a.neval_h[h];
+                if (sizeof(T) == 4) win_w[k] = dv_yf / (float)win_n[k];
+            }
         }
         __syncthreads();
 
@@ -504,7 +515,20 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             lh = lo;
         }
         int y0[DIMB];
-        {
+        float y0f[DIMB];   // FP32 mode: the stratum coordinates as floats (no per-sample conversion)
+        if (a.H <= 0x7fffffff) {   // 32-bit mixed-radix decode
+            int hh = (int)(h0 + lh);
+#pragma unroll
+            for (int d = 0; d < DIMB; d++) {
+                if (d < dim) {
+                    const int q = hh / a.nstrat[d];
+                    y0[d] = hh - q * a.nstrat[d];
+                    hh = q;
+                } else {
+                    y0[d] = 0;
+                }
+            }
+        } else {
             int64_t hh = h0 + lh;
 #pragma unroll
             for (int d = 0; d < DIMB; d++) {
@@ -517,8 +541,11 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 }
             }
         }
+#pragma unroll
+        for (int d = 0; d < DIMB; d++) y0f[d] = (float)y0[d];
         T xs[S][DIMB];
         T wg[S];   // sampler weight (FP32 in the FP32 mode)
+        float jn[S];   // FP32 mode: wgt * neval_h = jac * dv_y
         int lhs[S];
         int cur = lh;
 #pragma unroll
@@ -535,8 +562,13 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
 #pragma unroll
                     for (int d = 0; d < DIMB; d++) {
                         if (d < dim && carry) {
-                            if (++y0[d] < a.nstrat[d]) carry = 0;
-                            else y0[d] = 0;
+                            if (++y0[d] < a.nstrat[d]) {
+                                carry = 0;
+                                y0f[d] += 1.f;
+                            } else {
+                                y0[d] = 0;
+                                y0f[d] = 0.f;
+                            }
                         }
                     }
                 }
@@ -557,17 +589,24 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 for (int d = 0; d < DIMB; d++) {
                     if (d >= dim) continue;
                     const int K = a.ninc[d];
-                    T yd;
-                    if (sizeof(T) == 8)
+                    T yd, yn, dy;
+                    int iy;
+                    if (sizeof(T) == 8) {
                         yd = (T)__ddiv_rn(__dadd_rn((double)y0[d], (double)u[d]), (double)a.nstrat[d]);
-                    else
-                        yd = (T)__fdiv_rn((float)y0[d] + (float)u[d], (float)a.nstrat[d]);
+                        yn = (T)__dmul_rn((double)yd, (double)K);
+                        iy = (int)floor((double)yn);
+                        dy = yn - (T)iy;
+                    } else {
+                        // no int <-> float conversions per sample (they share the
+                        // slow FP64 pipe on GB300): reciprocal of nstrat, float K,
+                        // the floor's integer from the float's bits (0 <= yn < 2^23)
+                        yd = (T)((y0f[d] + (float)u[d]) * rstrat[d]);
+                        yn = (T)((float)yd * Kf[d]);
+                        const float fl = floorf((float)yn);
+                        iy = __float_as_int(fl + 8388608.f) - 0x4B000000;
+                        dy = (T)((float)yn - fl);
+                    }
                     yv[d] = yd;
-                    T yn;
-                    if (sizeof(T) == 8) yn = (T)__dmul_rn((double)yd, (double)K);
-                    else yn = (T)((float)yd * (float)K);
-                    int iy = (sizeof(T) == 8) ? (int)floor((double)yn) : (int)floorf((float)yn);
-                    T dy = yn - (T)iy;
                     const int clamp = iy >= K;
                     const int ie = clamp ? K : iy;
                     GE e;
@@ -586,7 +625,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                         jac = (T)__dmul_rn((double)jac, __dmul_rn((double)e.y, (double)K));
                     } else {
                         xs[k][d] = clamp ? e.x : (T)fmaf((float)e.y, (float)dy, (float)e.x);
-                        jac = (T)((float)jac * ((float)e.y * (float)K));
+                        jac = (T)((float)jac * ((float)e.y * Kf[d]));
                     }
                     if (use_bins)
                         sbins[(li0 + k) * dim + d] =
@@ -594,7 +633,10 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 }
                 // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
                 if (sizeof(T) == 8) wg[k] = (T)__dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
-                else wg[k] = (T)((float)jac * (dv_yf / (float)nh));
+                else {
+                    wg[k] = (T)((float)jac * win_w[cur]);
+                    jn[k] = (float)jac * dv_yf;   // wgt * neval_h, for fdv2
+                }
                 if (MODE == MODE_POINTS) {
                     T *xo = (T *)a.x_out;
 #pragma unroll
@@ -655,7 +697,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     const double t1 = __dmul_rn(w1, (double)win_n[lhs[k]]);
                     fd = (T)__dmul_rn(t1, t1);
                 } else {
-                    const float t1 = wf32 * (float)win_n[lhs[k]];
+                    const float t1 = (float)fv[k] * jn[k];
                     fd = (T)(t1 * t1);
                 }
                 for (int d = 0; d < dim; d++) {
