@@ -350,6 +350,12 @@ int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm,
  * nonzero in FP32; the rest are exactly zero and skipped. */
 int vg_set_term_counter(unsigned long long *count);
 
+/* Tuning: how FP32 iterations of the many-term ridge run -- 0 automatic
+ * (currently the fused kernel), 1 the single fused evaluate+reduce kernel,
+ * 2 split into an evaluation kernel that writes f and a reduction kernel
+ * that reads it back. */
+int vg_set_eval_split(int policy);
+
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);

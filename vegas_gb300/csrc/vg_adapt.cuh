@@ -22,6 +22,7 @@ struct AdaptArgs {
     int max_old;      // length of the shared avg_f buffer (pyx:533)
     int sequential;   // one block walks all axes, carrying avg_f (pyx:533 semantics)
     int fast;         // FP32 mode: MUFU transcendentals and reciprocal multiplies
+    int zero_hist;    // clear sum_f / n_f once read (the end of an iteration)
 };
 
 // ((1 - v) / -ln v)^alpha of the damping step (pyx:560-562), FP32-mode path:
@@ -45,55 +46,80 @@ __device__ __forceinline__ double div_fast(double a, double b)
 }
 
 // Block-wide inclusive prefix sum of v[0..n) in place (FP64, fixed order):
-// per-thread sequential over a contiguous chunk, then a scan of chunk totals.
+// per-thread sequential over a contiguous chunk, then a scan of the chunk
+// totals by warp shuffles (within each warp, then over the warp totals) --
+// few FP64 instructions per thread (GB300 issues FP64 at a low rate).
 template <int ADAPT_NT>
-__device__ void block_inclusive_scan(double *v, int n, double *part /* ADAPT_NT */)
+__device__ void block_inclusive_scan(double *v, int n, double *part /* >= 32 */)
 {
-    int t = threadIdx.x;
-    int per = (n + ADAPT_NT - 1) / ADAPT_NT;
-    int b = t * per, e = min(n, b + per);
+    constexpr int NW = ADAPT_NT / 32;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = (n + ADAPT_NT - 1) / ADAPT_NT;
+    const int b = t * per, e = min(n, b + per);
     double s = 0.0;
     for (int i = b; i < e; i++) {
         s = __dadd_rn(s, v[i]);
         v[i] = s;
     }
-    part[t] = s;
-    __syncthreads();
-    // Hillis-Steele on the ADAPT_NT chunk totals
-    for (int off = 1; off < ADAPT_NT; off <<= 1) {
-        double add = (t >= off) ? part[t - off] : 0.0;
-        __syncthreads();
-        part[t] = __dadd_rn(part[t], add);
-        __syncthreads();
+    double x = s;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x = __dadd_rn(x, y);
     }
-    double carry = (t > 0) ? part[t - 1] : 0.0;
-    if (t > 0)
+    if (lane == 31) part[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        double z = lane < NW ? part[lane] : 0.0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, z, off);
+            if (lane >= off) z = __dadd_rn(z, y);
+        }
+        if (lane < NW) part[lane] = z;
+    }
+    __syncthreads();
+    double ex = __shfl_up_sync(0xffffffffu, x, 1);   // exclusive prefix within the warp
+    if (lane == 0) ex = 0.0;
+    if (t > 0) {
+        const double carry = (w > 0) ? __dadd_rn(part[w - 1], ex) : ex;
         for (int i = b; i < e; i++) v[i] = __dadd_rn(v[i], carry);
+    }
     __syncthreads();
 }
 
 // Sum of v[0..n) in a fixed order; result broadcast to all threads.
 template <int ADAPT_NT>
-__device__ double block_sum(const double *v, int n, double *part)
+__device__ double block_sum(const double *v, int n, double *part /* >= 33 */)
 {
-    int t = threadIdx.x;
+    constexpr int NW = ADAPT_NT / 32;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     double s = 0.0;
     for (int i = t; i < n; i += ADAPT_NT) s = __dadd_rn(s, v[i]);
-    part[t] = s;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, off));
+    if (lane == 0) part[w] = s;
     __syncthreads();
-    for (int off = ADAPT_NT / 2; off > 0; off >>= 1) {
-        if (t < off) part[t] = __dadd_rn(part[t], part[t + off]);
-        __syncthreads();
+    if (w == 0) {
+        double z = lane < NW ? part[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) z = __dadd_rn(z, __shfl_xor_sync(0xffffffffu, z, off));
+        if (lane == 0) part[32] = z;
     }
-    double r = part[0];
+    __syncthreads();
+    const double r = part[32];
     __syncthreads();
     return r;
 }
 
 // One axis of AdaptiveMap.adapt.  avg (length >= max_old) holds the carried
-// avg_f values on entry, the final ones on exit.
+// avg_f values on entry, the final ones on exit.  With gs / is (shared
+// memory, max_old + 1 and max_old doubles) the axis' old nodes and
+// increments are staged there first, so new_grid / new_inc may be the grid
+// itself (adapt in place).
 template <int ADAPT_NT>
-__device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, double *part)
+__device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, double *part,
+                           double *gs = nullptr, double *is = nullptr)
 {
     const int K = a.old_ninc[d];
     const int Kn = a.new_ninc[d];
@@ -103,9 +129,16 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
         if (a.sum_f != nullptr) {
             for (int i = t; i < K; i += ADAPT_NT) {
                 const unsigned long long c = a.n_f[d * a.ldi + i];
-                const double nf = __dadd_rn((double)c, VG_TINY);
-                if (a.fast) avg[i] = c ? div_fast(a.sum_f[d * a.ldi + i], (double)c) : 0.0;
-                else avg[i] = (nf > 0) ? __ddiv_rn(a.sum_f[d * a.ldi + i], nf) : 0.0;
+                if (a.fast) {
+                    avg[i] = c ? div_fast(a.sum_f[d * a.ldi + i], (double)c) : 0.0;
+                } else {
+                    const double nf = __dadd_rn((double)c, VG_TINY);
+                    avg[i] = (nf > 0) ? __ddiv_rn(a.sum_f[d * a.ldi + i], nf) : 0.0;
+                }
+                if (a.zero_hist) {
+                    const_cast<double *>(a.sum_f)[d * a.ldi + i] = 0.0;
+                    const_cast<unsigned long long *>(a.n_f)[d * a.ldi + i] = 0ull;
+                }
             }
             __syncthreads();
         }
@@ -116,7 +149,7 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
                 if (i == 0) v = __dadd_rn(__dmul_rn(7., avg[0]), avg[1]);
                 else if (i == K - 1) v = __dadd_rn(__dmul_rn(7., avg[K - 1]), avg[K - 2]);
                 else v = __dadd_rn(__dadd_rn(__dmul_rn(6., avg[i]), avg[i - 1]), avg[i + 1]);
-                tmp[i] = __ddiv_rn(fabs(v), 8.);
+                tmp[i] = __dmul_rn(fabs(v), 0.125);   // == v / 8 exactly
             }
             __syncthreads();
             double s = block_sum<ADAPT_NT>(tmp, K, part);
@@ -139,29 +172,44 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
     // regrid, pyx:563-587: new node i sits where the running sum of avg_f
     // reaches i*f_ninc; found by a block scan + binary search per node.
     double *P = tmp;
-    for (int i = t; i < K; i += ADAPT_NT) P[i] = avg[i];
-    __syncthreads();
-    block_inclusive_scan<ADAPT_NT>(P, K, part);
-    double total = P[K - 1];
-    double f_ninc = __ddiv_rn(total, (double)Kn);
     const double *gd = a.grid + d * a.ldg;
     const double *id = a.inc + d * a.ldi;
+    for (int i = t; i < K; i += ADAPT_NT) {
+        P[i] = avg[i];
+        if (gs != nullptr) {
+            gs[i] = gd[i];
+            is[i] = id[i];
+        }
+    }
+    if (gs != nullptr && t == 0) gs[K] = gd[K];
+    __syncthreads();
+    if (gs != nullptr) {
+        gd = gs;
+        id = is;
+    }
+    block_inclusive_scan<ADAPT_NT>(P, K, part);
+    const double total = P[K - 1];
+    const double f_ninc = a.fast ? div_fast(total, (double)Kn) : __ddiv_rn(total, (double)Kn);
     double *ng = a.new_grid + d * a.ldg_new;
     for (int i = t; i <= Kn; i += ADAPT_NT) {
         double v;
         if (i == 0) v = gd[0];
         else if (i == Kn) v = gd[K];
         else {
-            double target = __dmul_rn((double)i, f_ninc);
-            int lo = 0, hi = K - 1;   // first j with P[j] >= target
+            const double target = __dmul_rn((double)i, f_ninc);
+            // first j with P[j] >= target; P and target are >= 0, so their
+            // IEEE bit patterns order like the values (integer compares)
+            const long long tb = __double_as_longlong(target);
+            int lo = 0, hi = K - 1;
             while (lo < hi) {
                 int mid = (lo + hi) >> 1;
-                if (P[mid] < target) lo = mid + 1;
+                if (__double_as_longlong(P[mid]) < tb) lo = mid + 1;
                 else hi = mid;
             }
             int j = lo;
             double acc = __dsub_rn(P[j], target);
-            v = __dsub_rn(gd[j + 1], __dmul_rn(__ddiv_rn(acc, avg[j]), id[j]));
+            const double q = a.fast ? div_fast(acc, avg[j]) : __ddiv_rn(acc, avg[j]);
+            v = __dsub_rn(gd[j + 1], __dmul_rn(q, id[j]));
         }
         ng[i] = v;
     }

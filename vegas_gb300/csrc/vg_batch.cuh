@@ -63,6 +63,7 @@ constexpr int APER = 4;          // hypercubes per thread and pass of the alloca
 static __device__ __noinline__ void cta_alloc(const IterArgs &a, int64_t *scan)
 {
     const int tid = threadIdx.x;
+    build_tablef(a, tid, NT);   // the FP32 grid table of this iteration
     vg_stats *st = a.stats;
     const double sum_sigf = st->sum_sigf;
     const double nsf = (a.beta > 0 && sum_sigf > 0)

@@ -6,15 +6,19 @@
 
 namespace vg {
 
-// Expensive integrands (many exponentials per evaluation) run split: an EVAL
-// kernel without the reduction's shared memory and barriers (higher
-// occupancy for the latency-bound SFU loop) writes f, a REDUCE kernel reads
-// it back.  Cheap integrands run in the single fused kernel.
+// One fused kernel by default.  The split form -- an EVAL kernel without the
+// reduction's shared memory and barriers (higher occupancy for an SFU-bound
+// loop) writing f, a REDUCE kernel reading it back -- stays selectable for
+// the ridge (vg_set_eval_split): it paid while the ridge evaluated all of its
+// terms; with the FP32 term window the fused kernel is faster.
+extern int g_eval_split;   // 0 automatic, 1 fused, 2 split (vg_set_eval_split)
+
 template <int KIND>
 int launch_fused_kind(IterArgs &a, const VgParams &P, int tab_len, int f64, cudaStream_t st)
 {
-    if (!f64 && KIND == VG_F_RIDGE) {
+    if (!f64 && KIND == VG_F_RIDGE && g_eval_split == 2) {
         int rc;
+        VG_CUDA_CHECK(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st));   // dynamic tiles
         if (a.dim <= 4) rc = launch_tile<float, MODE_EVAL, KIND, 4, 2>(a, &P, tab_len, st);
         else if (a.dim <= 8) rc = launch_tile<float, MODE_EVAL, KIND, 8, 2>(a, &P, tab_len, st);
         else if (a.dim <= 16) rc = launch_tile<float, MODE_EVAL, KIND, 16, 2>(a, &P, tab_len, st);

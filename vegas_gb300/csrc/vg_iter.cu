@@ -31,21 +31,82 @@ namespace {
 using namespace vg;
 
 // ======================================================== allocation
-// pyx:1692-1706 for hypercubes of this thread; block totals for the scan.
-__global__ void __launch_bounds__(ALLOC_NT) alloc_count_kernel(IterArgs a)
+// Block-wide exclusive prefix sum of one int64 per thread (warp shuffles,
+// then a scan of the warp totals); *total = the block's sum.
+template <int NTB>
+__device__ __forceinline__ int64_t block_excl_scan(int64_t v, int64_t *wtot /* NTB/32 */, int64_t *total)
 {
-    __shared__ int64_t ssum[ALLOC_NT / 32], smax[ALLOC_NT / 32];
-    const vg_stats *st = a.stats;
-    double sum_sigf = st->sum_sigf;
-    double nsf = (a.beta > 0 && sum_sigf > 0)
-                     ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
-                     : 0.0;
-    int64_t mx = a.max_neval_hcube > a.min_neval_hcube ? a.max_neval_hcube : a.min_neval_hcube;
-    int64_t avg = (int64_t)((double)a.neval / (double)a.H);
-    int64_t h0 = ((int64_t)blockIdx.x * ALLOC_NT + threadIdx.x) * ALLOC_PER;
+    constexpr int NW = NTB / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) wtot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int64_t z = lane < NW ? wtot[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, z, off);
+            if (lane >= off) z += y;
+        }
+        if (lane < NW) wtot[lane] = z;
+    }
+    __syncthreads();
+    *total = wtot[NW - 1];
+    const int64_t r = (w > 0 ? wtot[w - 1] : 0) + x - v;
+    __syncthreads();
+    return r;
+}
+
+template <int NTB>
+__device__ __forceinline__ int64_t block_max(int64_t v, int64_t *wtot /* NTB/32 */)
+{
+    constexpr int NW = NTB / 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const int64_t o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = o > v ? o : v;
+    }
+    if (lane == 0) wtot[w] = v;
+    __syncthreads();
+    int64_t m = wtot[0];
+    for (int i = 1; i < NW; i++) m = wtot[i] > m ? wtot[i] : m;
+    __syncthreads();
+    return m;
+}
+
+// pyx:1692-1706 for the block's ALLOC_NT * ALLOC_PER hypercubes (coalesced);
+// block totals for the scan.  The per-iteration constants are formed once
+// per block (FP64 divisions are slow on GB300).  With build_table the grid
+// also builds the FP32 grid table of the iteration.
+__global__ void __launch_bounds__(ALLOC_NT) alloc_count_kernel(IterArgs a, int build_table)
+{
+    __shared__ int64_t ssum[ALLOC_NT / 32];
+    __shared__ double s_nsf;
+    __shared__ int64_t s_avg;
+    if (threadIdx.x == 0) {
+        const double sum_sigf = a.stats->sum_sigf;
+        s_nsf = (a.beta > 0 && sum_sigf > 0) ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
+                                             : 0.0;
+        s_avg = (int64_t)((double)a.neval / (double)a.H);
+        if (blockIdx.x == 0) a.stats->neval_sigf = s_nsf;
+    }
+    if (build_table)
+        build_tablef(a, (int64_t)blockIdx.x * ALLOC_NT + threadIdx.x, (int64_t)gridDim.x * ALLOC_NT);
+    __syncthreads();
+    const double nsf = s_nsf;
+    const int64_t avg = s_avg;
+    const int64_t mx = a.max_neval_hcube > a.min_neval_hcube ? a.max_neval_hcube : a.min_neval_hcube;
+    const int64_t hb = (int64_t)blockIdx.x * ALLOC_NT * ALLOC_PER + threadIdx.x;
     int64_t s = 0, m = 0;
+#pragma unroll
     for (int k = 0; k < ALLOC_PER; k++) {
-        int64_t h = h0 + k;
+        const int64_t h = hb + k * ALLOC_NT;
         if (h >= a.H) break;
         int64_t n;
         if (a.adaptive_alloc) {
@@ -58,65 +119,36 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_count_kernel(IterArgs a)
         s += n;
         m = n > m ? n : m;
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        s += __shfl_down_sync(0xffffffffu, s, off);
-        int64_t o = __shfl_down_sync(0xffffffffu, m, off);
-        m = o > m ? o : m;
+    int64_t tot;
+    block_excl_scan<ALLOC_NT>(s, ssum, &tot);
+    const int64_t bm = block_max<ALLOC_NT>(m, ssum);
+    if (threadIdx.x == 0) {
+        a.bsum[blockIdx.x] = tot;
+        a.bmax[blockIdx.x] = bm;
     }
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { ssum[w] = s; smax[w] = m; }
-    __syncthreads();
-    if (w == 0) {
-        s = ssum[lane];
-        m = smax[lane];
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            s += __shfl_down_sync(0xffffffffu, s, off);
-            int64_t o = __shfl_down_sync(0xffffffffu, m, off);
-            m = o > m ? o : m;
-        }
-        if (lane == 0) {
-            a.bsum[blockIdx.x] = s;
-            a.bmax[blockIdx.x] = m;
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->neval_sigf = nsf;
 }
 
 // Exclusive scan of block totals (one CTA), totals, range, tile count.
-__global__ void __launch_bounds__(ALLOC_NT) alloc_scan_kernel(IterArgs a, int64_t nblk)
+__global__ void __launch_bounds__(SCAN_NT) alloc_scan_kernel(IterArgs a, int64_t nblk)
 {
-    __shared__ int64_t part[ALLOC_NT];
-    __shared__ int64_t pmax[ALLOC_NT];
-    int t = threadIdx.x;
-    int64_t per = (nblk + ALLOC_NT - 1) / ALLOC_NT;
-    int64_t b = t * per, e = b + per < nblk ? b + per : nblk;
+    __shared__ int64_t wtot[SCAN_NT / 32];
+    const int t = threadIdx.x;
+    const int64_t per = (nblk + SCAN_NT - 1) / SCAN_NT;
+    const int64_t b = t * per, e = b + per < nblk ? b + per : nblk;
     int64_t s = 0, m = 0;
     for (int64_t i = b; i < e; i++) {
         s += a.bsum[i];
         m = a.bmax[i] > m ? a.bmax[i] : m;
     }
-    part[t] = s;
-    pmax[t] = m;
-    __syncthreads();
-    for (int off = 1; off < ALLOC_NT; off <<= 1) {
-        int64_t add = t >= off ? part[t - off] : 0;
-        int64_t mm = t >= off ? pmax[t - off] : 0;
-        __syncthreads();
-        part[t] += add;
-        pmax[t] = mm > pmax[t] ? mm : pmax[t];
-        __syncthreads();
-    }
-    int64_t run = t > 0 ? part[t - 1] : 0;
+    int64_t N;
+    int64_t run = block_excl_scan<SCAN_NT>(s, wtot, &N);
+    const int64_t mx = block_max<SCAN_NT>(m, wtot);
     for (int64_t i = b; i < e; i++) {
-        int64_t v = a.bsum[i];
+        const int64_t v = a.bsum[i];
         a.bsum[i] = run;   // becomes the block offset
         run += v;
     }
-    if (t == ALLOC_NT - 1) {
-        int64_t N = part[ALLOC_NT - 1];
-        int64_t mx = pmax[ALLOC_NT - 1];
+    if (t == 0) {
         vg_stats *st = a.stats;
         st->neval = N;
         // neval_hcube_range starts at [mnh, mnh] and every count is >= mnh
@@ -134,42 +166,45 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_scan_kernel(IterArgs a, int64_
         st->ntiles = ntiles;
         st->nan_seen = 0;
         *a.counter = 0ull;
+        *a.fin_counter = 0u;
     }
 }
 
-// Offsets (exclusive scan within the block + block offset) and tile heads.
+// Offsets (exclusive scan within the block + block offset) and tile heads;
+// each thread owns ALLOC_PER consecutive hypercubes.
 __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
 {
-    __shared__ int64_t part[ALLOC_NT];
-    int t = threadIdx.x;
-    int64_t h0 = ((int64_t)blockIdx.x * ALLOC_NT + t) * ALLOC_PER;
+    __shared__ int64_t wtot[ALLOC_NT / 32];
+    const int t = threadIdx.x;
+    const int64_t h0 = ((int64_t)blockIdx.x * ALLOC_NT + t) * ALLOC_PER;
     int64_t loc[ALLOC_PER];
     int64_t s = 0;
-    for (int k = 0; k < ALLOC_PER; k++) {
-        int64_t h = h0 + k;
-        loc[k] = (h < a.H) ? (int64_t)a.neval_h[h] : 0;
-        s += loc[k];
+    if (h0 + ALLOC_PER <= a.H) {   // 16-byte aligned: h0 is a multiple of 4
+        const int4 q = *reinterpret_cast<const int4 *>(a.neval_h + h0);
+        loc[0] = q.x;
+        loc[1] = q.y;
+        loc[2] = q.z;
+        loc[3] = q.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < ALLOC_PER; k++) loc[k] = (h0 + k < a.H) ? (int64_t)a.neval_h[h0 + k] : 0;
     }
-    part[t] = s;
-    __syncthreads();
-    for (int off = 1; off < ALLOC_NT; off <<= 1) {
-        int64_t add = t >= off ? part[t - off] : 0;
-        __syncthreads();
-        part[t] += add;
-        __syncthreads();
-    }
-    int64_t run = a.bsum[blockIdx.x] + (t > 0 ? part[t - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < ALLOC_PER; k++) s += loc[k];
+    int64_t tot;
+    int64_t run = a.bsum[blockIdx.x] + block_excl_scan<ALLOC_NT>(s, wtot, &tot);
     const vg_stats *st = a.stats;
-    int64_t N = st->neval;
-    int64_t ntiles = st->ntiles;
+    const int64_t N = st->neval;
+    const int64_t ntiles = st->ntiles;
+#pragma unroll
     for (int k = 0; k < ALLOC_PER; k++) {
-        int64_t h = h0 + k;
+        const int64_t h = h0 + k;
         if (h >= a.H) break;
         a.offsets[h] = run;
         // tiles whose first sample falls in [run, run + n)
-        int64_t n = loc[k];
-        int64_t tfirst = (run + BASE_TILE - 1) / BASE_TILE;
-        for (int64_t tt = tfirst; tt * BASE_TILE < run + n && tt < ntiles; tt++) a.tile_h0[tt] = h;
+        const int64_t n = loc[k];
+        for (int64_t tt = (run + BASE_TILE - 1) / BASE_TILE; tt * BASE_TILE < run + n && tt < ntiles; tt++)
+            a.tile_h0[tt] = h;
         run += n;
         if (h == a.H - 1) {
             a.offsets[a.H] = N;
@@ -178,6 +213,12 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
     }
 }
 
+
+// FP32 mode: the grid as an FP32 (x_node, inc) table for the tile CTAs.
+__global__ void tablef_kernel(IterArgs a)
+{
+    build_tablef(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
 
 // ========================================================== finalize
 // Stage 1 (one thread per tile, FIN_TILES tiles per block): the tile's
@@ -188,89 +229,25 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
 // sum_sigf (compensated FP64), and the constant-integrand reset.
 constexpr int FIN_TILES = 32;   // one warp per finalize block: few FP64 lanes per value
 
-template <int FAST>
-__global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
+// Stage 2 body (one block): the stage-1 partials in block order -> the
+// iteration's mean, var, sum_sigf and the constant-integrand reset.
+__device__ __forceinline__ void finalize_totals(const IterArgs &a, int64_t nblk, VgKSum *red, int *reset)
 {
-    __shared__ VgKSum red[1];
-    const vg_stats *st = a.stats;
-    const int64_t N = st->neval;
-    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
-    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
-    if ((int64_t)blockIdx.x >= nblk) return;
-    const double beta_half = a.beta_half;
     VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
-    const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
-    if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
-        const TilePart p = a.parts[t];
-        cm = p.mean;
-        cv = p.var;
-        cs = p.sigf;
-    }
-    if (t < ntiles) {   // a hypercube starting in tile t and cut by its end
-        const TileRec r = a.recs[2 * t + 1];
-        if (r.h >= 0) {
-            double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
-            for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
-                const TileRec q = a.recs[2 * t2];
-                if (q.h != r.h) break;
-                const double n2 = n + q.n;
-                const double delta = q.S / q.n - Sx / n;
-                Q = Q + q.Q + delta * delta * (n * q.n / n2);
-                Sx += q.S;
-                D += q.D;
-                n = n2;
-                if (!q.spans) break;
-            }
-            const double vh =
-                __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
-            cm.add(__dadd_rn(Sx, D));
-            cv.add(vh);
-            if (a.adaptive) {
-                const double sg = FAST ? vg_pow_fast(fabs(vh), beta_half) : pow(fabs(vh), beta_half);
-                a.sigf[r.h] = sg;
-                cs.add(sg);
-            }
-        }
-    }
-    const VgKSum M = vg_block_ksum<FIN_TILES>(cm, red);
-    const VgKSum V = vg_block_ksum<FIN_TILES>(cv, red);
-    const VgKSum Sg = vg_block_ksum<FIN_TILES>(cs, red);
-    if (threadIdx.x == 0) {
-        TilePart p;
-        p.mean = M;
-        p.var = V;
-        p.sigf = Sg;
-        a.part2[blockIdx.x] = p;
-    }
-}
-
-constexpr int FIN2_NT = 32;
-
-__global__ void __launch_bounds__(FIN2_NT) finalize2_kernel(IterArgs a)
-{
-    __shared__ VgKSum red[1];
-    __shared__ int reset;
-    const vg_stats *st = a.stats;
-    const int64_t N = st->neval;
-    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
-    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
-    VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
-    for (int64_t b = threadIdx.x; b < nblk; b += FIN2_NT) {
+    for (int64_t b = threadIdx.x; b < nblk; b += FIN_TILES) {
         const TilePart p = a.part2[b];
         cm.merge(p.mean);
         cv.merge(p.var);
         cs.merge(p.sigf);
     }
-    const VgKSum M = vg_block_ksum<FIN2_NT>(cm, red);
-    const VgKSum V = vg_block_ksum<FIN2_NT>(cv, red);
-    const VgKSum Sg = vg_block_ksum<FIN2_NT>(cs, red);
+    const VgKSum M = vg_block_ksum<FIN_TILES>(cm, red);
+    const VgKSum V = vg_block_ksum<FIN_TILES>(cv, red);
+    const VgKSum Sg = vg_block_ksum<FIN_TILES>(cs, red);
     if (threadIdx.x == 0) {
         vg_stats *s = a.stats;
         s->mean = M.value();
         s->var = V.value();
-        reset = 0;
+        *reset = 0;
         s->sigf_reset = 0;
         if (a.adaptive) {
             const double ss = Sg.value();
@@ -279,19 +256,90 @@ __global__ void __launch_bounds__(FIN2_NT) finalize2_kernel(IterArgs a)
             } else {   // integrand looks constant: even distribution (pyx:2212-2215)
                 s->sum_sigf = (double)a.H;
                 s->sigf_reset = 1;
-                reset = 1;
+                *reset = 1;
             }
         }
     }
     __syncthreads();
-    if (reset)
-        for (int64_t h = threadIdx.x; h < a.H; h += FIN2_NT) a.sigf[h] = 1.0;
+    if (*reset)
+        for (int64_t h = threadIdx.x; h < a.H; h += FIN_TILES) a.sigf[h] = 1.0;
+}
+
+// Stage 1, and stage 2 in the block that finishes last (a counter the
+// allocation resets; the partials are read back in block order, so the
+// result does not depend on which block that is).
+template <int FAST>
+__global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
+{
+    __shared__ VgKSum red[1];
+    __shared__ int s_last, s_reset;
+    const vg_stats *st = a.stats;
+    const int64_t N = st->neval;
+    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
+    const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
+    const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
+    if ((int64_t)blockIdx.x < nblk) {
+        const double beta_half = a.beta_half;
+        VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
+        const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
+        if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
+            const TilePart p = a.parts[t];
+            cm = p.mean;
+            cv = p.var;
+            cs = p.sigf;
+        }
+        if (t < ntiles) {   // a hypercube starting in tile t and cut by its end
+            const TileRec r = a.recs[2 * t + 1];
+            if (r.h >= 0) {
+                double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
+                for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+                    const TileRec q = a.recs[2 * t2];
+                    if (q.h != r.h) break;
+                    const double n2 = n + q.n;
+                    const double delta = q.S / q.n - Sx / n;
+                    Q = Q + q.Q + delta * delta * (n * q.n / n2);
+                    Sx += q.S;
+                    D += q.D;
+                    n = n2;
+                    if (!q.spans) break;
+                }
+                const double vh =
+                    __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
+                cm.add(__dadd_rn(Sx, D));
+                cv.add(vh);
+                if (a.adaptive) {
+                    const double sg = FAST ? vg_pow_fast(fabs(vh), beta_half) : pow(fabs(vh), beta_half);
+                    a.sigf[r.h] = sg;
+                    cs.add(sg);
+                }
+            }
+        }
+        const VgKSum M = vg_block_ksum<FIN_TILES>(cm, red);
+        const VgKSum V = vg_block_ksum<FIN_TILES>(cv, red);
+        const VgKSum Sg = vg_block_ksum<FIN_TILES>(cs, red);
+        if (threadIdx.x == 0) {
+            TilePart p;
+            p.mean = M;
+            p.var = V;
+            p.sigf = Sg;
+            a.part2[blockIdx.x] = p;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = (atomicAdd(a.fin_counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) *a.fin_counter = 0u;
+    finalize_totals(a, nblk, red, &s_reset);
 }
 
 // ================================================================ host
 struct WorkLayout {
     size_t neval_h, offsets, bsum, bmax, tile_h0, counter, recs, parts, part2, feval, newgrid,
-        newinc, total;
+        newinc, tablef, total;
     int64_t nblk, ntiles_cap, ncap;
 };
 
@@ -319,7 +367,7 @@ WorkLayout layout(const vg_integrator *it, int64_t ncap)
     L.bsum = o;    o = align256(o + sizeof(int64_t) * L.nblk);
     L.bmax = o;    o = align256(o + sizeof(int64_t) * L.nblk);
     L.tile_h0 = o; o = align256(o + sizeof(int64_t) * (L.ntiles_cap + 1));
-    L.counter = o; o = align256(o + sizeof(unsigned long long));
+    L.counter = o; o = align256(o + sizeof(unsigned long long) + sizeof(unsigned int));
     L.recs = o;    o = align256(o + sizeof(TileRec) * 2 * L.ntiles_cap);
     L.parts = o;   o = align256(o + sizeof(TilePart) * L.ntiles_cap);
     L.part2 = o;   o = align256(o + sizeof(TilePart) * (L.ntiles_cap / FIN_TILES + 4096 / FIN_TILES + 2));
@@ -327,6 +375,9 @@ WorkLayout layout(const vg_integrator *it, int64_t ncap)
     L.ncap = ncap;
     L.newgrid = o; o = align256(o + sizeof(double) * it->dim * it->ldg);
     L.newinc = o;  o = align256(o + sizeof(double) * it->dim * it->ldi);
+    int64_t maxK = 1;
+    for (int d = 0; d < it->dim; d++) maxK = it->ninc[d] > maxK ? it->ninc[d] : maxK;
+    L.tablef = o;  o = align256(o + sizeof(float2) * it->dim * (maxK + 1));
     L.total = o;
     return L;
 }
@@ -373,10 +424,12 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     a.bmax = (int64_t *)(w + L.bmax);
     a.tile_h0 = (int64_t *)(w + L.tile_h0);
     a.counter = (unsigned long long *)(w + L.counter);
+    a.fin_counter = (unsigned int *)(w + L.counter + sizeof(unsigned long long));
     a.recs = (TileRec *)(w + L.recs);
     a.parts = (TilePart *)(w + L.parts);
     a.part2 = (TilePart *)(w + L.part2);
     a.f_eval = (float *)(w + L.feval);
+    a.tablef = (float2 *)(w + L.tablef);
     a.ntiles_cap = L.ntiles_cap;
     a.neval = it->neval;
     a.neval_frac = it->neval_frac;
@@ -402,8 +455,6 @@ int finalize_launch(IterArgs &a, cudaStream_t st, int fast)
     const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     if (fast) finalize1_kernel<1><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
     else finalize1_kernel<0><<<(unsigned)nblk, FIN_TILES, 0, st>>>(a);
-    VG_LAUNCH_CHECK();
-    finalize2_kernel<<<1, FIN2_NT, 0, st>>>(a);
     VG_LAUNCH_CHECK();
     return VG_OK;
 }
@@ -443,12 +494,20 @@ extern "C" int vg_allocate(const vg_integrator *it, void *stream)
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     WorkLayout L = layout(it, a.ncap);
-    alloc_count_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a);
+    // the FP32 grid table is built by the counting grid, or alone when that
+    // grid has too few threads for it
+    const int64_t ntab = (int64_t)a.dim * (a.maxK + 1);
+    const int table_in_count = (it->precision == VG_F32) && ntab <= L.nblk * ALLOC_NT;
+    alloc_count_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a, table_in_count);
     VG_LAUNCH_CHECK();
-    alloc_scan_kernel<<<1, ALLOC_NT, 0, st>>>(a, L.nblk);
+    alloc_scan_kernel<<<1, SCAN_NT, 0, st>>>(a, L.nblk);
     VG_LAUNCH_CHECK();
     alloc_offsets_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a);
     VG_LAUNCH_CHECK();
+    if (it->precision == VG_F32 && !table_in_count) {
+        tablef_kernel<<<(unsigned)((ntab + 255) / 256), 256, 0, st>>>(a);
+        VG_LAUNCH_CHECK();
+    }
     return VG_OK;
 }
 
@@ -488,12 +547,21 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     a.f_in = f;
     a.f_f64 = (f_dtype == VG_F64);
     cudaStream_t st = (cudaStream_t)stream;
-    if ((rc = reset_counter(a, st))) return rc;
-    if ((rc = vg::launch_reduce(a, it->precision == VG_F64, st))) return rc;
+    if ((rc = vg::launch_reduce(a, it->precision == VG_F64, st))) return rc;   // static tiles
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
 static unsigned long long *g_term_count = nullptr;
+namespace vg { int g_eval_split = 0; }
+
+// Tuning: how FP32 iterations of the ridge run -- 0 automatic, 1 the single
+// fused kernel, 2 split into EVAL (writes f) + REDUCE.
+extern "C" int vg_set_eval_split(int policy)
+{
+    if (policy < 0 || policy > 2) return vg_fail(VG_ERR_VALUE, "split policy %d", policy);
+    vg::g_eval_split = policy;
+    return VG_OK;
+}
 
 // Instrumentation: while set, the FP32 ridge adds the number of Gaussian
 // terms it evaluates to *count (device); NULL turns it off.
@@ -550,7 +618,6 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
     int tab_len = 0;
     if ((rc = vg_build_params(kind, it->dim, params, nparams, &P, &tab_len))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    if ((rc = reset_counter(a, st))) return rc;
     if ((rc = vg::launch_fused(a, kind, P, tab_len, it->precision == VG_F64, st))) return rc;
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
@@ -558,13 +625,23 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
 int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
                     const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
                     const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
-                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast);
+                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast, int zero_hist);
+int vg_adapt_in_place_ok(int max_old);
 
 extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
 {
     vg_clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     if (!(it->adapt && it->alpha > 0)) return VG_OK;
+    int64_t kmin = it->ninc[0], kmax = it->ninc[0];
+    for (int d = 1; d < it->dim; d++) {
+        kmin = it->ninc[d] < kmin ? it->ninc[d] : kmin;
+        kmax = it->ninc[d] > kmax ? it->ninc[d] : kmax;
+    }
+    if (kmin > 1 && vg_adapt_in_place_ok((int)kmax))   // one kernel: adapt in place, clear the histogram
+        return vg_adapt_launch(it->dim, it->ninc, it->ninc, it->grid, it->inc, it->ldg, it->ldi, it->sum_f,
+                               it->n_f, it->alpha, it->grid, it->inc, it->ldg, it->ldi, st,
+                               it->precision == VG_F32, 1);
     WorkLayout L = layout(it, neval_cap(it));
     if (it->work_bytes < L.total) return vg_fail(VG_ERR_VALUE, "workspace too small");
     char *w = (char *)it->work;
@@ -572,7 +649,7 @@ extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
     double *ni = (double *)(w + L.newinc);
     int rc = vg_adapt_launch(it->dim, it->ninc, it->ninc, it->grid, it->inc, it->ldg, it->ldi,
                              it->sum_f, it->n_f, it->alpha, ng, ni, it->ldg, it->ldi, st,
-                             it->precision == VG_F32);
+                             it->precision == VG_F32, 0);
     if (rc) return rc;
     VG_CUDA_CHECK(cudaMemcpyAsync(it->grid, ng, sizeof(double) * it->dim * it->ldg,
                                   cudaMemcpyDeviceToDevice, st));

@@ -118,12 +118,15 @@ __global__ void __launch_bounds__(ADAPT_NT) adapt_kernel(AdaptArgs a)
     double *avg = sm;                 // [max_old]
     double *tmp = sm + a.max_old;     // [max_old]
     double *part = tmp + a.max_old;   // [ADAPT_NT]
+    // in place (new_grid == grid): the axis' old nodes and increments staged
+    double *gs = a.new_grid == a.grid ? part + ADAPT_NT : nullptr;   // [max_old + 1]
+    double *is = gs != nullptr ? gs + a.max_old + 1 : nullptr;        // [max_old]
     for (int i = threadIdx.x; i < a.max_old; i += ADAPT_NT) avg[i] = 1.0;
     __syncthreads();
     if (a.sequential) {
-        for (int d = 0; d < a.dim; d++) vgadapt::adapt_axis<ADAPT_NT>(a, d, avg, tmp, part);
+        for (int d = 0; d < a.dim; d++) vgadapt::adapt_axis<ADAPT_NT>(a, d, avg, tmp, part, gs, is);
     } else {
-        vgadapt::adapt_axis<ADAPT_NT>(a, blockIdx.x, avg, tmp, part);
+        vgadapt::adapt_axis<ADAPT_NT>(a, blockIdx.x, avg, tmp, part, gs, is);
     }
 }
 
@@ -255,10 +258,16 @@ extern "C" int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, i
 // Largest old ninc the adapt kernel handles (two FP64 rows in shared memory).
 #define VG_ADAPT_MAX_NINC 12288
 
+// In place the kernel also stages the old nodes and increments (two more rows).
+int vg_adapt_in_place_ok(int max_old) { return 4 * (size_t)max_old + 1 <= 2 * VG_ADAPT_MAX_NINC; }
+
+// In place (new_grid == grid, new_inc == inc) needs the old ninc to equal
+// the new one and vg_adapt_in_place_ok(); zero_hist clears sum_f / n_f once
+// read.
 int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
                     const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
                     const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
-                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast)
+                    int64_t ldg_new, int64_t ldi_new, cudaStream_t st, int fast, int zero_hist)
 {
     if (dim < 1 || dim > VG_MAX_DIM) return vg_fail(VG_ERR_UNSUPPORTED, "dim %d", dim);
     AdaptArgs a;
@@ -293,6 +302,14 @@ int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, c
     a.ldi_new = ldi_new;
     a.max_old = max_old;
     a.fast = fast;
+    a.zero_hist = zero_hist;
+    const int in_place = (new_grid == grid);
+    if (in_place) {
+        for (int d = 0; d < dim; d++)
+            if (old_ninc[d] != new_ninc[d] || new_inc != inc || ldg_new != ldg || ldi_new != ldi)
+                return vg_fail(VG_ERR_VALUE, "in-place adapt keeps ninc and strides");
+        if (!vg_adapt_in_place_ok(max_old)) return vg_fail(VG_ERR_UNSUPPORTED, "in-place adapt: ninc too large");
+    }
     if (max_new == 1) {
         adapt_single_kernel<<<1, 64, 0, st>>>(a);
         VG_LAUNCH_CHECK();
@@ -304,6 +321,7 @@ int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, c
     // previous axis' avg_f[0] (pyx:533-564).
     a.sequential = ((sum_f == nullptr && alpha > 0) || (alpha != 0 && any_one)) ? 1 : 0;
     size_t smem = sizeof(double) * (2 * (size_t)max_old + ADAPT_NT);
+    if (in_place) smem += sizeof(double) * (2 * (size_t)max_old + 1);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(adapt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -321,6 +339,7 @@ extern "C" int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_nin
                         double *new_inc, int64_t ldg_new, int64_t ldi_new, void *stream)
 {
     vg_clear_error();
+    if (new_grid == grid) return vg_fail(VG_ERR_VALUE, "vg_adapt writes a separate grid");
     return vg_adapt_launch(dim, old_ninc, new_ninc, grid, inc, ldg, ldi, sum_f, n_f, alpha,
-                           new_grid, new_inc, ldg_new, ldi_new, (cudaStream_t)stream, 0);
+                           new_grid, new_inc, ldg_new, ldi_new, (cudaStream_t)stream, 0, 0);
 }

@@ -25,8 +25,9 @@ namespace vg {
 
 constexpr int NT = 256;          // threads per tile CTA
 constexpr int BASE_TILE = 256;   // granularity of the tile schedule tile_h0[]
-constexpr int ALLOC_NT = 1024;
-constexpr int ALLOC_PER = 4;
+constexpr int ALLOC_NT = 256;    // allocation count / offsets blocks
+constexpr int ALLOC_PER = 4;     // hypercubes per thread there
+constexpr int SCAN_NT = 1024;    // the one-CTA scan of their block totals
 constexpr int FIN_NT = 1024;
 
 // POINTS: write points for a torch integrand; REDUCE: read f and reduce;
@@ -71,6 +72,7 @@ struct IterArgs {
     int64_t *bsum, *bmax;
     int64_t *tile_h0;         // first hypercube of each BASE_TILE samples
     unsigned long long *counter;  // dynamic tile counter (reset by allocation)
+    unsigned int *fin_counter;    // finalize blocks done (reset by allocation)
     TileRec *recs;
     TilePart *parts;
     int64_t ntiles_cap;       // in BASE_TILE units
@@ -88,6 +90,7 @@ struct IterArgs {
     TilePart *part2;          // finalize: one partial per finalize block
     double *wgt_out;
     int64_t *hc_out;
+    float2 *tablef;           // FP32 mode: (x_node, inc) table [dim][maxK+1], built by the allocation
     int table_smem;           // grid table staged in shared memory
     int hist_smem;            // training histogram in shared memory
     int maxK;
@@ -206,6 +209,38 @@ __device__ __forceinline__ void ff_add_pair(float &ah, float &al, float bh, floa
     e = __fadd_rn(e, __fadd_rn(al, bl));
     ah = __fadd_rn(s, e);
     al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
+// (h, l) = (ah, al) * b in float-float (the head's product error by fma).
+__device__ __forceinline__ void ff_mul_f(float ah, float al, float b, float &h, float &l)
+{
+    const float p = __fmul_rn(ah, b);
+    float e = __fmaf_rn(ah, b, -p);
+    e = __fmaf_rn(al, b, e);
+    h = __fadd_rn(p, e);
+    l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
+// (h, l) = (ah, al)^2 in float-float.
+__device__ __forceinline__ void ff_sqr(float ah, float al, float &h, float &l)
+{
+    const float p = __fmul_rn(ah, ah);
+    float e = __fmaf_rn(ah, ah, -p);
+    e = __fmaf_rn(__fmul_rn(2.f, ah), al, e);
+    h = __fadd_rn(p, e);
+    l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
+// (h, l) = (ah, al) / b in float-float: head quotient, its remainder by fma,
+// one correction term.
+__device__ __forceinline__ void ff_div_f(float ah, float al, float b, float &h, float &l)
+{
+    const float rb = 1.f / b;
+    const float q1 = __fmul_rn(ah, rb);
+    const float r = __fadd_rn(__fmaf_rn(-q1, b, ah), al);
+    const float q2 = __fmul_rn(r, rb);
+    h = __fadd_rn(q1, q2);
+    l = __fsub_rn(q2, __fsub_rn(h, q1));
 }
 
 // Inclusive segmented scan over the NT threads of float-float values:
@@ -377,6 +412,38 @@ __device__ __forceinline__ double vg_div(double a, double b)
     return a * r;
 }
 
+// FP32 mode, rare path: a hypercube whose squared deviations leave the float
+// range, finished in FP64.  Returns its (mean, variance, sigf) contributions
+// and stores its sigf.
+static __device__ __noinline__ double3 finish_f64(double Sx, double Dx, double Qx, int nin, double beta_half,
+                                           int adaptive, double *sigf_h)
+{
+    const double nd = (double)nin;
+    const double vh = vg_div<float>(__dsub_rn(__dmul_rn(nd, Qx), __dmul_rn(Dx, Dx)), __dsub_rn(nd, 1.));
+    double sg = 0.0;
+    if (adaptive) {
+        sg = vg_pow_fast(fabs(vh), beta_half);
+        *sigf_h = sg;
+    }
+    return make_double3(__dadd_rn(Sx, Dx), vh, sg);
+}
+
+// FP32 mode: the (x_node, inc) table of the grid in FP32, entry K of each
+// axis = (grid[K], inc[K-1]) -- built once per iteration by the allocation so
+// the tile CTAs copy it instead of converting FP64 nodes themselves.
+__device__ __forceinline__ void build_tablef(const IterArgs &a, int64_t first, int64_t stride)
+{
+    const int W = a.maxK + 1;
+    for (int64_t i = first; i < (int64_t)a.dim * W; i += stride) {
+        const int d = (int)(i / W), j = (int)(i % W);
+        const int K = a.ninc[d];
+        float2 e = make_float2(0.f, 1.f);
+        if (j < K) e = make_float2((float)a.grid[d * a.ldg + j], (float)a.inc[d * a.ldi + j]);
+        else if (j == K) e = make_float2((float)a.grid[d * a.ldg + K], (float)a.inc[d * a.ldi + K - 1]);
+        a.tablef[i] = e;
+    }
+}
+
 // ------------------------------------------------------------------ kernel
 // The work of one CTA: reduction modes take tiles first, first + stride, ...
 // (static, deterministic); evaluation-only modes take tiles from the atomic
@@ -419,18 +486,25 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
 
     // ---- per-CTA setup: grid table, histogram, integrand constants
     if (a.table_smem) {
-        for (int d = 0; d < dim; d++) {
-            const int K = a.ninc[d];
-            for (int i = tid; i <= K; i += NT) {
-                GE e;
-                if (i < K) {
-                    e.x = (T)a.grid[d * a.ldg + i];
-                    e.y = (T)a.inc[d * a.ldi + i];
-                } else {
-                    e.x = (T)a.grid[d * a.ldg + K];
-                    e.y = (T)a.inc[d * a.ldi + K - 1];
+        if (sizeof(T) == 4) {   // FP32 mode: copy the float table built by the allocation
+            const int n = dim * (a.maxK + 1);
+            const float2 *src = a.tablef;
+            float2 *dst = reinterpret_cast<float2 *>(table);
+            for (int i = tid; i < n; i += NT) dst[i] = src[i];
+        } else {
+            for (int d = 0; d < dim; d++) {
+                const int K = a.ninc[d];
+                for (int i = tid; i <= K; i += NT) {
+                    GE e;
+                    if (i < K) {
+                        e.x = (T)a.grid[d * a.ldg + i];
+                        e.y = (T)a.inc[d * a.ldi + i];
+                    } else {
+                        e.x = (T)a.grid[d * a.ldg + K];
+                        e.y = (T)a.inc[d * a.ldi + K - 1];
+                    }
+                    table[(size_t)d * (a.maxK + 1) + i] = e;
                 }
-                table[(size_t)d * (a.maxK + 1) + i] = e;
             }
         }
     }
@@ -450,6 +524,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     const double dv_y = a.dv_y;
     const float dv_yf = (float)a.dv_y;
     const double beta_half = a.beta_half;
+    const float beta_half_f = (float)a.beta_half;
     float Kf[DIMB], rstrat[DIMB];   // FP32 mode: per-axis constants
 #pragma unroll
     for (int d = 0; d < DIMB; d++) {
@@ -459,6 +534,9 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     int nan_local = 0;
     // per-thread running sums over every hypercube this thread finalises
     double acc_m = 0.0, acc_v = 0.0, acc_s = 0.0;
+    // FP32 mode: the same running sums in float-float, folded in at the end
+    float am_h = 0.f, am_l = 0.f, av_h = 0.f, av_l = 0.f, as_h = 0.f, as_l = 0.f;
+    int used64 = 0;   // FP32 mode: a hypercube went through the FP64 fallback
     int64_t next_static = first;
 
     for (;;) {
@@ -612,6 +690,10 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     GE e;
                     if (a.table_smem) {
                         e = table[(size_t)d * (a.maxK + 1) + ie];
+                    } else if (sizeof(T) == 4) {
+                        const float2 t2 = a.tablef[(size_t)d * (a.maxK + 1) + ie];
+                        e.x = (T)t2.x;
+                        e.y = (T)t2.y;
                     } else if (!clamp) {
                         e.x = (T)a.grid[d * a.ldg + ie];
                         e.y = (T)a.inc[d * a.ldi + ie];
@@ -745,44 +827,78 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         }
         if (ends_last) segf[lk] = make_float2(Pi.x, Pi.y);
         __syncthreads();
-        // per hypercube: mean, variance, sigf in FP64 (pyx:2174-2186)
-        auto finish = [&](int64_t h, int nin, double Sx, double Dx, double Qx) {
-            const double nd = (double)nin;
-            const double vh = vg_div<T>(__dsub_rn(__dmul_rn(nd, Qx), __dmul_rn(Dx, Dx)), __dsub_rn(nd, 1.));
-            acc_m += __dadd_rn(Sx, Dx);
-            acc_v += vh;
+        // per hypercube: mean S + D, variance (n Q - D^2) / (n - 1) and
+        // sigf = |var|^(beta/2) (pyx:2174-2186), in float-float with an FP32
+        // sigf; FP64 only where the squares leave the float range
+        auto finish = [&](int64_t h, int nin, float Sh, float Sl, float Dh, float Dl, float Qh, float Ql,
+                          int big, double Qbig) {
+            if (big || !(fabsf(Qh) < 1e30f)) {
+                const double3 r = finish_f64(vg_ff_value(Sh, Sl), vg_ff_value(Dh, Dl),
+                                             __dadd_rn(vg_ff_value(Qh, Ql), Qbig), nin, beta_half,
+                                             a.adaptive, a.sigf + h);
+                acc_m += r.x;
+                acc_v += r.y;
+                acc_s += r.z;
+                used64 = 1;
+                return;
+            }
+            const float fn = (float)nin;
+            float mh = Sh, ml = Sl;
+            ff_add_pair(mh, ml, Dh, Dl);
+            ff_add_pair(am_h, am_l, mh, ml);
+            float nqh, nql, d2h, d2l, vh, vl;
+            ff_mul_f(Qh, Ql, fn, nqh, nql);
+            ff_sqr(Dh, Dl, d2h, d2l);
+            ff_add_pair(nqh, nql, -d2h, -d2l);
+            ff_div_f(nqh, nql, fn - 1.f, vh, vl);
+            ff_add_pair(av_h, av_l, vh, vl);
             if (a.adaptive) {
-                const double sg = vg_pow_fast(fabs(vh), beta_half);
-                a.sigf[h] = sg;
-                acc_s += sg;
+                const float av = fabsf(vh);
+                const float sg = av > 0.f ? vg_ex2_approx(beta_half_f * vg_lg2_approx(av)) : 0.f;
+                a.sigf[h] = (double)sg;
+                vg_ff_add(as_h, as_l, sg);
             }
         };
+        // pass 2 over the thread's runs of equal hypercube, unrolled over the
+        // S samples so that wf[] and lhs[] stay in registers
         float4 dq_first = make_float4(0.f, 0.f, 0.f, 0.f), dq_last = dq_first;   // (D, Q) float-float
         {
-            int k = 0;
-            while (k < nmine) {
-                const int key = lhs[k];
-                int k1 = k;
-                float sh = 0.f, sl = 0.f;
-                while (k1 < nmine && lhs[k1] == key) vg_ff_add(sh, sl, (float)wf[k1++]);
-                const int nin = win_off[key + 1] - win_off[key];
-                const bool is_first = (key == fk), is_last = (key == lk);
-                if (is_first || is_last) {
-                    const float2 t2 = segf[key];
-                    sh = t2.x;
-                    sl = t2.y;
+            int key = -1, nin = 1, big = 0, nguard = 0;
+            bool is_first = false, is_last = false;
+            float sh = 0.f, sl = 0.f, m_hi = 0.f, m_lo = 0.f, thr_f = 0.f;
+            float dh_s = 0.f, dl_s = 0.f, qh = 0.f, ql = 0.f;
+            double Qbig = 0.0;
+#pragma unroll
+            for (int k = 0; k < S; k++) {
+                if (k >= nmine) continue;
+                if (k == 0 || lhs[k] != key) {   // a run starts: its sum, mean and guard
+                    key = lhs[k];
+                    sh = 0.f;
+                    sl = 0.f;
+#pragma unroll
+                    for (int j = k; j < S; j++)
+                        if (j < nmine && lhs[j] == key) vg_ff_add(sh, sl, (float)wf[j]);
+                    nin = win_off[key + 1] - win_off[key];
+                    is_first = (key == fk);
+                    is_last = (key == lk);
+                    if (is_first || is_last) {
+                        const float2 t2 = segf[key];
+                        sh = t2.x;
+                        sl = t2.y;
+                    }
+                    // mean m = S / nin as float-float
+                    const float fn = (float)nin;
+                    const float rn = 1.f / fn;
+                    m_hi = sh * rn;
+                    m_lo = (__fadd_rn(fmaf(-m_hi, fn, sh), sl)) * rn;
+                    thr_f = (float)VG_EPSILON * fabsf(m_hi);
+                    dh_s = dl_s = qh = ql = 0.f;
+                    nguard = 0;
+                    big = 0;
+                    Qbig = 0.0;
                 }
-                // mean m = S / nin as float-float
-                const float fn = (float)nin;
-                const float rn = 1.f / fn;
-                const float m_hi = sh * rn;
-                const float m_lo = (__fadd_rn(fmaf(-m_hi, fn, sh), sl)) * rn;
-                const float thr_f = (float)VG_EPSILON * fabsf(m_hi);
-                float dh_s = 0.f, dl_s = 0.f, qh = 0.f, ql = 0.f;
-                int nguard = 0;
-                double Qbig = 0.0;
-                for (int q = k; q < k1; q++) {
-                    const float x = (float)wf[q];
+                {
+                    const float x = (float)wf[k];
                     const float s0 = __fsub_rn(x, m_hi);   // TwoSum(wf, -m_hi), then - m_lo
                     const float bb = __fsub_rn(s0, x);
                     float e0 = __fadd_rn(__fsub_rn(x, __fsub_rn(s0, bb)), __fsub_rn(-m_hi, bb));
@@ -791,29 +907,31 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     e0 = __fsub_rn(e0, __fsub_rn(d, s0));
                     if (fabsf(d) < thr_f) {   // |dwf| < EPSILON |mean|, pyx:2156
                         nguard++;
-                        continue;
-                    }
-                    if (fabsf(d) > 1e18f) {   // squares beyond the float range: FP64
-                        const double dd = (double)d + (double)e0;
-                        Qbig = __dadd_rn(Qbig, __dmul_rn(dd, dd));
                     } else {
-                        const float p = __fmul_rn(d, d);
-                        const float pe = __fadd_rn(fmaf(d, d, -p), __fmul_rn(2.f * d, e0));
-                        ff_add_pair(qh, ql, p, pe);
+                        if (fabsf(d) > 1e18f) {   // squares beyond the float range: FP64
+                            const double dd = (double)d + (double)e0;
+                            Qbig = __dadd_rn(Qbig, __dmul_rn(dd, dd));
+                            big = 1;
+                        } else {
+                            const float p = __fmul_rn(d, d);
+                            const float pe = __fadd_rn(fmaf(d, d, -p), __fmul_rn(2.f * d, e0));
+                            ff_add_pair(qh, ql, p, pe);
+                        }
+                        ff_add_pair(dh_s, dl_s, d, e0);
                     }
-                    ff_add_pair(dh_s, dl_s, d, e0);
                 }
-                if (nguard) ff_add_pair(qh, ql, (float)nguard * thr_f * thr_f, 0.f);
-                if (is_first) dq_first = make_float4(dh_s, dl_s, qh, ql);
-                if (is_last) dq_last = make_float4(dh_s, dl_s, qh, ql);
-                if (!is_first && !is_last)   // hypercube wholly inside this thread
-                    finish(h0 + key, nin, vg_ff_value(sh, sl), vg_ff_value(dh_s, dl_s),
-                           __dadd_rn(vg_ff_value(qh, ql), Qbig));
-                else if (Qbig != 0.0) {   // rare: carry the FP64 part through the scan's head
-                    if (is_first) dq_first.z = (float)((double)dq_first.z + Qbig);
-                    else dq_last.z = (float)((double)dq_last.z + Qbig);
+                const bool run_end = (k + 1 >= nmine) || lhs[k + 1 < S ? k + 1 : k] != key;
+                if (run_end) {
+                    if (nguard) ff_add_pair(qh, ql, (float)nguard * thr_f * thr_f, 0.f);
+                    if (is_first) dq_first = make_float4(dh_s, dl_s, qh, ql);
+                    if (is_last) dq_last = make_float4(dh_s, dl_s, qh, ql);
+                    if (!is_first && !is_last)   // hypercube wholly inside this thread
+                        finish(h0 + key, nin, sh, sl, dh_s, dl_s, qh, ql, big, Qbig);
+                    else if (big) {   // rare: carry the FP64 part through the scan's head
+                        if (is_first) dq_first.z = (float)((double)dq_first.z + Qbig);
+                        else dq_last.z = (float)((double)dq_last.z + Qbig);
+                    }
                 }
-                k = k1;
             }
         }
         __syncthreads();
@@ -840,14 +958,14 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             const int nin = win_off[key + 1] - win_off[key];
             const int nh = win_n[key];
             const float2 sg2 = segf[key];
-            const double Sseg = vg_ff_value(sg2.x, sg2.y);
-            const double Dx = vg_ff_value(dq.x, dq.y), Qx = vg_ff_value(dq.z, dq.w);
             const int64_t ostart = a.offsets[h];
             const bool starts_before = ostart < tile_start;
             const bool ends_after = ostart + nh > tile_start + tile_len;
             if (!starts_before && !ends_after) {
-                finish(h, nin, Sseg, Dx, Qx);
+                finish(h, nin, sg2.x, sg2.y, dq.x, dq.y, dq.z, dq.w, 0, 0.0);
             } else {
+                const double Sseg = vg_ff_value(sg2.x, sg2.y);
+                const double Dx = vg_ff_value(dq.x, dq.y), Qx = vg_ff_value(dq.z, dq.w);
                 TileRec r;
                 r.h = h;
                 r.n = (double)nin;
@@ -990,15 +1108,53 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     // NaN flag, histogram flush
     if (NEED_RED) {
         __syncthreads();
-        const VgKSum m = vg_block_ksum<NT>(VgKSum{acc_m, 0.0}, red);
-        const VgKSum v = vg_block_ksum<NT>(VgKSum{acc_v, 0.0}, red);
-        const VgKSum sg = vg_block_ksum<NT>(VgKSum{acc_s, 0.0}, red);
-        if (tid == 0) {
-            TilePart p;
-            p.mean = m;
-            p.var = v;
-            p.sigf = sg;
-            a.parts[part_slot] = p;
+        if constexpr (sizeof(T) == 4) {
+            // float-float block reduction in a fixed order (FP32 pipe); the
+            // rare FP64 finishes are folded in first
+            if (used64) {
+                float h = (float)acc_m;
+                ff_add_pair(am_h, am_l, h, (float)(acc_m - (double)h));
+                h = (float)acc_v;
+                ff_add_pair(av_h, av_l, h, (float)(acc_v - (double)h));
+                h = (float)acc_s;
+                ff_add_pair(as_h, as_l, h, (float)(acc_s - (double)h));
+            }
+            float r6[6] = {am_h, am_l, av_h, av_l, as_h, as_l};
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                float o6[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
+#pragma unroll
+                for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
+            }
+            float *wred = reinterpret_cast<float *>(red);
+            if ((tid & 31) == 0) {
+#pragma unroll
+                for (int i = 0; i < 6; i++) wred[(tid >> 5) * 6 + i] = r6[i];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (int w = 1; w < NT / 32; w++)
+#pragma unroll
+                    for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], wred[w * 6 + i], wred[w * 6 + i + 1]);
+                TilePart p;
+                p.mean = VgKSum{(double)r6[0], (double)r6[1]};
+                p.var = VgKSum{(double)r6[2], (double)r6[3]};
+                p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
+                a.parts[part_slot] = p;
+            }
+        } else {
+            const VgKSum m = vg_block_ksum<NT>(VgKSum{acc_m, 0.0}, red);
+            const VgKSum v = vg_block_ksum<NT>(VgKSum{acc_v, 0.0}, red);
+            const VgKSum sg = vg_block_ksum<NT>(VgKSum{acc_s, 0.0}, red);
+            if (tid == 0) {
+                TilePart p;
+                p.mean = m;
+                p.var = v;
+                p.sigf = sg;
+                a.parts[part_slot] = p;
+            }
         }
         if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
         if (use_bins && a.hist_smem) {

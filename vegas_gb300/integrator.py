@@ -267,7 +267,7 @@ class Integrator(object):
         ncap = L.vg_neval_cap(ctypes.byref(it))
         need = L.vg_workspace_bytes(ctypes.byref(it), 0)
         if self._work is None or self._work.numel() < need:
-            self._work = torch.empty(need, dtype=torch.uint8, device=self.device)
+            self._work = torch.zeros(need, dtype=torch.uint8, device=self.device)
         if self._stats is None:
             self._stats = torch.zeros(ctypes.sizeof(N.VgStats), dtype=torch.uint8, device=self.device)
         if self.map.sum_f is None or self.map.sum_f.shape != inc.shape:
@@ -482,6 +482,10 @@ class Integrator(object):
             raise ValueError('integrand given is a class, not an object -- need to initialize?')
         kind = self._classify(fcn)
         result = RAvg(weighted=self.adapt)
+        if (kind == 'builtin' and self.ran_array_generator is None and not self.uses_jac
+                and self.analyzer is None and save is None and saveall is None
+                and self.rtol == 0 and self.atol == 0):
+            return self._call_pipelined(fcn, result)
         L = N.load()
         stream = N.stream_ptr(self.device)
         dt = torch.float64 if self.precision == 'fp64' else torch.float32
@@ -545,16 +549,7 @@ class Integrator(object):
             # adapt the map on the device before reading the iteration record
             N.check(L.vg_end_iteration(ctypes.byref(it), stream))
             st = self._read_stats()
-            if st.status == N.VG_ERR_MEMORY:
-                raise MemoryError('iteration exceeded its evaluation capacity')
-            elif st.status != 0:
-                raise N.VegasError('device status %d' % st.status)
-            if st.nan_seen:
-                raise ValueError('integrand evaluates to nan')
-            self.last_neval = int(st.neval)
-            self.neval_hcube_range = np.array([st.range_lo, st.range_hi])
-            if self.beta > 0 and self.adapt and self.nhcube > 1:
-                self.sum_sigf = float(st.sum_sigf)
+            self._take_record(st)
             if arr is not None:
                 # array- or dictionary-valued integrand: RAvgArray of the
                 # integrand's shape / RAvgDict of its keys
@@ -583,6 +578,61 @@ class Integrator(object):
                 _save(saveall, (result, self))
             if result.converged(self.rtol, self.atol):
                 break
+        return result
+
+    def _take_record(self, st):
+        """Checks of one iteration's device record; the integrator's copies
+        of its neval, neval range and sum_sigf."""
+        if st.status == N.VG_ERR_MEMORY:
+            raise MemoryError('iteration exceeded its evaluation capacity')
+        elif st.status != 0:
+            raise N.VegasError('device status %d' % st.status)
+        if st.nan_seen:
+            raise ValueError('integrand evaluates to nan')
+        self.last_neval = int(st.neval)
+        self.neval_hcube_range = np.array([st.range_lo, st.range_hi])
+        if self.beta > 0 and self.adapt and self.nhcube > 1:
+            self.sum_sigf = float(st.sum_sigf)
+
+    def _records_host(self, n):
+        sz = ctypes.sizeof(N.VgStats)
+        buf = getattr(self, '_rec_host', None)
+        if buf is None or buf.shape[0] < n:
+            buf = torch.empty((max(n, 16), sz), dtype=torch.uint8, pin_memory=True)
+            self._rec_host = buf
+        return buf
+
+    def _call_pipelined(self, fcn, result):
+        """__call__ for a built-in integrand when no iteration needs a host
+        decision (no rtol/atol stop, analyzer or save): every iteration --
+        allocation, fused evaluate+reduce, adapt -- is enqueued without
+        waiting, and each iteration's record is copied to pinned host memory
+        on the same stream; the records are read once after the last
+        iteration.  Same kernels and results as the iteration-by-iteration
+        loop, without a host round trip per iteration."""
+        L = N.load()
+        stream = N.stream_ptr(self.device)
+        it, ncap = self._struct()
+        self._put_sum_sigf()
+        p = fcn.params(self.dim)
+        params = N.dbl_array(p)
+        nitn = int(self.nitn)
+        host = self._records_host(nitn)
+        for k in range(nitn):
+            N.check(L.vg_allocate(ctypes.byref(it), stream))
+            self._itn += 1
+            N.check(L.vg_fused_iteration(ctypes.byref(it), self._itn & 0xffffffff, None, int(fcn.kind),
+                                         params, len(p), stream))
+            N.check(L.vg_end_iteration(ctypes.byref(it), stream))
+            host[k].copy_(self._stats, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        raw = host[:nitn].numpy().tobytes()
+        sz = ctypes.sizeof(N.VgStats)
+        for k in range(nitn):
+            st = N.VgStats.from_buffer_copy(raw, k * sz)
+            self._take_record(st)
+            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            result.sum_neval += self.last_neval
         return result
 
     # --------------------------------------------------------------- report
