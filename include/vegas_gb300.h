@@ -356,6 +356,11 @@ int vg_set_term_counter(unsigned long long *count);
  * that reads it back. */
 int vg_set_eval_split(int policy);
 
+/* Tuning of the tile kernels: samples per thread of the fused FP32 ridge for
+ * dim <= 4 (0 automatic, 2 or 4); grid table and training histogram in
+ * shared memory (-1 automatic, 0 off, 1 on where it fits). */
+int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem);
+
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */
 int vg_probe_mufu_ex2(float *out, int64_t nthreads, int iters, void *stream);

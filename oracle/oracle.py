@@ -73,10 +73,10 @@ def lib():
         L.vo_alloc.argtypes = [i64, P, dbl, i32, i64, i64, i64, P, P]
         L.vo_alloc.restype = i64
         L.vo_points.argtypes = [i32, P, P, P, i64, P, i64, i64, P, P, u64, u32, u32, P, P, P, P]
-        L.vo_reduce.argtypes = [i64, P, i32, P, P, i32, dbl, P, P, P, P, P]
+        L.vo_reduce.argtypes = [i64, P, i32, P, P, i32, dbl, P, P, P, P, P, P]
         L.vo_eval.argtypes = [i32, P, i32, i64, P, P]
         L.vo_iterate.argtypes = [i32, i32, P, P, P, P, i64, P, i64, i64, P, P, i64, dbl, i64,
-                                 i64, dbl, dbl, i32, u64, u32, u32, i32, P]
+                                 i64, dbl, dbl, i32, i32, u64, u32, u32, i32, P]
         L.vo_iterate.restype = i32
         _lib = L
     return _lib
@@ -257,7 +257,9 @@ def points(nstrat, grid, inc, ninc, neval_h, u=None, seed=0, stream=0, itn=0):
     return y, x, w, hc
 
 
-def reduce(neval_h, wgt, fx, beta=0.75, adaptive=True, sigf=None):
+def reduce(neval_h, wgt, fx, beta=0.75, adaptive=True, sigf=None, hc_var=False):
+    """Returns mean, var, sigf, sum_sigf, fdv2 (and, with hc_var, the
+    per-hypercube |variance| that adapt_to_errors trains the map on)."""
     neval_h = _c(neval_h, np.int64)
     wgt = _c(wgt, float)
     fx = _c(fx, float)
@@ -270,11 +272,14 @@ def reduce(neval_h, wgt, fx, beta=0.75, adaptive=True, sigf=None):
     sigf = np.ones(H) if sigf is None else _c(sigf, float).copy()
     ss = np.zeros(1)
     fdv2 = np.empty(len(wgt))
+    hv = np.empty(H) if hc_var else None
     lib().vo_reduce(H, _p(neval_h), s, _p(wgt), _p(fx), int(adaptive), float(beta), _p(mean),
-                    _p(var), _p(sigf), _p(ss), _p(fdv2))
+                    _p(var), _p(sigf), _p(ss), _p(fdv2), _p(hv))
     for a in range(s):
         for b in range(a):
             var[b, a] = var[a, b]
+    if hc_var:
+        return mean, var, sigf, float(ss[0]), fdv2, hv
     return mean, var, sigf, float(ss[0]), fdv2
 
 
@@ -291,11 +296,12 @@ class State(object):
     """Integrator state for the multi-threaded oracle driver ``iterate``."""
 
     def __init__(self, limits, neval, nitn_hint=None, alpha=0.5, beta=0.75, neval_frac=0.75,
-                 maxinc_axis=1000, max_neval_hcube=50000, nstrat=None):
+                 maxinc_axis=1000, max_neval_hcube=50000, nstrat=None, adapt_to_errors=False):
         limits = np.asarray(limits, float)
         dim = len(limits)
         sz = sizing(dim, neval=neval, neval_frac=neval_frac, beta=beta, maxinc_axis=maxinc_axis,
-                    max_neval_hcube=max_neval_hcube, nstrat=nstrat)
+                    max_neval_hcube=max_neval_hcube, nstrat=nstrat, adapt_to_errors=adapt_to_errors)
+        self.adapt_to_errors = bool(adapt_to_errors)
         self.dim = dim
         self.nstrat = sz['nstrat'].astype(np.int64)
         # AdaptiveMap(limits) then set() regrids with adapt(ninc=...), pyx:1386
@@ -322,7 +328,8 @@ class State(object):
                               self.grid.shape[1], _p(self.inc), self.inc.shape[1], self.H,
                               _p(self.sigf), _p(ss), self.neval, self.neval_frac,
                               self.min_neval_hcube, self.max_neval_hcube, self.alpha, self.beta,
-                              int(adapt), seed, stream, itn, nthreads, _p(out))
+                              int(adapt), int(self.adapt_to_errors), seed, stream, itn, nthreads,
+                              _p(out))
         assert rc == 0
         self.sum_sigf = float(ss[0])
         return dict(mean=out[0], var=out[1], neval=int(out[2]), range=(int(out[3]), int(out[4])))

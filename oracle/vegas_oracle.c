@@ -314,10 +314,13 @@ void vo_points(int dim, const int64_t *nstrat, const int64_t *ninc, const double
 /* Per-hypercube two-pass reduction, pyx:2136-2193, for hypercubes [h0,h1)
  * whose samples start at i0.  fx is [n, s] row-major.  mean[s] and
  * var[s*s] (lower triangle, correlate_integrals=True form) are ACCUMULATED.
- * sigf/sum_sigf updated when adaptive.  fdv2[i] written when non-NULL.     */
+ * sigf/sum_sigf updated when adaptive.  fdv2[i] written when non-NULL.
+ * hc_var[h - h0] = sigf2 = |variance of component 0| (pyx:2181, the
+ * adapt_to_errors training value) when non-NULL.                          */
 static void vo_reduce_range(int64_t h0, int64_t h1, int64_t i0, const int64_t *neval_h, int s,
                             const double *wgt, const double *fx, int adaptive, double beta,
-                            double *mean, double *var, double *sigf, double *sum_sigf, double *fdv2)
+                            double *mean, double *var, double *sigf, double *sum_sigf, double *fdv2,
+                            double *hc_var)
 {
     double sum_wf[16], sum_dwf[16], sum_dwf2[256], dwf[16];
     int64_t j = i0;
@@ -351,6 +354,7 @@ static void vo_reduce_range(int64_t h0, int64_t h1, int64_t i0, const int64_t *n
                 var[a * s + b] += ((double)n * sum_dwf2[a * s + b] - sum_dwf[a] * sum_dwf[b]) / ((double)n - 1.);
         }
         double sigf2 = fabs(((double)n * sum_dwf2[0] - sum_dwf[0] * sum_dwf[0]) / ((double)n - 1.));
+        if (hc_var) hc_var[h - h0] = sigf2;
         if (adaptive) {
             sigf[h] = pow(sigf2, beta / 2.);
             *sum_sigf += sigf[h];
@@ -361,9 +365,10 @@ static void vo_reduce_range(int64_t h0, int64_t h1, int64_t i0, const int64_t *n
 
 void vo_reduce(int64_t H, const int64_t *neval_h, int s, const double *wgt, const double *fx,
                int adaptive, double beta, double *mean, double *var, double *sigf,
-               double *sum_sigf, double *fdv2)
+               double *sum_sigf, double *fdv2, double *hc_var)
 {
-    vo_reduce_range(0, H, 0, neval_h, s, wgt, fx, adaptive, beta, mean, var, sigf, sum_sigf, fdv2);
+    vo_reduce_range(0, H, 0, neval_h, s, wgt, fx, adaptive, beta, mean, var, sigf, sum_sigf, fdv2,
+                    hc_var);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -448,7 +453,7 @@ void vo_eval(int kind, const double *p, int dim, int64_t n, const double *x, dou
 /* out[0]=mean, out[1]=var, out[2]=last_neval, out[3]=range lo, out[4]=hi. */
 /* ------------------------------------------------------------------------ */
 typedef struct {
-    int dim, kind, adaptive, train;
+    int dim, kind, adaptive, train, train_hc;
     const double *p;
     const int64_t *nstrat, *ninc;
     const double *grid, *inc;
@@ -478,6 +483,7 @@ static void *vo_job_run(void *arg)
     double *w = (double *)malloc(sizeof(double) * (size_t)cap);
     double *f = (double *)malloc(sizeof(double) * (size_t)cap);
     double *fdv2 = (double *)malloc(sizeof(double) * (size_t)cap);
+    double *hcv = (double *)malloc(sizeof(double) * (size_t)(J->h1 - J->h0 + 1));
     J->mean = 0.0; J->var = 0.0; J->sum_sigf = 0.0;
     int64_t h = J->h0;
     while (h < J->h1) {
@@ -503,30 +509,42 @@ static void *vo_job_run(void *arg)
         vo_eval(J->kind, J->p, dim, cnt, x, f);
         double m = 0.0, v = 0.0;
         vo_reduce_range(h, he, 0, J->neval_h, 1, w, f, J->adaptive, J->beta, &m, &v, J->sigf,
-                        &J->sum_sigf, fdv2);
+                        &J->sum_sigf, fdv2, hcv);
         J->mean += m;
         J->var += v;
         if (J->train)
             vo_add_training_data(dim, J->ninc, J->ldi, cnt, y, fdv2, J->sum_f, J->n_f);
+        if (J->train_hc) {   /* adapt_to_errors: sigf2 at each hypercube's last sample, pyx:2187-2193 */
+            int64_t klast = -1;
+            for (int64_t hh = h; hh < he; hh++) {
+                klast += J->neval_h[hh];
+                vo_add_training_data(dim, J->ninc, J->ldi, 1, y + klast * dim, &hcv[hh - h], J->sum_f,
+                                     J->n_f);
+            }
+        }
         h = he;
     }
-    free(y); free(x); free(w); free(f); free(fdv2);
+    free(y); free(x); free(w); free(f); free(fdv2); free(hcv);
     return NULL;
 }
 
 int vo_iterate(int dim, int kind, const double *p, const int64_t *nstrat, int64_t *ninc,
                double *grid, int64_t ldg, double *inc, int64_t ldi, int64_t H, double *sigf,
                double *sum_sigf, int64_t neval, double neval_frac, int64_t min_neval_hcube,
-               int64_t max_neval_hcube, double alpha, double beta, int adapt, uint64_t seed,
-               uint32_t stream, uint32_t itn, int nthreads, double *out)
+               int64_t max_neval_hcube, double alpha, double beta, int adapt, int adapt_to_errors,
+               uint64_t seed, uint32_t stream, uint32_t itn, int nthreads, double *out)
 {
-    int adaptive_alloc = (beta > 0 && H > 1);
+    /* adapt_to_errors: uniform allocation, no sigf, the map trained on each
+     * hypercube's variance (pyx:1659, 1675, 2187-2196, 2209)               */
+    int adaptive_alloc = (beta > 0 && H > 1 && !adapt_to_errors);
     int adaptive = adaptive_alloc && adapt;
-    int train = adapt && alpha > 0;
+    int train_hc = adapt_to_errors && adapt;
+    int train = (adapt && alpha > 0 && !adapt_to_errors) || train_hc;
     int64_t *neval_h = (int64_t *)malloc(sizeof(int64_t) * (size_t)H);
     int64_t *offs = (int64_t *)malloc(sizeof(int64_t) * (size_t)(H + 1));
     int64_t range[2];
-    double neval_sigf = (beta > 0 && *sum_sigf > 0) ? neval_frac * (double)neval / *sum_sigf : 0.0;
+    double neval_sigf = (beta > 0 && *sum_sigf > 0 && !adapt_to_errors)
+                            ? neval_frac * (double)neval / *sum_sigf : 0.0;
     int64_t tot = vo_alloc(H, sigf, neval_sigf, adaptive_alloc, min_neval_hcube, max_neval_hcube,
                            (int64_t)((double)neval / (double)H), neval_h, range);
     offs[0] = 0;
@@ -548,7 +566,8 @@ int vo_iterate(int dim, int kind, const double *p, const int64_t *nstrat, int64_
     for (int t = 0; t < nthreads; t++) {
         vo_job *J = &jobs[t];
         memset(J, 0, sizeof(*J));
-        J->dim = dim; J->kind = kind; J->p = p; J->adaptive = adaptive; J->train = train;
+        J->dim = dim; J->kind = kind; J->p = p; J->adaptive = adaptive;
+        J->train = train && !train_hc; J->train_hc = train_hc;
         J->nstrat = nstrat; J->ninc = ninc; J->grid = grid; J->inc = inc; J->ldg = ldg; J->ldi = ldi;
         J->H = H; J->neval_h = neval_h; J->offs = offs;
         J->h0 = bnd[t];
@@ -570,7 +589,7 @@ int vo_iterate(int dim, int kind, const double *p, const int64_t *nstrat, int64_
         if (ss > 0) *sum_sigf = ss;
         else { for (int64_t h = 0; h < H; h++) sigf[h] = 1.; *sum_sigf = (double)H; }
     }
-    if (train) {
+    if (train && alpha > 0) {
         double *sum_f = (double *)calloc(hsz, sizeof(double));
         double *n_f = (double *)malloc(sizeof(double) * hsz);
         for (size_t q = 0; q < hsz; q++) n_f[q] = VO_TINY;
@@ -584,6 +603,8 @@ int vo_iterate(int dim, int kind, const double *p, const int64_t *nstrat, int64_
         memcpy(grid, ng, sizeof(double) * (size_t)dim * (size_t)ldg);
         memcpy(inc, ni, sizeof(double) * hsz);
         free(ng); free(ni); free(sum_f); free(n_f);
+    } else if (train) {   /* adapt_to_errors with alpha = 0: the map is not adapted */
+        for (int t = 0; t < nthreads; t++) { free(jobs[t].sum_f); free(jobs[t].n_f); }
     }
     free(neval_h);
     free(offs);

@@ -121,6 +121,17 @@ def const7(x):
     return 7 * np.ones(x.shape[0], float)
 
 
+def peak2(x):
+    return np.exp(-50 * (x[:, 0] - 0.3) ** 2) * (1 + x[:, 1] ** 2)
+
+
+def ate_trace(v):
+    """adapt_to_errors=True: map increments = strata, uniform allocation, the
+    map trained on each hypercube's variance at its last sample."""
+    return trace(v, 2 * [[0, 1]], peak2, nitn=3, neval=2000, seed=5, alpha=0.5,
+                 adapt_to_errors=True)
+
+
 def adapt_cases(v):
     """Direct AdaptiveMap cases: map edges, training skips, adapt variants."""
     rng = np.random.default_rng(7)
@@ -211,6 +222,7 @@ def main():
                                 lambda x: (np.sin(x[:, 0]) ** 2 + np.cos(x[:, 1]) ** 2) / np.pi ** 2,
                                 nitn=2, neval=3000, seed=4, beta=0.0))
     np.savez_compressed(os.path.join(HERE, 'ref_map_adapt.npz'), **adapt_cases(v), **alloc_cases(v))
+    np.savez_compressed(os.path.join(HERE, 'ref_ate_injected.npz'), **ate_trace(v))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -271,3 +271,39 @@ def test_live_reference_sizing_sweep():
             assert list(I.nstrat) == list(s['nstrat'])
             assert list(I.map.ninc) == list(s['ninc'])
             assert I.min_neval_hcube == s['min_neval_hcube']
+
+
+def replay_ate(tr, alpha=0.5):
+    """adapt_to_errors=True trace: increments = strata, uniform allocation,
+    the map trained on each hypercube's |variance| at the hypercube's last
+    sample (pyx:1372, 1662, 2181-2193)."""
+    nstrat, ninc = tr['nstrat'], tr['ninc']
+    assert np.array_equal(nstrat, ninc)
+    H = int(np.prod(nstrat))
+    neval = int(tr['neval'])
+    mnh, mxh = int(tr['min_neval_hcube']), int(tr['max_neval_hcube'])
+    grid = tr['grid_init']
+    for k in range(int(tr['nitn'])):
+        inc = np.diff(np.nan_to_num(grid), axis=1)
+        nh, rng, tot = O.alloc(np.ones(H), 0.0, False, mnh, mxh, int(neval / H))
+        assert tot == int(tr['last_neval%d' % k])
+        assert list(rng) == list(tr['range%d' % k])
+        u = tr['u%d' % k].astype(np.float64) * 2.0 ** -24
+        y, x, w, hc = O.points(nstrat, np.nan_to_num(grid), inc, ninc, nh, u=u)
+        mean, var, _, _, _, hv = O.reduce(nh, w, tr['f%d' % k], adaptive=False, hc_var=True)
+        assert mean[0] == tr['mean%d' % k]
+        assert var[0, 0] ** 0.5 == tr['sdev%d' % k]
+        last = np.cumsum(nh) - 1
+        sum_f, n_f = O.add_training_data(ninc, inc.shape[1], y[last], hv)
+        grid_new, _, _ = O.adapt(np.nan_to_num(grid), inc, ninc, sum_f, n_f, alpha)
+        want = tr['grid%d' % k]
+        ok = ~np.isnan(want)
+        assert np.array_equal(grid_new[ok], want[ok])
+        grid = want
+
+
+def test_replay_adapt_to_errors():
+    tr = load('ref_ate_injected.npz')
+    sz = O.sizing(2, neval=2000, adapt_to_errors=True)
+    assert list(sz['nstrat']) == list(tr['nstrat']) and list(sz['ninc']) == list(tr['ninc'])
+    replay_ate(tr)

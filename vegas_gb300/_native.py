@@ -170,6 +170,7 @@ SIGNATURES = {
     'vg_flow_train_batch': (I32, [I64, I64, U64, U32, I32, P, P, P, P, P, I32, P, P, P, P]),
     'vg_set_term_counter': (I32, [P]),
     'vg_set_eval_split': (I32, [I32]),
+    'vg_set_tile_tuning': (I32, [I32, I32, I32]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
     'vg_probe_fp32_fma': (I32, [P, I64, I32, P]),

@@ -112,6 +112,91 @@ __device__ double block_sum(const double *v, int n, double *part /* >= 33 */)
     return r;
 }
 
+// FP32 block reductions (max, sum) over ADAPT_NT threads; f = shared scratch
+// of >= 33 floats.  Result broadcast to all threads.
+template <int ADAPT_NT, bool MAX>
+__device__ float block_reduce_f(float v, float *f)
+{
+    constexpr int NW = ADAPT_NT / 32;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float o = __shfl_xor_sync(0xffffffffu, v, off);
+        v = MAX ? fmaxf(v, o) : v + o;
+    }
+    if (lane == 0) f[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        float z = lane < NW ? f[lane] : 0.f;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, z, off);
+            z = MAX ? fmaxf(z, o) : z + o;
+        }
+        if (lane == 0) f[32] = z;
+    }
+    __syncthreads();
+    const float r = f[32];
+    __syncthreads();
+    return r;
+}
+
+// FP32 mode, alpha > 0 with training data: the weights of one axis (average,
+// 3-tap smoothing, normalisation, damping; pyx:539-562) in FP32 on the MUFU,
+// written to avg[] as doubles.  A normalised weight outside the float range
+// (or within 1e-5 of 1) is formed and damped in FP64, so tiny weights keep
+// the reference's ((1 - v) / -ln v)^alpha.  The cumulative sums and the new
+// nodes (regrid) stay FP64.
+template <int ADAPT_NT>
+__device__ void adapt_weights_fast(const AdaptArgs &a, int d, int K, double *avg, double *tmp, double *part)
+{
+    const int t = threadIdx.x;
+    float *af = reinterpret_cast<float *>(tmp);   // [K] averages
+    float *sf = af + K;                           // [K] smoothed (tmp holds 2K floats)
+    float *pf = reinterpret_cast<float *>(part);
+    for (int i = t; i < K; i += ADAPT_NT) {
+        const unsigned long long c = a.n_f[d * a.ldi + i];
+        af[i] = c ? (float)div_fast(a.sum_f[d * a.ldi + i], (double)c) : 0.f;
+        if (a.zero_hist) {
+            const_cast<double *>(a.sum_f)[d * a.ldi + i] = 0.0;
+            const_cast<unsigned long long *>(a.n_f)[d * a.ldi + i] = 0ull;
+        }
+    }
+    __syncthreads();
+    float mx = 0.f;
+    for (int i = t; i < K; i += ADAPT_NT) {
+        float v;
+        if (i == 0) v = fmaf(7.f, af[0], af[1]);
+        else if (i == K - 1) v = fmaf(7.f, af[K - 1], af[K - 2]);
+        else v = fmaf(6.f, af[i], af[i - 1] + af[i + 1]);
+        v = fabsf(v) * 0.125f;
+        sf[i] = v;
+        mx = fmaxf(mx, v);
+    }
+    mx = block_reduce_f<ADAPT_NT, true>(mx, pf);
+    const float rmx = mx > 0.f ? 1.f / mx : 0.f;   // sum of values scaled by the max: no overflow
+    float sp = 0.f;
+    for (int i = t; i < K; i += ADAPT_NT) sp += sf[i] * rmx;
+    sp = block_reduce_f<ADAPT_NT, false>(sp, pf);
+    const float rs = sp > 0.f ? 1.f / sp : 0.f;
+    const float alf = (float)a.alpha;
+    for (int i = t; i < K; i += ADAPT_NT) {
+        const float vf = sf[i] * rmx * rs;
+        double v;
+        if (sp > 0.f && vf >= 1.17549435e-38f && vf < 0.99999f) {
+            const float one_m = 1.f - vf;
+            const float lnv = one_m < 0.25f ? log1pf(-one_m) : vg_lg2_approx(vf) * 0.69314718f;
+            const float q = one_m / (-lnv);
+            v = (double)vg_ex2_approx(alf * vg_lg2_approx(q));
+        } else {
+            v = sp > 0.f ? (double)sf[i] * (double)rmx * (double)rs + VG_TINY : VG_TINY;
+            if (v > 0 && v <= 0.99999999) v = damp_fast(v, a.alpha);
+        }
+        avg[i] = v;
+    }
+    __syncthreads();
+}
+
 // One axis of AdaptiveMap.adapt.  avg (length >= max_old) holds the carried
 // avg_f values on entry, the final ones on exit.  With gs / is (shared
 // memory, max_old + 1 and max_old doubles) the axis' old nodes and
@@ -125,7 +210,9 @@ __device__ void adapt_axis(const AdaptArgs &a, int d, double *avg, double *tmp, 
     const int Kn = a.new_ninc[d];
     const int t = threadIdx.x;
     const double alpha = a.alpha;
-    if (alpha != 0 && K > 1) {
+    if (alpha > 0 && K > 1 && a.fast && a.sum_f != nullptr) {
+        adapt_weights_fast<ADAPT_NT>(a, d, K, avg, tmp, part);
+    } else if (alpha != 0 && K > 1) {
         if (a.sum_f != nullptr) {
             for (int i = t; i < K; i += ADAPT_NT) {
                 const unsigned long long c = a.n_f[d * a.ldi + i];

@@ -176,6 +176,7 @@ __device__ __forceinline__ VgKSum vg_block_ksum(VgKSum v, VgKSum *smem /* NT/32 
         VgKSum o = vg_ksum_shfl_down(v, off);
         v.merge(o);
     }
+    if (NT == 32) return v;   // one warp: done (FP64 instructions are costly)
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) smem[w] = v;
     __syncthreads();

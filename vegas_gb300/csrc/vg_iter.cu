@@ -25,6 +25,7 @@
 #include <math.h>
 #include <string.h>
 
+#include "vg_adapt.cuh"
 #include "vg_tile.cuh"
 
 namespace {
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_count_kernel(IterArgs a, int b
     __shared__ int64_t s_avg;
     if (threadIdx.x == 0) {
         const double sum_sigf = a.stats->sum_sigf;
-        s_nsf = (a.beta > 0 && sum_sigf > 0) ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
+        s_nsf = (a.adaptive_alloc && sum_sigf > 0) ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
                                              : 0.0;
         s_avg = (int64_t)((double)a.neval / (double)a.H);
         if (blockIdx.x == 0) a.stats->neval_sigf = s_nsf;
@@ -278,7 +279,100 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
     const int64_t nwork = ntiles > a.ncta ? ntiles : a.ncta;
     const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
-    if ((int64_t)blockIdx.x < nblk) {
+    if (FAST && (int64_t)blockIdx.x < nblk) {
+        // FP32 mode: the tile partials and the cut hypercubes' records hold
+        // float-float values; merged and summed in float-float (FP32 pipe),
+        // one FP64 partial per block for the FP64 sum of stage 2
+        float mh = 0.f, ml = 0.f, vh_ = 0.f, vl_ = 0.f, sh = 0.f, sl = 0.f;
+        const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
+        if (t < a.ncta && ntiles > 0) {
+            const TilePart p = a.parts[t];
+            mh = (float)p.mean.s;
+            ml = (float)p.mean.c;
+            vh_ = (float)p.var.s;
+            vl_ = (float)p.var.c;
+            sh = (float)p.sigf.s;
+            sl = (float)p.sigf.c;
+        }
+        if (t < ntiles) {
+            const TileRec r = a.recs[2 * t + 1];
+            if (r.h >= 0) {
+                float n = (float)r.n, Sh, Sl, Qh, Ql, Dh, Dl;
+                ff_from_double(r.S, Sh, Sl);
+                ff_from_double(r.Q, Qh, Ql);
+                ff_from_double(r.D, Dh, Dl);
+                bool big = !(fabsf(Qh) < 1e30f);
+                for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+                    const TileRec q = a.recs[2 * t2];
+                    if (q.h != r.h) break;
+                    const float qn = (float)q.n, n2 = n + qn;
+                    float qSh, qSl, qQh, qQl, qDh, qDl;
+                    ff_from_double(q.S, qSh, qSl);
+                    ff_from_double(q.Q, qQh, qQl);
+                    ff_from_double(q.D, qDh, qDl);
+                    big |= !(fabsf(qQh) < 1e30f);
+                    // Chan et al.: Q = Q1 + Q2 + (m2 - m1)^2 n1 n2 / (n1 + n2)
+                    float m1h, m1l, m2h, m2l, wph, wpl, wh, wl, ddh, ddl, th, tl;
+                    ff_div_f(Sh, Sl, n, m1h, m1l);
+                    ff_div_f(qSh, qSl, qn, m2h, m2l);
+                    ff_add_pair(m2h, m2l, -m1h, -m1l);
+                    wph = __fmul_rn(n, qn);
+                    wpl = __fmaf_rn(n, qn, -wph);
+                    ff_div_f(wph, wpl, n2, wh, wl);
+                    ff_sqr(m2h, m2l, ddh, ddl);
+                    ff_mul(ddh, ddl, wh, wl, th, tl);
+                    ff_add_pair(Qh, Ql, qQh, qQl);
+                    ff_add_pair(Qh, Ql, th, tl);
+                    ff_add_pair(Sh, Sl, qSh, qSl);
+                    ff_add_pair(Dh, Dl, qDh, qDl);
+                    n = n2;
+                    if (!q.spans) break;
+                }
+                float vh, vl;
+                if (!big) {
+                    float nqh, nql, d2h, d2l;
+                    ff_mul_f(Qh, Ql, n, nqh, nql);
+                    ff_sqr(Dh, Dl, d2h, d2l);
+                    ff_add_pair(nqh, nql, -d2h, -d2l);
+                    ff_div_f(nqh, nql, n - 1.f, vh, vl);
+                } else {   // squares beyond the float range: this hypercube in FP64
+                    const double Q = vg_ff_value(Qh, Ql), D = vg_ff_value(Dh, Dl), nd = (double)n;
+                    ff_from_double(vgadapt::div_fast(__dsub_rn(__dmul_rn(nd, Q), __dmul_rn(D, D)), nd - 1.0),
+                                   vh, vl);
+                }
+                if (a.train_hc) {   // adapt_to_errors: train at the hypercube's last sample
+                    unsigned short b[VG_MAX_DIM];
+                    last_sample_bins<float>(a, r.h, b);
+                    train_hcube(a, b, fabs(vg_ff_value(vh, vl)));
+                }
+                ff_add_pair(Sh, Sl, Dh, Dl);
+                ff_add_pair(mh, ml, Sh, Sl);
+                ff_add_pair(vh_, vl_, vh, vl);
+                if (a.adaptive) {
+                    const float av = fabsf(vh);
+                    const float sg = av > 0.f ? vg_ex2_approx((float)a.beta_half * vg_lg2_approx(av)) : 0.f;
+                    a.sigf[r.h] = (double)sg;
+                    vg_ff_add(sh, sl, sg);
+                }
+            }
+        }
+        float r6[6] = {mh, ml, vh_, vl_, sh, sl};
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            float o6[6];
+#pragma unroll
+            for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
+#pragma unroll
+            for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
+        }
+        if (threadIdx.x == 0) {
+            TilePart p;
+            p.mean = VgKSum{(double)r6[0], (double)r6[1]};
+            p.var = VgKSum{(double)r6[2], (double)r6[3]};
+            p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
+            a.part2[blockIdx.x] = p;
+        }
+    } else if ((int64_t)blockIdx.x < nblk) {
         const double beta_half = a.beta_half;
         VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
         const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
@@ -296,15 +390,23 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
                     const TileRec q = a.recs[2 * t2];
                     if (q.h != r.h) break;
                     const double n2 = n + q.n;
-                    const double delta = q.S / q.n - Sx / n;
-                    Q = Q + q.Q + delta * delta * (n * q.n / n2);
+                    // Chan et al. merge; FP32 mode: reciprocal-multiply divisions
+                    const double delta = FAST ? vgadapt::div_fast(q.S, q.n) - vgadapt::div_fast(Sx, n)
+                                              : q.S / q.n - Sx / n;
+                    Q = Q + q.Q + delta * delta * (FAST ? vgadapt::div_fast(n * q.n, n2) : n * q.n / n2);
                     Sx += q.S;
                     D += q.D;
                     n = n2;
                     if (!q.spans) break;
                 }
-                const double vh =
-                    __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
+                const double num = __dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D));
+                const double vh = FAST ? vgadapt::div_fast(num, __dsub_rn(n, 1.))
+                                       : __ddiv_rn(num, __dsub_rn(n, 1.));
+                if (a.train_hc) {   // adapt_to_errors: train at the hypercube's last sample
+                    unsigned short b[VG_MAX_DIM];
+                    last_sample_bins<double>(a, r.h, b);
+                    train_hcube(a, b, fabs(vh));
+                }
                 cm.add(__dadd_rn(Sx, D));
                 cv.add(vh);
                 if (a.adaptive) {
@@ -386,7 +488,6 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
 {
     memset(&a, 0, sizeof(a));
     if (it->dim < 1 || it->dim > VG_MAX_DIM) return vg_fail(VG_ERR_UNSUPPORTED, "dim");
-    if (it->adapt_to_errors) return vg_fail(VG_ERR_UNSUPPORTED, "adapt_to_errors");
     if (!it->work || !it->stats) return vg_fail(VG_ERR_VALUE, "missing workspace/stats");
     a.dim = it->dim;
     int maxK = 1;
@@ -412,9 +513,13 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     char *w = (char *)it->work;
     a.sigf = it->sigf;
     a.beta = it->beta;
-    a.adaptive_alloc = (it->beta > 0 && it->nhcube > 1) ? 1 : 0;
+    // adapt_to_errors: uniform allocation, no sigf, the map trained on each
+    // hypercube's variance (pyx:1659, 1675, 2187-2196, 2209)
+    const int ate = it->adapt_to_errors ? 1 : 0;
+    a.adaptive_alloc = (it->beta > 0 && it->nhcube > 1 && !ate) ? 1 : 0;
     a.adaptive = (a.adaptive_alloc && it->adapt) ? 1 : 0;
-    a.train = (it->adapt && it->alpha > 0) ? 1 : 0;
+    a.train = (it->adapt && it->alpha > 0 && !ate) ? 1 : 0;
+    a.train_hc = (ate && it->adapt) ? 1 : 0;
     a.sum_f = it->sum_f;
     a.n_f = (unsigned long long *)it->n_f;
     a.stats = it->stats;
@@ -531,6 +636,7 @@ extern "C" int vg_sample(const vg_integrator *it, uint32_t itn, const double *u,
     a.wgt_out = wgt;
     a.hc_out = hcube;
     a.train = 0;
+    a.train_hc = 0;
     a.adaptive = 0;
     cudaStream_t st = (cudaStream_t)stream;
     if ((rc = reset_counter(a, st))) return rc;
@@ -552,7 +658,24 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
 }
 
 static unsigned long long *g_term_count = nullptr;
-namespace vg { int g_eval_split = 0; }
+namespace vg {
+int g_eval_split = 0;
+int g_tile_s4 = 0, g_tile_table = -1, g_tile_hist = -1;
+}
+
+// Tuning of the tile kernels: samples per thread of the fused FP32 ridge for
+// dim <= 4 (0 automatic, 2 or 4), grid table and training histogram in shared
+// memory (-1 automatic, 0 off, 1 on where it fits).
+extern "C" int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem)
+{
+    if (s_dim4 != 0 && s_dim4 != 2 && s_dim4 != 4) return vg_fail(VG_ERR_VALUE, "s_dim4 %d", s_dim4);
+    if (table_smem < -1 || table_smem > 1 || hist_smem < -1 || hist_smem > 1)
+        return vg_fail(VG_ERR_VALUE, "shared-memory policy");
+    vg::g_tile_s4 = s_dim4;
+    vg::g_tile_table = table_smem;
+    vg::g_tile_hist = hist_smem;
+    return VG_OK;
+}
 
 // Tuning: how FP32 iterations of the ridge run -- 0 automatic, 1 the single
 // fused kernel, 2 split into EVAL (writes f) + REDUCE.

@@ -64,6 +64,7 @@ struct IterArgs {
     int adaptive;             // update sigf (pyx:2083, 2183-2186)
     int adaptive_alloc;       // allocate from sigf (pyx:1668)
     int train;                // accumulate training histogram (pyx:2196)
+    int train_hc;             // adapt_to_errors: train on each hypercube's variance (pyx:2187-2193)
     double *sum_f;
     unsigned long long *n_f;
     vg_stats *stats;
@@ -219,6 +220,24 @@ __device__ __forceinline__ void ff_mul_f(float ah, float al, float b, float &h, 
     e = __fmaf_rn(al, b, e);
     h = __fadd_rn(p, e);
     l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
+// (h, l) = (ah, al) * (bh, bl) in float-float.
+__device__ __forceinline__ void ff_mul(float ah, float al, float bh, float bl, float &h, float &l)
+{
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    h = __fadd_rn(p, e);
+    l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
+// A double as float-float (exact when it came from one).
+__device__ __forceinline__ void ff_from_double(double x, float &h, float &l)
+{
+    h = (float)x;
+    l = (float)(x - (double)h);
 }
 
 // (h, l) = (ah, al)^2 in float-float.
@@ -412,11 +431,83 @@ __device__ __forceinline__ double vg_div(double a, double b)
     return a * r;
 }
 
+// One sample's y along one axis and its map increment index (pyx:1738-1742,
+// 325-330): yd = (y0 + u) / nstrat, yn = yd * K, iy = floor(yn); yfl = the
+// floor as T.  FP32 mode: the reciprocal of nstrat and K as float are given,
+// the floor's integer comes from the float's bits (0 <= yn < 2^23): no
+// int <-> float conversion per sample (those share GB300's slow FP64 pipe).
+template <typename T>
+__device__ __forceinline__ int sample_y(int y0, float y0f, T u, int ns, float rns, int K, float Kf, T &yd,
+                                        T &yn, T &yfl)
+{
+    int iy;
+    if (sizeof(T) == 8) {
+        yd = (T)__ddiv_rn(__dadd_rn((double)y0, (double)u), (double)ns);
+        yn = (T)__dmul_rn((double)yd, (double)K);
+        iy = (int)floor((double)yn);
+        yfl = (T)iy;
+    } else {
+        yd = (T)__fmul_rn(__fadd_rn(y0f, (float)u), rns);
+        yn = (T)__fmul_rn((float)yd, Kf);
+        const float fl = floorf((float)yn);
+        iy = __float_as_int(fl + 8388608.f) - 0x4B000000;
+        yfl = (T)fl;
+    }
+    return iy;
+}
+
+// Training bin of a sample along one axis: its increment, or 0xffff when y
+// is 0 or 1 (add_training_data skips those, pyx:460).
+template <typename T>
+__device__ __forceinline__ unsigned short sample_bin(T yd, int iy, int K)
+{
+    return (unsigned short)((yd > (T)0 && yd < (T)1 && iy < K) ? iy : 0xffff);
+}
+
+// adapt_to_errors: the hypercube's |variance| into the training histogram
+// at its last sample's bins, count 1 (pyx:2187-2193).
+__device__ __forceinline__ void train_hcube(const IterArgs &a, const unsigned short *bins, double v)
+{
+    for (int d = 0; d < a.dim; d++) {
+        const unsigned short b = bins[d];
+        if (b == 0xffff) continue;
+        atomicAdd(&a.sum_f[d * a.ldi + b], v);
+        atomicAdd(&a.n_f[d * a.ldi + b], 1ull);
+    }
+}
+
+// The training bins of hypercube h's last sample, regenerated from its
+// uniforms exactly as the tile kernels form them (for hypercubes that the
+// finalize merges across tiles).
+template <typename T>
+__device__ void last_sample_bins(const IterArgs &a, int64_t h, unsigned short *bins)
+{
+    const int dim = a.dim;
+    const int64_t ig = a.offsets[h] + a.neval_h[h] - 1;
+    T u[VG_MAX_DIM];
+    if (a.u != nullptr) {
+        for (int d = 0; d < dim; d++) u[d] = (T)a.u[ig * dim + d];
+    } else {
+        VgUniform<T>::template draw<VG_MAX_DIM>(a.seed, a.stream, a.itn, (uint64_t)ig, dim, u);
+    }
+    int64_t hh = h;
+    for (int d = 0; d < dim; d++) {
+        const int ns = a.nstrat[d];
+        const int y0 = (int)(hh % ns);
+        hh /= ns;
+        const int K = a.ninc[d];
+        T yd, yn, yfl;
+        const int iy = sample_y<T>(y0, (float)y0, u[d], ns, 1.f / (float)ns, K, (float)K, yd, yn, yfl);
+        bins[d] = sample_bin<T>(yd, iy, K);
+    }
+}
+
 // FP32 mode, rare path: a hypercube whose squared deviations leave the float
 // range, finished in FP64.  Returns its (mean, variance, sigf) contributions
 // and stores its sigf.
+// (With want_var, the third value is |variance| instead: adapt_to_errors.)
 static __device__ __noinline__ double3 finish_f64(double Sx, double Dx, double Qx, int nin, double beta_half,
-                                           int adaptive, double *sigf_h)
+                                                  int adaptive, double *sigf_h, int want_var)
 {
     const double nd = (double)nin;
     const double vh = vg_div<float>(__dsub_rn(__dmul_rn(nd, Qx), __dmul_rn(Dx, Dx)), __dsub_rn(nd, 1.));
@@ -425,7 +516,7 @@ static __device__ __noinline__ double3 finish_f64(double Sx, double Dx, double Q
         sg = vg_pow_fast(fabs(vh), beta_half);
         *sigf_h = sg;
     }
-    return make_double3(__dadd_rn(Sx, Dx), vh, sg);
+    return make_double3(__dadd_rn(Sx, Dx), vh, want_var ? fabs(vh) : sg);
 }
 
 // FP32 mode: the (x_node, inc) table of the grid in FP32, entry K of each
@@ -460,7 +551,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     const int dim = a.dim;
     const int tid = threadIdx.x;
     constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
-    const int use_bins = NEED_RED && a.train;
+    const int use_bins = NEED_RED && (a.train || a.train_hc);   // per-sample bins in shared memory
     const SmemPlan sp = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, a.tab_len,
                                      use_bins, NEED_RED);
     GE *table = (GE *)(smem + sp.table);
@@ -667,23 +758,9 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 for (int d = 0; d < DIMB; d++) {
                     if (d >= dim) continue;
                     const int K = a.ninc[d];
-                    T yd, yn, dy;
-                    int iy;
-                    if (sizeof(T) == 8) {
-                        yd = (T)__ddiv_rn(__dadd_rn((double)y0[d], (double)u[d]), (double)a.nstrat[d]);
-                        yn = (T)__dmul_rn((double)yd, (double)K);
-                        iy = (int)floor((double)yn);
-                        dy = yn - (T)iy;
-                    } else {
-                        // no int <-> float conversions per sample (they share the
-                        // slow FP64 pipe on GB300): reciprocal of nstrat, float K,
-                        // the floor's integer from the float's bits (0 <= yn < 2^23)
-                        yd = (T)((y0f[d] + (float)u[d]) * rstrat[d]);
-                        yn = (T)((float)yd * Kf[d]);
-                        const float fl = floorf((float)yn);
-                        iy = __float_as_int(fl + 8388608.f) - 0x4B000000;
-                        dy = (T)((float)yn - fl);
-                    }
+                    T yd, yn, yfl;
+                    const int iy = sample_y<T>(y0[d], y0f[d], u[d], a.nstrat[d], rstrat[d], K, Kf[d], yd, yn, yfl);
+                    const T dy = yn - yfl;
                     yv[d] = yd;
                     const int clamp = iy >= K;
                     const int ie = clamp ? K : iy;
@@ -709,9 +786,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                         xs[k][d] = clamp ? e.x : (T)fmaf((float)e.y, (float)dy, (float)e.x);
                         jac = (T)((float)jac * ((float)e.y * Kf[d]));
                     }
-                    if (use_bins)
-                        sbins[(li0 + k) * dim + d] =
-                            (unsigned short)((yd > (T)0 && yd < (T)1 && iy < K) ? iy : 0xffff);
+                    if (use_bins) sbins[(li0 + k) * dim + d] = sample_bin<T>(yd, iy, K);
                 }
                 // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
                 if (sizeof(T) == 8) wg[k] = (T)__dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
@@ -772,7 +847,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 wf32 = (float)wg[k] * (float)fv[k];
                 wf[k] = (T)wf32;
             }
-            if (use_bins) {
+            if (use_bins && a.train) {
                 // fdv2 = (wgt*f*neval)^2, pyx:2173; |fdv2| into the bins, pyx:460-463
                 T fd;
                 if (sizeof(T) == 8) {
@@ -835,11 +910,12 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             if (big || !(fabsf(Qh) < 1e30f)) {
                 const double3 r = finish_f64(vg_ff_value(Sh, Sl), vg_ff_value(Dh, Dl),
                                              __dadd_rn(vg_ff_value(Qh, Ql), Qbig), nin, beta_half,
-                                             a.adaptive, a.sigf + h);
+                                             a.adaptive, a.sigf + h, a.train_hc);
                 acc_m += r.x;
                 acc_v += r.y;
-                acc_s += r.z;
+                if (!a.train_hc) acc_s += r.z;
                 used64 = 1;
+                if (a.train_hc) train_hcube(a, sbins + (size_t)(win_off[(int)(h - h0) + 1] - 1) * dim, r.z);
                 return;
             }
             const float fn = (float)nin;
@@ -858,6 +934,8 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 a.sigf[h] = (double)sg;
                 vg_ff_add(as_h, as_l, sg);
             }
+            if (a.train_hc)
+                train_hcube(a, sbins + (size_t)(win_off[(int)(h - h0) + 1] - 1) * dim, fabs(vg_ff_value(vh, vl)));
         };
         // pass 2 over the thread's runs of equal hypercube, unrolled over the
         // S samples so that wf[] and lhs[] stay in registers
@@ -1039,6 +1117,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                         a.sigf[h0 + key] = sg;
                         acc_s += sg;
                     }
+                    if (a.train_hc) train_hcube(a, sbins + (size_t)(win_off[key + 1] - 1) * dim, fabs(vh));
                 }
                 k = k1;
             }
@@ -1079,6 +1158,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     a.sigf[h] = sg;
                     acc_s += sg;
                 }
+                if (a.train_hc) train_hcube(a, sbins + (size_t)(win_off[key + 1] - 1) * dim, fabs(vh));
             } else {
                 TileRec r;
                 r.h = h;
@@ -1181,6 +1261,11 @@ __global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
 }
 
 // ---------------------------------------------------------------- launcher
+// Tuning (vg_set_tile_tuning): samples per thread of the fused FP32 kernel
+// for dim <= 4 (0 = automatic), grid table / histogram in shared memory
+// (-1 automatic, 0 off, 1 on where it fits).
+extern int g_tile_s4, g_tile_table, g_tile_hist;
+
 template <typename T, int MODE, int KIND, int DIMB, int S>
 int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
 {
@@ -1189,10 +1274,10 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
     a.tab_len = tab_len;
     a.T = TT;
     constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
-    const int bins = NEED_RED && a.train;
+    const int bins = NEED_RED && (a.train || a.train_hc);
     const size_t budget = 200 * 1024;
-    a.table_smem = 1;
-    a.hist_smem = bins;
+    a.table_smem = g_tile_table == 0 ? 0 : 1;
+    a.hist_smem = g_tile_hist == 0 ? 0 : (NEED_RED && a.train);
     SmemPlan p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins, NEED_RED);
     if (p.total > budget && a.hist_smem) {
         a.hist_smem = 0;

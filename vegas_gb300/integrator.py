@@ -182,8 +182,6 @@ class Integrator(object):
                 raise AttributeError('no parameter named "%s"' % str(k))
         if self.precision not in ('fp32', 'fp64'):
             raise ValueError("precision must be 'fp32' or 'fp64'")
-        if self.adapt_to_errors:
-            raise NotImplementedError('adapt_to_errors=True is not supported yet')
         # sanity checks (pyx:1319-1330)
         if nstrat is not None:
             if len(nstrat) != self.map.dim:
