@@ -451,7 +451,8 @@ def gpu_arm(args):
         'gpu_launches': 6 * args.steps,
         'roofline': {'bound': 'sfu', 'achieved': achieved, 'peak': peak, 'unit': 'Gex2/s',
                      'frac': achieved / peak, 'traffic': None,
-                     'kernel': 'ridge iteration: tile_kernel EVAL + REDUCE + finalize (CUDA events)',
+                     'kernel': 'ridge iteration: fused tile_kernel (evaluate + reduce) + finalize '
+                               '(CUDA events)',
                      'algorithmic': 'ex2 evaluated per launch: %d (the terms that can be nonzero '
                                     'in FP32; all M=1000 terms per evaluation = %d, the rest are '
                                     'exactly zero and skipped)' % (executed, ex2_per_launch),

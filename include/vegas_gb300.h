@@ -146,6 +146,11 @@ int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const do
 /* AdaptiveMap.map, pyx:310-360: y[n,dim] -> x[n,dim], jac[n] (dtype VG_F32/VG_F64). */
 int vg_map(int dim, const int64_t *ninc, const double *grid, const double *inc, int64_t ldg,
            int64_t ldi, int64_t n, const void *y, void *x, void *jac, int dtype, void *stream);
+/* AdaptiveMap.invmap (_vegas.pyx:362-413): y[n, dim] and jac[n] for x[n, dim]
+ * (searchsorted per axis; y = 0 / 1 outside the grid), FP64 arithmetic,
+ * dtype VG_F32 / VG_F64 for x, y and jac. */
+int vg_invmap(int dim, const int64_t *ninc, const double *grid, const double *inc, int64_t ldg,
+              int64_t ldi, int64_t n, const void *x, void *y, void *jac, int dtype, void *stream);
 /* AdaptiveMap.jac1d (_vegas.pyx:265-295): out[n, dim] = dx[d]/dy[d] at y[n, dim]
  * (dtype VG_F32 / VG_F64 for y and out). */
 int vg_jac1d(int dim, const int64_t *ninc, const double *inc, int64_t ldi, int64_t n, const void *y,
@@ -357,8 +362,9 @@ int vg_set_term_counter(unsigned long long *count);
 int vg_set_eval_split(int policy);
 
 /* Tuning of the tile kernels: samples per thread of the fused FP32 ridge for
- * dim <= 4 (0 automatic, 2 or 4); grid table and training histogram in
- * shared memory (-1 automatic, 0 off, 1 on where it fits). */
+ * dim <= 4 (0 automatic = 2, four CTAs per SM; or 4); grid table and
+ * training histogram in shared memory (-1 automatic, 0 off, 1 on where it
+ * fits). */
 int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem);
 
 /* ------------------------------------------------------------- probes */

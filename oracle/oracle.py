@@ -69,6 +69,7 @@ def lib():
         L.vo_make_uniform.argtypes = [i32, P, P, P, P, i64, P, i64]
         L.vo_map.argtypes = [i32, P, P, i64, P, i64, i64, P, P, P]
         L.vo_add_training_data.argtypes = [i32, P, i64, i64, P, P, P, P]
+        L.vo_invmap.argtypes = [i32, P, P, i64, P, i64, i64, P, P, P]
         L.vo_adapt.argtypes = [i32, P, P, i64, P, i64, P, P, dbl, P, P, i64, P, i64]
         L.vo_alloc.argtypes = [i64, P, dbl, i32, i64, i64, i64, P, P]
         L.vo_alloc.restype = i64
@@ -194,6 +195,39 @@ def map_points(grid, inc, ninc, y):
     lib().vo_map(dim, _p(ninc), _p(grid), grid.shape[1], _p(inc), inc.shape[1], n, _p(y), _p(x),
                  _p(jac))
     return x, jac
+
+
+def invmap(grid, inc, ninc, x):
+    """AdaptiveMap.invmap (pyx:362-413): returns y, jac."""
+    ninc = _c(ninc, np.int64)
+    grid = _c(grid, float)
+    inc = _c(inc, float)
+    x = _c(x, float)
+    n, dim = x.shape
+    y = np.empty_like(x)
+    jac = np.empty(n)
+    lib().vo_invmap(dim, _p(ninc), _p(grid), grid.shape[1], _p(inc), inc.shape[1], n, _p(x), _p(y),
+                    _p(jac))
+    return y, jac
+
+
+def adapt_to_samples(grid, inc, ninc, x, fx, nitn=5, alpha=1.0, maxinc_axis=1000):
+    """AdaptiveMap.adapt_to_samples (pyx:728-790) composed from the oracle's
+    invmap, add_training_data and adapt: returns grid, inc, ninc."""
+    ninc = _c(ninc, np.int64)
+    fx = _c(fx, float)
+    old_ninc = max(int(max(ninc)), maxinc_axis)
+    tmp_ninc = int(min(old_ninc, x.shape[0] / 10.))
+    if tmp_ninc < 2:
+        raise ValueError('not enough samples')
+    grid, inc, ninc = adapt(grid, inc, ninc, None, None, 0.0, tmp_ninc)
+    for _ in range(nitn):
+        y, jac = invmap(grid, inc, ninc, x)
+        sum_f, n_f = add_training_data(ninc, inc.shape[1], y, (jac * fx) ** 2)
+        grid, inc, ninc = adapt(grid, inc, ninc, sum_f, n_f, alpha, tmp_ninc)
+    if tmp_ninc != old_ninc:
+        grid, inc, ninc = adapt(grid, inc, ninc, None, None, 0.0, old_ninc)
+    return grid, inc, ninc
 
 
 def add_training_data(ninc, ldi, y, f, sum_f=None, n_f=None):

@@ -133,6 +133,40 @@ void vo_map(int dim, const int64_t *ninc, const double *grid, int64_t ldg, const
     }
 }
 
+/* AdaptiveMap.invmap, pyx:362-413: iy = searchsorted(grid[d], x, 'right');
+ * y = (iy-1 + (x - grid[iy-1]) / inc[iy-1]) / ninc inside, 0 below, 1 above;
+ * jac *= inc * ninc.                                                       */
+void vo_invmap(int dim, const int64_t *ninc, const double *grid, int64_t ldg, const double *inc,
+               int64_t ldi, int64_t n, const double *x, double *y, double *jac)
+{
+    for (int64_t i = 0; i < n; i++) jac[i] = 1.;
+    for (int d = 0; d < dim; d++) {
+        int64_t K = ninc[d];
+        const double *gd = grid + d * ldg;
+        for (int64_t i = 0; i < n; i++) {
+            double xv = x[i * dim + d];
+            int64_t lo = 0, hi = K + 1;
+            while (lo < hi) {
+                int64_t mid = (lo + hi) / 2;
+                if (gd[mid] <= xv) lo = mid + 1;
+                else hi = mid;
+            }
+            int64_t iy = lo;
+            if (iy > 0 && iy <= K) {
+                int64_t iyi = iy - 1;
+                y[i * dim + d] = ((double)iyi + (xv - gd[iyi]) / inc[d * ldi + iyi]) / (double)K;
+                jac[i] *= inc[d * ldi + iyi] * (double)K;
+            } else if (iy <= 0) {
+                y[i * dim + d] = 0.;
+                jac[i] *= inc[d * ldi] * (double)K;
+            } else {
+                y[i * dim + d] = 1.0;
+                jac[i] *= inc[d * ldi + K - 1] * (double)K;
+            }
+        }
+    }
+}
+
 /* AdaptiveMap.add_training_data, pyx:421-464.  sum_f/n_f [dim, ldi] must be
  * initialised by the caller (0 and TINY, pyx:450-452).                      */
 void vo_add_training_data(int dim, const int64_t *ninc, int64_t ldi, int64_t n, const double *y,

@@ -183,6 +183,43 @@ def adapt_cases(v):
     return cases
 
 
+def invmap_cases(v):
+    """AdaptiveMap.invmap on an adapted map (points inside, on nodes, outside
+    the grid) and adapt_to_samples.  Equal ninc on every axis: with unequal
+    ninc the reference's rows are zero-padded and numpy.searchsorted sees an
+    unsorted row."""
+    rng = np.random.default_rng(13)
+    out = {}
+    m = v.AdaptiveMap([[0, 1], [-2, 3]], ninc=[9, 9])
+    y0 = rng.random((400, 2))
+    m.add_training_data(y0, np.exp(-20 * (y0[:, 0] - 0.4) ** 2) + y0[:, 1] ** 2)
+    m.adapt(alpha=1.0)
+    g = np.asarray(m.grid)
+    x = np.concatenate([rng.uniform([-0.1, -2.5], [1.1, 3.5], (200, 2)),
+                        np.stack([g[0, :9], g[1, 1:10]], axis=1),
+                        [[0.0, -2.0], [1.0, 3.0], [-1e-9, 3.0 + 1e-9]]])
+    y = np.empty_like(x)
+    jac = np.empty(len(x))
+    m.invmap(x, y, jac)
+    out['inv_grid'] = valid_grid(m)
+    out['inv_ninc'] = np.asarray(m.ninc, np.int64)
+    out['inv_x'] = x
+    out['inv_y'] = y
+    out['inv_jac'] = jac
+    # adapt_to_samples: a 3-d map adapted to samples of a peaked function
+    m2 = v.AdaptiveMap([[0, 1], [0, 2], [-1, 1]], ninc=[50, 50, 50])
+    xs = np.column_stack([rng.random(3000), 2 * rng.random(3000), 2 * rng.random(3000) - 1])
+    fs = np.exp(-30 * (xs[:, 0] - 0.3) ** 2 - 10 * (xs[:, 1] - 1.2) ** 2) * (1 + xs[:, 2] ** 2)
+    out['ats_grid_in'] = valid_grid(m2)
+    out['ats_ninc_in'] = np.asarray(m2.ninc, np.int64)
+    m2.adapt_to_samples(xs, fs, nitn=4, alpha=0.8)
+    out['ats_x'] = xs
+    out['ats_f'] = fs
+    out['ats_grid_out'] = valid_grid(m2)
+    out['ats_ninc_out'] = np.asarray(m2.ninc, np.int64)
+    return out
+
+
 def alloc_cases(v):
     """Allocation from a given sigf, incl. the max_neval_hcube clamp."""
     rng = np.random.default_rng(11)
@@ -223,6 +260,7 @@ def main():
                                 nitn=2, neval=3000, seed=4, beta=0.0))
     np.savez_compressed(os.path.join(HERE, 'ref_map_adapt.npz'), **adapt_cases(v), **alloc_cases(v))
     np.savez_compressed(os.path.join(HERE, 'ref_ate_injected.npz'), **ate_trace(v))
+    np.savez_compressed(os.path.join(HERE, 'ref_invmap.npz'), **invmap_cases(v))
     for f in sorted(os.listdir(HERE)):
         if f.endswith('.npz'):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -307,3 +307,22 @@ def test_replay_adapt_to_errors():
     sz = O.sizing(2, neval=2000, adapt_to_errors=True)
     assert list(sz['nstrat']) == list(tr['nstrat']) and list(sz['ninc']) == list(tr['ninc'])
     replay_ate(tr)
+
+
+def test_invmap_golden():
+    c = load('ref_invmap.npz')
+    g = np.nan_to_num(c['inv_grid'])
+    y, jac = O.invmap(g, np.diff(g, axis=1), c['inv_ninc'], c['inv_x'])
+    assert np.array_equal(y, c['inv_y'])
+    assert np.array_equal(jac, c['inv_jac'])
+
+
+def test_adapt_to_samples_golden():
+    c = load('ref_invmap.npz')
+    g = np.nan_to_num(c['ats_grid_in'])
+    grid, inc, ninc = O.adapt_to_samples(g, np.diff(g, axis=1), c['ats_ninc_in'], c['ats_x'],
+                                         c['ats_f'], nitn=4, alpha=0.8)
+    assert list(ninc) == list(c['ats_ninc_out'])
+    want = c['ats_grid_out']
+    ok = ~np.isnan(want)
+    assert np.array_equal(grid[ok], want[ok])

@@ -139,6 +139,7 @@ SIGNATURES = {
     'vg_make_uniform': (I32, [I32, P, P, P, P, I64, P, I64, P]),
     'vg_adapt': (I32, [I32, P, P, P, P, I64, I64, P, P, DBL, P, P, I64, I64, P]),
     'vg_map': (I32, [I32, P, P, P, I64, I64, I64, P, P, P, I32, P]),
+    'vg_invmap': (I32, [I32, P, P, P, I64, I64, I64, P, P, P, I32, P]),
     'vg_jac1d': (I32, [I32, P, P, I64, I64, P, P, I32, P]),
     'vg_add_training_data': (I32, [I32, P, I64, I64, P, P, I32, P, P, P]),
     'vg_allocate': (I32, [P, P]),

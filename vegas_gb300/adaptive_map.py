@@ -1,8 +1,8 @@
 """AdaptiveMap with its grid resident in GPU memory.
 
 Python face of the reference's ``AdaptiveMap`` (src/vegas/_vegas.pyx:39-832):
-same constructor, ``map``/``__call__``/``jac``/``jac1d``,
-``add_training_data``, ``adapt``, ``make_uniform``, ``region``,
+same constructor, ``map``/``invmap``/``__call__``/``jac``/``jac1d``,
+``add_training_data``, ``adapt``, ``adapt_to_samples``, ``make_uniform``, ``region``,
 ``extract_grid``, ``settings`` and pickling.  The grid ``[dim, max(ninc)+1]``
 and increments live on the device in FP64; every numeric operation is a
 kernel of ``libvegas_gb300.so``.  Host (numpy) arguments are copied to the
@@ -210,6 +210,62 @@ class AdaptiveMap(object):
         if xt is not x:
             x[:n] = xt[:n].cpu().numpy() if not isinstance(x, torch.Tensor) else xt[:n]
             jac[:n] = jt[:n].cpu().numpy() if not isinstance(jac, torch.Tensor) else jt[:n]
+
+    def invmap(self, x, y, jac, nx=-1):
+        """Fill y[j, d] and jac[j] (= dx/dy) for x[j, d] (pyx:362-413).
+
+        CUDA tensors are used in place; host arrays are computed on the
+        device and copied back."""
+        xt, on_dev = self._as_device(x)
+        n = xt.shape[0] if nx < 0 else int(nx)
+        if n > xt.shape[0]:
+            raise ValueError('nx > x.shape[0]: %d > %d' % (n, xt.shape[0]))
+        if xt.dtype not in (torch.float32, torch.float64):
+            xt = xt.to(torch.float64)
+        dt = N.VG_F64 if xt.dtype == torch.float64 else N.VG_F32
+        if on_dev and isinstance(y, torch.Tensor) and isinstance(jac, torch.Tensor):
+            yt, jt = y, jac
+        else:
+            yt = torch.empty_like(xt)
+            jt = torch.empty(xt.shape[0], dtype=xt.dtype, device=self.device)
+        L = N.load()
+        N.check(L.vg_invmap(self.dim, self._geom(), N.ptr(self._grid), N.ptr(self._inc),
+                            self._grid.shape[1], self._inc.shape[1], n, N.ptr(xt), N.ptr(yt),
+                            N.ptr(jt), dt, N.stream_ptr(self.device)))
+        if yt is not y:
+            y[:n] = yt[:n].cpu().numpy() if not isinstance(y, torch.Tensor) else yt[:n]
+            jac[:n] = jt[:n].cpu().numpy() if not isinstance(jac, torch.Tensor) else jt[:n]
+
+    def adapt_to_samples(self, x, f, nitn=5, alpha=1.0, nproc=1):
+        """Adapt the map to data {x, f(x)} (pyx:728-790): the grid is
+        regridded to min(max(ninc, 1000), len(x) / 10) increments, then nitn
+        rounds of invmap -> training data (jac f)^2 -> adapt(alpha), and
+        finally regridded to max(max(ninc), 1000) increments, as the
+        reference does.  ``f`` is a callable (called with ``x`` as given)
+        or an array of values; ``nproc`` is accepted for compatibility (the
+        device does the work)."""
+        xt, _ = self._as_device(x, torch.float64)
+        if xt.dim() != 2 or xt.shape[1] != self.dim:
+            raise ValueError('incompatible shape of x: {}'.format(tuple(xt.shape)))
+        fx = f(x) if callable(f) else f
+        ft, _ = self._as_device(fx, torch.float64)
+        ft = ft.reshape(-1)
+        if ft.shape[0] != xt.shape[0]:
+            raise ValueError('shape of x and f(x) mismatch: {} vs {}'.format(
+                tuple(xt.shape), tuple(ft.shape)))
+        old_ninc = max(int(max(self._ninc)), 1000)   # Integrator.defaults['maxinc_axis']
+        tmp_ninc = int(min(old_ninc, xt.shape[0] / 10.))
+        if tmp_ninc < 2:
+            raise ValueError('not enough samples: {}'.format(xt.shape[0]))
+        y = torch.empty_like(xt)
+        jac = torch.empty(xt.shape[0], dtype=torch.float64, device=self.device)
+        self.adapt(ninc=tmp_ninc)
+        for _ in range(int(nitn)):
+            self.invmap(xt, y, jac)
+            self.add_training_data(y, (jac * ft) ** 2)
+            self.adapt(alpha=alpha, ninc=tmp_ninc)
+        if tmp_ninc != old_ninc:
+            self.adapt(ninc=old_ninc)
 
     def __call__(self, y):
         """x values for y (any leading shape; last axis is direction)."""

@@ -40,7 +40,7 @@ __device__ __forceinline__ double damp_fast(double v, double alpha)
 // a / b in double with one Newton step on a float reciprocal (FP32 mode).
 __device__ __forceinline__ double div_fast(double a, double b)
 {
-    double r = (double)(1.0f / (float)b);
+    double r = (double)__frcp_rn((float)b);
     r = fma(r, fma(-b, r, 1.0), r);
     return a * r;
 }

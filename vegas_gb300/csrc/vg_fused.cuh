@@ -35,7 +35,7 @@ int launch_fused_kind(IterArgs &a, const VgParams &P, int tab_len, int f64, cuda
     }
     if (a.dim <= 4) {
         if constexpr (KIND == VG_F_RIDGE)
-            if (g_tile_s4 == 2) return launch_tile<float, MODE_FUSED, KIND, 4, 2>(a, &P, tab_len, st);
+            if (g_tile_s4 != 4) return launch_tile<float, MODE_FUSED, KIND, 4, 2>(a, &P, tab_len, st);
         return launch_tile<float, MODE_FUSED, KIND, 4, 4>(a, &P, tab_len, st);
     }
     if (a.dim <= 8) return launch_tile<float, MODE_FUSED, KIND, 8, 4>(a, &P, tab_len, st);

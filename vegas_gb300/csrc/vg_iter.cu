@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
         // one FP64 partial per block for the FP64 sum of stage 2
         float mh = 0.f, ml = 0.f, vh_ = 0.f, vl_ = 0.f, sh = 0.f, sl = 0.f;
         const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
-        if (t < a.ncta && ntiles > 0) {
+        if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
             const TilePart p = a.parts[t];
             mh = (float)p.mean.s;
             ml = (float)p.mean.c;
@@ -664,8 +664,9 @@ int g_tile_s4 = 0, g_tile_table = -1, g_tile_hist = -1;
 }
 
 // Tuning of the tile kernels: samples per thread of the fused FP32 ridge for
-// dim <= 4 (0 automatic, 2 or 4), grid table and training histogram in shared
-// memory (-1 automatic, 0 off, 1 on where it fits).
+// dim <= 4 (0 automatic = 2, with 4 CTAs per SM; or 4), grid table and
+// training histogram in shared memory (-1 automatic, 0 off, 1 on where it
+// fits).
 extern "C" int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem)
 {
     if (s_dim4 != 0 && s_dim4 != 2 && s_dim4 != 4) return vg_fail(VG_ERR_VALUE, "s_dim4 %d", s_dim4);

@@ -234,6 +234,69 @@ extern "C" int vg_map(int dim, const int64_t *ninc, const double *grid, const do
     return VG_OK;
 }
 
+// ---------------------------------------------------------------- invmap
+// pyx:362-413: iy = searchsorted(grid[d], x, side='right') (nodes <= x);
+// inside: y = (iy-1 + (x - grid[iy-1]) / inc[iy-1]) / ninc, jac *= inc*ninc;
+// below the first node y = 0 with inc[0]; above the last y = 1 with
+// inc[ninc-1].  FP64 arithmetic for either storage type.
+template <typename T>
+__global__ void invmap_kernel(MapGeom g, const double *__restrict__ grid,
+                              const double *__restrict__ inc, int64_t ldg, int64_t ldi, int64_t n,
+                              const T *__restrict__ x, T *__restrict__ y, T *__restrict__ jac)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int dim = g.dim;
+    double j = 1.0;
+    for (int d = 0; d < dim; d++) {
+        const int K = g.ninc[d];
+        const double xv = (double)x[i * dim + d];
+        const double *gd = grid + d * ldg;
+        int lo = 0, hi = K + 1;   // first node > xv, in [0, K+1]
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (gd[mid] <= xv) lo = mid + 1;
+            else hi = mid;
+        }
+        const int iy = lo;
+        double yv, w;
+        if (iy > 0 && iy <= K) {
+            w = inc[d * ldi + iy - 1];
+            yv = __ddiv_rn(__dadd_rn((double)(iy - 1), __ddiv_rn(__dsub_rn(xv, gd[iy - 1]), w)), (double)K);
+        } else if (iy <= 0) {
+            w = inc[d * ldi];
+            yv = 0.0;
+        } else {
+            w = inc[d * ldi + K - 1];
+            yv = 1.0;
+        }
+        y[i * dim + d] = (T)yv;
+        j = __dmul_rn(j, __dmul_rn(w, (double)K));
+    }
+    jac[i] = (T)j;
+}
+
+extern "C" int vg_invmap(int dim, const int64_t *ninc, const double *grid, const double *inc,
+                         int64_t ldg, int64_t ldi, int64_t n, const void *x, void *y, void *jac,
+                         int dtype, void *stream)
+{
+    vg_clear_error();
+    MapGeom g;
+    int rc = fill_geom(g, dim, ninc);
+    if (rc) return rc;
+    if (n <= 0) return VG_OK;
+    const int nt = 256;
+    const int64_t nb = (n + nt - 1) / nt;
+    if (dtype == VG_F64)
+        invmap_kernel<double><<<(unsigned)nb, nt, 0, (cudaStream_t)stream>>>(
+            g, grid, inc, ldg, ldi, n, (const double *)x, (double *)y, (double *)jac);
+    else
+        invmap_kernel<float><<<(unsigned)nb, nt, 0, (cudaStream_t)stream>>>(
+            g, grid, inc, ldg, ldi, n, (const float *)x, (float *)y, (float *)jac);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
 extern "C" int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, int64_t n,
                                     const void *y, const void *f, int dtype, double *sum_f,
                                     uint64_t *n_f, void *stream)

@@ -254,7 +254,7 @@ __device__ __forceinline__ void ff_sqr(float ah, float al, float &h, float &l)
 // one correction term.
 __device__ __forceinline__ void ff_div_f(float ah, float al, float b, float &h, float &l)
 {
-    const float rb = 1.f / b;
+    const float rb = __frcp_rn(b);   // correctly rounded reciprocal, cheaper than a division
     const float q1 = __fmul_rn(ah, rb);
     const float r = __fadd_rn(__fmaf_rn(-q1, b, ah), al);
     const float q2 = __fmul_rn(r, rb);
@@ -372,14 +372,15 @@ struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
         }
         const float4 *t4 = reinterpret_cast<const float4 *>(tab);
         const int n4 = nterm >> 2;
-        // Window of groups of 4 terms that can be nonzero for one of the S
-        // samples: a term with E0 - (w - v_j)^2 < -127 is exactly zero
-        // (ex2.approx.ftz flushes it), so skipping whole groups of such terms
-        // leaves every accumulator -- and f -- bit-identical.
-        int qlo = n4, qhi = 0;
         const float rc = 1.f / kc.c[4];
+        unsigned int nt = 0;
 #pragma unroll
         for (int k = 0; k < S; k++) {
+            // This sample's window of groups of 4 terms that can be nonzero: a
+            // term with E0 - (w - v_j)^2 < -127 is exactly zero
+            // (ex2.approx.ftz flushes it), so skipping whole groups of such
+            // terms leaves the sum -- and f -- bit-identical.
+            int qlo = n4, qhi = 0;
             const float rad2 = E0[k] + 127.f;
             if (rad2 > 0.f) {
                 const float delta = sqrtf(rad2) * 1.0001f + 1e-3f;
@@ -387,33 +388,31 @@ struct BatchEval<float, VG_F_RIDGE, DIMB, S> {
                 int jhi = (int)ceilf((w[k] + delta) * rc - 0.5f) + 1;
                 jlo = jlo < 0 ? 0 : jlo;
                 jhi = jhi > nterm - 1 ? nterm - 1 : jhi;
-                qlo = min(qlo, jlo >> 2);
-                qhi = max(qhi, min(n4, (jhi >> 2) + 1));
+                qlo = jlo >> 2;
+                qhi = min(n4, (jhi >> 2) + 1);
             }
+            nt += qhi > qlo ? (unsigned int)(4 * (qhi - qlo)) : 0u;
+            float b0 = 0.f, b1 = 0.f, b2 = 0.f, b3 = 0.f;
+            const float wk = w[k], ek = E0[k];
+#pragma unroll 2
+            for (int q = qlo; q < qhi; q++) {
+                const float4 v = t4[q];
+                const float d0 = wk - v.x, d1 = wk - v.y, d2 = wk - v.z, d3 = wk - v.w;
+                b0 += vg_ex2(fmaf(-d0, d0, ek));
+                b1 += vg_ex2(fmaf(-d1, d1, ek));
+                b2 += vg_ex2(fmaf(-d2, d2, ek));
+                b3 += vg_ex2(fmaf(-d3, d3, ek));
+            }
+            for (int j = n4 << 2; j < nterm; j++) {
+                const float d0 = wk - tab[j];
+                b0 += vg_ex2(fmaf(-d0, d0, ek));
+            }
+            a0[k] = b0 + b1;
+            a1[k] = b2 + b3;
         }
         if (prm.term_count != nullptr) {   // instrumentation: terms evaluated
-            const unsigned int nt = qhi > qlo ? (unsigned int)(4 * S * (qhi - qlo)) : 0u;
             const unsigned int tot = __reduce_add_sync(0xffffffffu, nt);
             if ((threadIdx.x & 31) == 0) atomicAdd(prm.term_count, (unsigned long long)tot);
-        }
-#pragma unroll 2
-        for (int q = qlo; q < qhi; q++) {
-            const float4 v = t4[q];
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                float d0 = w[k] - v.x, d1 = w[k] - v.y, d2 = w[k] - v.z, d3 = w[k] - v.w;
-                a0[k] += vg_ex2(fmaf(-d0, d0, E0[k]));
-                a1[k] += vg_ex2(fmaf(-d1, d1, E0[k]));
-                a0[k] += vg_ex2(fmaf(-d2, d2, E0[k]));
-                a1[k] += vg_ex2(fmaf(-d3, d3, E0[k]));
-            }
-        }
-        for (int j = n4 << 2; j < nterm; j++) {
-#pragma unroll
-            for (int k = 0; k < S; k++) {
-                float d0 = w[k] - tab[j];
-                a0[k] += vg_ex2(fmaf(-d0, d0, E0[k]));
-            }
         }
 #pragma unroll
         for (int k = 0; k < S; k++) f[k] = kc.c[2] * (a0[k] + a1[k]);
@@ -426,7 +425,7 @@ template <typename T>
 __device__ __forceinline__ double vg_div(double a, double b)
 {
     if (sizeof(T) == 8) return __ddiv_rn(a, b);
-    double r = (double)(1.0f / (float)b);
+    double r = (double)__frcp_rn((float)b);
     r = fma(r, fma(-b, r, 1.0), r);
     return a * r;
 }
@@ -540,7 +539,7 @@ __device__ __forceinline__ void build_tablef(const IterArgs &a, int64_t first, i
 // (static, deterministic); evaluation-only modes take tiles from the atomic
 // counter.  The CTA's partial sums go to a.parts[part_slot].  Called by the
 // grid-wide tile_kernel (first = blockIdx.x, stride = gridDim.x) and by the
-// batched kernel, where one CTA runs a whole integral (0, 1, 0).
+// batched kernel, where G CTAs share an integral (rank, G, rank).
 template <typename T, int MODE, int KIND, int DIMB, int S>
 __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm, unsigned char *smem,
                                           int64_t first, int64_t stride, int64_t part_slot)
@@ -573,6 +572,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
 
     const int64_t N = a.stats->neval;
     const int64_t ntiles = (N + TT - 1) / TT;
+    const int64_t nbase = (N + BASE_TILE - 1) / BASE_TILE;
     if (a.stats->ntiles == 0) return;   // allocation failed: nothing to do
 
     // ---- per-CTA setup: grid table, histogram, integrand constants
@@ -628,6 +628,64 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     // FP32 mode: the same running sums in float-float, folded in at the end
     float am_h = 0.f, am_l = 0.f, av_h = 0.f, av_l = 0.f, as_h = 0.f, as_l = 0.f;
     int used64 = 0;   // FP32 mode: a hypercube went through the FP64 fallback
+    // The running sums -> one compensated block reduction in a fixed order ->
+    // a.parts[slot]; the sums restart from zero.
+    auto emit_partial = [&](int64_t slot) {
+        __syncthreads();
+        if constexpr (sizeof(T) == 4) {
+            // float-float block reduction (FP32 pipe); the rare FP64
+            // finishes are folded in first
+            if (used64) {
+                float h = (float)acc_m;
+                ff_add_pair(am_h, am_l, h, (float)(acc_m - (double)h));
+                h = (float)acc_v;
+                ff_add_pair(av_h, av_l, h, (float)(acc_v - (double)h));
+                h = (float)acc_s;
+                ff_add_pair(as_h, as_l, h, (float)(acc_s - (double)h));
+            }
+            float r6[6] = {am_h, am_l, av_h, av_l, as_h, as_l};
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                float o6[6];
+#pragma unroll
+                for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
+#pragma unroll
+                for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
+            }
+            float *wred = reinterpret_cast<float *>(red);
+            if ((tid & 31) == 0) {
+#pragma unroll
+                for (int i = 0; i < 6; i++) wred[(tid >> 5) * 6 + i] = r6[i];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (int w = 1; w < NT / 32; w++)
+#pragma unroll
+                    for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], wred[w * 6 + i], wred[w * 6 + i + 1]);
+                TilePart p;
+                p.mean = VgKSum{(double)r6[0], (double)r6[1]};
+                p.var = VgKSum{(double)r6[2], (double)r6[3]};
+                p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
+                a.parts[slot] = p;
+            }
+            am_h = am_l = av_h = av_l = as_h = as_l = 0.f;
+            if (used64) acc_m = acc_v = acc_s = 0.0;
+            used64 = 0;
+        } else {
+            const VgKSum m = vg_block_ksum<NT>(VgKSum{acc_m, 0.0}, red);
+            const VgKSum v = vg_block_ksum<NT>(VgKSum{acc_v, 0.0}, red);
+            const VgKSum sg = vg_block_ksum<NT>(VgKSum{acc_s, 0.0}, red);
+            if (tid == 0) {
+                TilePart p;
+                p.mean = m;
+                p.var = v;
+                p.sigf = sg;
+                a.parts[slot] = p;
+            }
+            acc_m = acc_v = acc_s = 0.0;
+        }
+        __syncthreads();
+    };
     int64_t next_static = first;
 
     for (;;) {
@@ -649,7 +707,6 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         const int tile_len = (int)min((int64_t)TT, N - tile_start);
         const int64_t h0 = a.tile_h0[tile * KSUB];
         const int64_t bnext = (tile + 1) * KSUB;            // base tile after this tile
-        const int64_t nbase = (N + BASE_TILE - 1) / BASE_TILE;
         const int64_t hnext = bnext < nbase ? a.tile_h0[bnext] : a.H;
         const int64_t hlast = (hnext < a.H) ? hnext : a.H - 1;
         const int nwin = (int)(hlast - h0 + 1);
@@ -966,7 +1023,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     }
                     // mean m = S / nin as float-float
                     const float fn = (float)nin;
-                    const float rn = 1.f / fn;
+                    const float rn = __frcp_rn(fn);
                     m_hi = sh * rn;
                     m_lo = (__fadd_rn(fmaf(-m_hi, fn, sh), sl)) * rn;
                     thr_f = (float)VG_EPSILON * fabsf(m_hi);
@@ -1184,58 +1241,10 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         }
     }
 
-    // ---- CTA epilogue: partial sums (one compensated block reduction),
-    // NaN flag, histogram flush
+    // ---- epilogue: partial sums (unless written per tile), NaN flag,
+    // histogram flush
     if (NEED_RED) {
-        __syncthreads();
-        if constexpr (sizeof(T) == 4) {
-            // float-float block reduction in a fixed order (FP32 pipe); the
-            // rare FP64 finishes are folded in first
-            if (used64) {
-                float h = (float)acc_m;
-                ff_add_pair(am_h, am_l, h, (float)(acc_m - (double)h));
-                h = (float)acc_v;
-                ff_add_pair(av_h, av_l, h, (float)(acc_v - (double)h));
-                h = (float)acc_s;
-                ff_add_pair(as_h, as_l, h, (float)(acc_s - (double)h));
-            }
-            float r6[6] = {am_h, am_l, av_h, av_l, as_h, as_l};
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float o6[6];
-#pragma unroll
-                for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
-#pragma unroll
-                for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
-            }
-            float *wred = reinterpret_cast<float *>(red);
-            if ((tid & 31) == 0) {
-#pragma unroll
-                for (int i = 0; i < 6; i++) wred[(tid >> 5) * 6 + i] = r6[i];
-            }
-            __syncthreads();
-            if (tid == 0) {
-                for (int w = 1; w < NT / 32; w++)
-#pragma unroll
-                    for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], wred[w * 6 + i], wred[w * 6 + i + 1]);
-                TilePart p;
-                p.mean = VgKSum{(double)r6[0], (double)r6[1]};
-                p.var = VgKSum{(double)r6[2], (double)r6[3]};
-                p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
-                a.parts[part_slot] = p;
-            }
-        } else {
-            const VgKSum m = vg_block_ksum<NT>(VgKSum{acc_m, 0.0}, red);
-            const VgKSum v = vg_block_ksum<NT>(VgKSum{acc_v, 0.0}, red);
-            const VgKSum sg = vg_block_ksum<NT>(VgKSum{acc_s, 0.0}, red);
-            if (tid == 0) {
-                TilePart p;
-                p.mean = m;
-                p.var = v;
-                p.sigf = sg;
-                a.parts[part_slot] = p;
-            }
-        }
+        emit_partial(part_slot);
         if (nan_local) atomicExch((int *)&a.stats->nan_seen, 1);
         if (use_bins && a.hist_smem) {
             __syncthreads();
@@ -1253,8 +1262,17 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     }
 }
 
+// Resident CTAs per SM the register allocation targets for the fused FP32
+// ridge at dim <= 4: 4 with 2 samples per thread (64 registers; its shared
+// memory then holds no grid table), 2 with 4; 1 (no limit) otherwise.
 template <typename T, int MODE, int KIND, int DIMB, int S>
-__global__ void __launch_bounds__(NT) tile_kernel(IterArgs a, VgParams prm)
+constexpr int tile_min_blocks()
+{
+    return (sizeof(T) == 4 && MODE == MODE_FUSED && KIND == VG_F_RIDGE && DIMB <= 4) ? (S == 2 ? 4 : 2) : 1;
+}
+
+template <typename T, int MODE, int KIND, int DIMB, int S>
+__global__ void __launch_bounds__(NT, tile_min_blocks<T, MODE, KIND, DIMB, S>()) tile_kernel(IterArgs a, VgParams prm)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     tile_body<T, MODE, KIND, DIMB, S>(a, prm, smem, blockIdx.x, gridDim.x, blockIdx.x);
@@ -1276,7 +1294,10 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
     constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
     const int bins = NEED_RED && (a.train || a.train_hc);
     const size_t budget = 200 * 1024;
-    a.table_smem = g_tile_table == 0 ? 0 : 1;
+    // the 4-CTA-per-SM configuration reads the FP32 grid table through L1
+    // (its shared memory then fits four CTAs); others stage it
+    constexpr bool many_ctas = tile_min_blocks<T, MODE, KIND, DIMB, S>() >= 4;
+    a.table_smem = g_tile_table == 0 ? 0 : (g_tile_table == 1 ? 1 : (many_ctas ? 0 : 1));
     a.hist_smem = g_tile_hist == 0 ? 0 : (NEED_RED && a.train);
     SmemPlan p = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, tab_len, bins, NEED_RED);
     if (p.total > budget && a.hist_smem) {
