@@ -151,51 +151,28 @@ static __device__ __noinline__ void cta_alloc(const IterArgs &a, int64_t *scan)
 // reset (pyx:2209-2215).
 static __device__ __noinline__ void cta_finalize(const IterArgs &a, int ngroup, VgKSum *red, int *flag)
 {
+    // the group CTAs' float-float partials and the cut hypercubes, merged
+    // and summed in float-float, converted to FP64 once (FP32 mode)
     const int tid = threadIdx.x;
     vg_stats *st = a.stats;
     const int64_t N = st->neval;
     const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
-    VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
+    float r6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (tid < ngroup && ntiles > 0) {   // the partial sums of each CTA of the group
         const TilePart p = a.parts[tid];
-        cm = p.mean;
-        cv = p.var;
-        cs = p.sigf;
+        ff_unpack(p.mean.s, r6[0], r6[1]);
+        ff_unpack(p.var.s, r6[2], r6[3]);
+        ff_unpack(p.sigf.s, r6[4], r6[5]);
     }
-    for (int64_t t = tid; t < ntiles; t += NT) {
-        const TileRec r = a.recs[2 * t + 1];
-        if (r.h < 0) continue;
-        double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
-        for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
-            const TileRec q = a.recs[2 * t2];
-            if (q.h != r.h) break;
-            const double n2 = n + q.n;
-            const double delta = q.S / q.n - Sx / n;
-            Q = Q + q.Q + delta * delta * (n * q.n / n2);
-            Sx += q.S;
-            D += q.D;
-            n = n2;
-            if (!q.spans) break;
-        }
-        const double vh = __ddiv_rn(__dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D)), __dsub_rn(n, 1.));
-        cm.add(__dadd_rn(Sx, D));
-        cv.add(vh);
-        if (a.adaptive) {
-            const double sg = vg_pow_fast(fabs(vh), a.beta_half);
-            a.sigf[r.h] = sg;
-            cs.add(sg);
-        }
-    }
-    const VgKSum M = vg_block_ksum<NT>(cm, red);
-    const VgKSum V = vg_block_ksum<NT>(cv, red);
-    const VgKSum Sg = vg_block_ksum<NT>(cs, red);
+    for (int64_t t = tid; t < ntiles; t += NT) merge_cut_ff(a, t, ntiles, r6[0], r6[1], r6[2], r6[3], r6[4], r6[5]);
+    ff_block_reduce6<NT>(r6, reinterpret_cast<float *>(red));
     if (tid == 0) {
-        st->mean = M.value();
-        st->var = V.value();
+        st->mean = vg_ff_value(r6[0], r6[1]);
+        st->var = vg_ff_value(r6[2], r6[3]);
         st->sigf_reset = 0;
         *flag = 0;
         if (a.adaptive) {
-            const double ss = Sg.value();
+            const double ss = vg_ff_value(r6[4], r6[5]);
             if (ss > 0) {
                 st->sum_sigf = ss;
             } else {
@@ -284,7 +261,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ IterArgs sa;
     __shared__ int64_t scan[NT];
-    __shared__ VgKSum red[NT / 32 + 2];
+    __shared__ VgKSum red[NT / 32 + 4];   // also 6 floats per warp for float-float reductions
     __shared__ int s_q, s_flag;
     const int tid = threadIdx.x;
     const int G = group > 1 ? group : 1;

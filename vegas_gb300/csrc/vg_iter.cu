@@ -266,6 +266,50 @@ __device__ __forceinline__ void finalize_totals(const IterArgs &a, int64_t nblk,
         for (int64_t h = threadIdx.x; h < a.H; h += FIN_TILES) a.sigf[h] = 1.0;
 }
 
+// The iteration's results from the stats fields (mean, var, sum_sigf) and
+// the constant-integrand reset (pyx:2209-2215); thread 0 has the sums.
+__device__ __forceinline__ void finalize_store(const IterArgs &a, double mean, double var, double ss, int *reset)
+{
+    if (threadIdx.x == 0) {
+        vg_stats *st = a.stats;
+        st->mean = mean;
+        st->var = var;
+        *reset = 0;
+        st->sigf_reset = 0;
+        if (a.adaptive) {
+            if (ss > 0) {
+                st->sum_sigf = ss;
+            } else {   // integrand looks constant: even distribution
+                st->sum_sigf = (double)a.H;
+                st->sigf_reset = 1;
+                *reset = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (*reset)
+        for (int64_t h = threadIdx.x; h < a.H; h += blockDim.x) a.sigf[h] = 1.0;
+}
+
+// FP32 mode, stage 2: the blocks' float-float partials summed in float-float
+// in block order (lane-strided, then a fixed tree), converted to FP64 once.
+__device__ __forceinline__ void finalize_totals_ff(const IterArgs &a, int64_t nblk, int *reset)
+{
+    float r6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int64_t b = threadIdx.x; b < nblk; b += FIN_TILES) {
+        const TilePart p = a.part2[b];
+        float h, l;
+        ff_unpack(p.mean.s, h, l);
+        ff_add_pair(r6[0], r6[1], h, l);
+        ff_unpack(p.var.s, h, l);
+        ff_add_pair(r6[2], r6[3], h, l);
+        ff_unpack(p.sigf.s, h, l);
+        ff_add_pair(r6[4], r6[5], h, l);
+    }
+    ff_block_reduce6<FIN_TILES>(r6, nullptr);
+    finalize_store(a, vg_ff_value(r6[0], r6[1]), vg_ff_value(r6[2], r6[3]), vg_ff_value(r6[4], r6[5]), reset);
+}
+
 // Stage 1, and stage 2 in the block that finishes last (a counter the
 // allocation resets; the partials are read back in block order, so the
 // result does not depend on which block that is).
@@ -281,95 +325,23 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
     const int64_t nblk = (nwork + FIN_TILES - 1) / FIN_TILES;
     if (FAST && (int64_t)blockIdx.x < nblk) {
         // FP32 mode: the tile partials and the cut hypercubes' records hold
-        // float-float values; merged and summed in float-float (FP32 pipe),
-        // one FP64 partial per block for the FP64 sum of stage 2
-        float mh = 0.f, ml = 0.f, vh_ = 0.f, vl_ = 0.f, sh = 0.f, sl = 0.f;
+        // packed float-float values; merged and summed in float-float
+        // (FP32 pipe, no FP64 instruction on the path)
+        float r6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int64_t t = (int64_t)blockIdx.x * FIN_TILES + threadIdx.x;
         if (t < a.ncta && ntiles > 0) {   // partial sums of the reduction CTA t
             const TilePart p = a.parts[t];
-            mh = (float)p.mean.s;
-            ml = (float)p.mean.c;
-            vh_ = (float)p.var.s;
-            vl_ = (float)p.var.c;
-            sh = (float)p.sigf.s;
-            sl = (float)p.sigf.c;
+            ff_unpack(p.mean.s, r6[0], r6[1]);
+            ff_unpack(p.var.s, r6[2], r6[3]);
+            ff_unpack(p.sigf.s, r6[4], r6[5]);
         }
-        if (t < ntiles) {
-            const TileRec r = a.recs[2 * t + 1];
-            if (r.h >= 0) {
-                float n = (float)r.n, Sh, Sl, Qh, Ql, Dh, Dl;
-                ff_from_double(r.S, Sh, Sl);
-                ff_from_double(r.Q, Qh, Ql);
-                ff_from_double(r.D, Dh, Dl);
-                bool big = !(fabsf(Qh) < 1e30f);
-                for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
-                    const TileRec q = a.recs[2 * t2];
-                    if (q.h != r.h) break;
-                    const float qn = (float)q.n, n2 = n + qn;
-                    float qSh, qSl, qQh, qQl, qDh, qDl;
-                    ff_from_double(q.S, qSh, qSl);
-                    ff_from_double(q.Q, qQh, qQl);
-                    ff_from_double(q.D, qDh, qDl);
-                    big |= !(fabsf(qQh) < 1e30f);
-                    // Chan et al.: Q = Q1 + Q2 + (m2 - m1)^2 n1 n2 / (n1 + n2)
-                    float m1h, m1l, m2h, m2l, wph, wpl, wh, wl, ddh, ddl, th, tl;
-                    ff_div_f(Sh, Sl, n, m1h, m1l);
-                    ff_div_f(qSh, qSl, qn, m2h, m2l);
-                    ff_add_pair(m2h, m2l, -m1h, -m1l);
-                    wph = __fmul_rn(n, qn);
-                    wpl = __fmaf_rn(n, qn, -wph);
-                    ff_div_f(wph, wpl, n2, wh, wl);
-                    ff_sqr(m2h, m2l, ddh, ddl);
-                    ff_mul(ddh, ddl, wh, wl, th, tl);
-                    ff_add_pair(Qh, Ql, qQh, qQl);
-                    ff_add_pair(Qh, Ql, th, tl);
-                    ff_add_pair(Sh, Sl, qSh, qSl);
-                    ff_add_pair(Dh, Dl, qDh, qDl);
-                    n = n2;
-                    if (!q.spans) break;
-                }
-                float vh, vl;
-                if (!big) {
-                    float nqh, nql, d2h, d2l;
-                    ff_mul_f(Qh, Ql, n, nqh, nql);
-                    ff_sqr(Dh, Dl, d2h, d2l);
-                    ff_add_pair(nqh, nql, -d2h, -d2l);
-                    ff_div_f(nqh, nql, n - 1.f, vh, vl);
-                } else {   // squares beyond the float range: this hypercube in FP64
-                    const double Q = vg_ff_value(Qh, Ql), D = vg_ff_value(Dh, Dl), nd = (double)n;
-                    ff_from_double(vgadapt::div_fast(__dsub_rn(__dmul_rn(nd, Q), __dmul_rn(D, D)), nd - 1.0),
-                                   vh, vl);
-                }
-                if (a.train_hc) {   // adapt_to_errors: train at the hypercube's last sample
-                    unsigned short b[VG_MAX_DIM];
-                    last_sample_bins<float>(a, r.h, b);
-                    train_hcube(a, b, fabs(vg_ff_value(vh, vl)));
-                }
-                ff_add_pair(Sh, Sl, Dh, Dl);
-                ff_add_pair(mh, ml, Sh, Sl);
-                ff_add_pair(vh_, vl_, vh, vl);
-                if (a.adaptive) {
-                    const float av = fabsf(vh);
-                    const float sg = av > 0.f ? vg_ex2_approx((float)a.beta_half * vg_lg2_approx(av)) : 0.f;
-                    a.sigf[r.h] = (double)sg;
-                    vg_ff_add(sh, sl, sg);
-                }
-            }
-        }
-        float r6[6] = {mh, ml, vh_, vl_, sh, sl};
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            float o6[6];
-#pragma unroll
-            for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
-#pragma unroll
-            for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
-        }
+        if (t < ntiles) merge_cut_ff(a, t, ntiles, r6[0], r6[1], r6[2], r6[3], r6[4], r6[5]);
+        ff_block_reduce6<FIN_TILES>(r6, nullptr);
         if (threadIdx.x == 0) {
             TilePart p;
-            p.mean = VgKSum{(double)r6[0], (double)r6[1]};
-            p.var = VgKSum{(double)r6[2], (double)r6[3]};
-            p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
+            p.mean = VgKSum{ff_pack(r6[0], r6[1]), 0.0};
+            p.var = VgKSum{ff_pack(r6[2], r6[3]), 0.0};
+            p.sigf = VgKSum{ff_pack(r6[4], r6[5]), 0.0};
             a.part2[blockIdx.x] = p;
         }
     } else if ((int64_t)blockIdx.x < nblk) {
@@ -435,7 +407,8 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
     if (!s_last) return;
     __threadfence();
     if (threadIdx.x == 0) *a.fin_counter = 0u;
-    finalize_totals(a, nblk, red, &s_reset);
+    if (FAST) finalize_totals_ff(a, nblk, &s_reset);
+    else finalize_totals(a, nblk, red, &s_reset);
 }
 
 // ================================================================ host

@@ -212,6 +212,51 @@ __device__ __forceinline__ void ff_add_pair(float &ah, float &al, float bh, floa
     al = __fsub_rn(e, __fsub_rn(ah, s));
 }
 
+// FP32 mode keeps float-float values in the FP64 fields of the tile records
+// and partial sums as bit patterns (low word = head, high word = tail), so
+// storing and loading them moves integers -- GB300's FP64 pipe is slow, and
+// a single warp waits hundreds of cycles per dependent FP64 instruction.
+__device__ __forceinline__ double ff_pack(float h, float l)
+{
+    return __hiloint2double(__float_as_int(l), __float_as_int(h));
+}
+
+__device__ __forceinline__ void ff_unpack(double d, float &h, float &l)
+{
+    h = __int_as_float(__double2loint(d));
+    l = __int_as_float(__double2hiint(d));
+}
+
+// Block-wide float-float reduction of six floats (three float-float values)
+// in a fixed order; the result is valid in thread 0.  scratch: 6 * NTB/32
+// floats of shared memory.
+template <int NTB>
+__device__ __forceinline__ void ff_block_reduce6(float (&r6)[6], float *scratch)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        float o6[6];
+#pragma unroll
+        for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
+#pragma unroll
+        for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
+    }
+    if (NTB > 32) {
+        const int tid = threadIdx.x;
+        if ((tid & 31) == 0) {
+#pragma unroll
+            for (int i = 0; i < 6; i++) scratch[(tid >> 5) * 6 + i] = r6[i];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < NTB / 32; w++)
+#pragma unroll
+                for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], scratch[w * 6 + i], scratch[w * 6 + i + 1]);
+        }
+        __syncthreads();
+    }
+}
+
 // (h, l) = (ah, al) * b in float-float (the head's product error by fma).
 __device__ __forceinline__ void ff_mul_f(float ah, float al, float b, float &h, float &l)
 {
@@ -479,7 +524,7 @@ __device__ __forceinline__ void train_hcube(const IterArgs &a, const unsigned sh
 // uniforms exactly as the tile kernels form them (for hypercubes that the
 // finalize merges across tiles).
 template <typename T>
-__device__ void last_sample_bins(const IterArgs &a, int64_t h, unsigned short *bins)
+static __device__ void last_sample_bins(const IterArgs &a, int64_t h, unsigned short *bins)
 {
     const int dim = a.dim;
     const int64_t ig = a.offsets[h] + a.neval_h[h] - 1;
@@ -498,6 +543,75 @@ __device__ void last_sample_bins(const IterArgs &a, int64_t h, unsigned short *b
         T yd, yn, yfl;
         const int iy = sample_y<T>(y0, (float)y0, u[d], ns, 1.f / (float)ns, K, (float)K, yd, yn, yfl);
         bins[d] = sample_bin<T>(yd, iy, K);
+    }
+}
+
+// FP32 mode: the hypercube whose first piece is the tail record of tile t,
+// merged in float-float with its pieces in the following tiles (Chan et
+// al.'s parallel-variance update: Q = Q1 + Q2 + (m2 - m1)^2 n1 n2 / (n1 +
+// n2)).  Adds its mean S + D and variance (nQ - D^2)/(n - 1) to (m, v), sets
+// its sigf and adds it to s, and trains it under adapt_to_errors.
+static __device__ __noinline__ void merge_cut_ff(const IterArgs &a, int64_t t, int64_t ntiles, float &mh, float &ml, float &vh_,
+                             float &vl_, float &sh, float &sl)
+{
+    const TileRec r = a.recs[2 * t + 1];
+    if (r.h < 0) return;
+    float n = (float)r.pad, Sh, Sl, Qh, Ql, Dh, Dl;
+    ff_unpack(r.S, Sh, Sl);
+    ff_unpack(r.Q, Qh, Ql);
+    ff_unpack(r.D, Dh, Dl);
+    bool big = !(fabsf(Qh) < 1e30f);
+    for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+        const TileRec q = a.recs[2 * t2];
+        if (q.h != r.h) break;
+        const float qn = (float)q.pad, n2 = n + qn;
+        float qSh, qSl, qQh, qQl, qDh, qDl;
+        ff_unpack(q.S, qSh, qSl);
+        ff_unpack(q.Q, qQh, qQl);
+        ff_unpack(q.D, qDh, qDl);
+        big |= !(fabsf(qQh) < 1e30f);
+        float m1h, m1l, m2h, m2l, wh, wl, ddh, ddl, th, tl;
+        ff_div_f(Sh, Sl, n, m1h, m1l);
+        ff_div_f(qSh, qSl, qn, m2h, m2l);
+        ff_add_pair(m2h, m2l, -m1h, -m1l);
+        const float wph = __fmul_rn(n, qn);
+        const float wpl = __fmaf_rn(n, qn, -wph);
+        ff_div_f(wph, wpl, n2, wh, wl);
+        ff_sqr(m2h, m2l, ddh, ddl);
+        ff_mul(ddh, ddl, wh, wl, th, tl);
+        ff_add_pair(Qh, Ql, qQh, qQl);
+        ff_add_pair(Qh, Ql, th, tl);
+        ff_add_pair(Sh, Sl, qSh, qSl);
+        ff_add_pair(Dh, Dl, qDh, qDl);
+        n = n2;
+        if (!q.spans) break;
+    }
+    float vh, vl;
+    if (!big) {
+        float nqh, nql, d2h, d2l;
+        ff_mul_f(Qh, Ql, n, nqh, nql);
+        ff_sqr(Dh, Dl, d2h, d2l);
+        ff_add_pair(nqh, nql, -d2h, -d2l);
+        ff_div_f(nqh, nql, n - 1.f, vh, vl);
+    } else {   // squares beyond the float range: this hypercube in FP64
+        const double Q = vg_ff_value(Qh, Ql), D = vg_ff_value(Dh, Dl), nd = (double)n;
+        const double v = vg_div<float>(__dsub_rn(__dmul_rn(nd, Q), __dmul_rn(D, D)), nd - 1.0);
+        vh = (float)v;
+        vl = (float)(v - (double)vh);
+    }
+    if (a.train_hc) {   // adapt_to_errors: train at the hypercube's last sample
+        unsigned short b[VG_MAX_DIM];
+        last_sample_bins<float>(a, r.h, b);
+        train_hcube(a, b, fabs(vg_ff_value(vh, vl)));
+    }
+    ff_add_pair(Sh, Sl, Dh, Dl);
+    ff_add_pair(mh, ml, Sh, Sl);
+    ff_add_pair(vh_, vl_, vh, vl);
+    if (a.adaptive) {
+        const float av = fabsf(vh);
+        const float sg = av > 0.f ? vg_ex2_approx((float)a.beta_half * vg_lg2_approx(av)) : 0.f;
+        a.sigf[r.h] = (double)sg;
+        vg_ff_add(sh, sl, sg);
     }
 }
 
@@ -644,28 +758,12 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 ff_add_pair(as_h, as_l, h, (float)(acc_s - (double)h));
             }
             float r6[6] = {am_h, am_l, av_h, av_l, as_h, as_l};
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float o6[6];
-#pragma unroll
-                for (int i = 0; i < 6; i++) o6[i] = __shfl_down_sync(0xffffffffu, r6[i], off);
-#pragma unroll
-                for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], o6[i], o6[i + 1]);
-            }
-            float *wred = reinterpret_cast<float *>(red);
-            if ((tid & 31) == 0) {
-#pragma unroll
-                for (int i = 0; i < 6; i++) wred[(tid >> 5) * 6 + i] = r6[i];
-            }
-            __syncthreads();
-            if (tid == 0) {
-                for (int w = 1; w < NT / 32; w++)
-#pragma unroll
-                    for (int i = 0; i < 6; i += 2) ff_add_pair(r6[i], r6[i + 1], wred[w * 6 + i], wred[w * 6 + i + 1]);
+            ff_block_reduce6<NT>(r6, reinterpret_cast<float *>(red));
+            if (tid == 0) {   // float-float partials, packed
                 TilePart p;
-                p.mean = VgKSum{(double)r6[0], (double)r6[1]};
-                p.var = VgKSum{(double)r6[2], (double)r6[3]};
-                p.sigf = VgKSum{(double)r6[4], (double)r6[5]};
+                p.mean = VgKSum{ff_pack(r6[0], r6[1]), 0.0};
+                p.var = VgKSum{ff_pack(r6[2], r6[3]), 0.0};
+                p.sigf = VgKSum{ff_pack(r6[4], r6[5]), 0.0};
                 a.parts[slot] = p;
             }
             am_h = am_l = av_h = av_l = as_h = as_l = 0.f;
@@ -1098,17 +1196,15 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
             const bool ends_after = ostart + nh > tile_start + tile_len;
             if (!starts_before && !ends_after) {
                 finish(h, nin, sg2.x, sg2.y, dq.x, dq.y, dq.z, dq.w, 0, 0.0);
-            } else {
-                const double Sseg = vg_ff_value(sg2.x, sg2.y);
-                const double Dx = vg_ff_value(dq.x, dq.y), Qx = vg_ff_value(dq.z, dq.w);
+            } else {   // a piece of a hypercube cut by the tile: float-float record
                 TileRec r;
                 r.h = h;
-                r.n = (double)nin;
-                r.S = Sseg;
-                r.Q = Qx;
-                r.D = Dx;
+                r.n = 0.0;
+                r.S = ff_pack(sg2.x, sg2.y);
+                r.Q = ff_pack(dq.z, dq.w);
+                r.D = ff_pack(dq.x, dq.y);
                 r.spans = (starts_before && ends_after) ? 1 : 0;
-                r.pad = 0;
+                r.pad = nin;
                 a.recs[2 * tile + (starts_before ? 0 : 1)] = r;
             }
         }
