@@ -456,7 +456,9 @@ def gpu_arm(args):
                      'algorithmic': 'ex2 evaluated per launch: %d (the terms that can be nonzero '
                                     'in FP32; all M=1000 terms per evaluation = %d, the rest are '
                                     'exactly zero and skipped)' % (executed, ex2_per_launch),
-                     'frac_all_terms': ex2_per_launch / kern_s / 1e9 / peak,
+                     # the rate the reference's algorithm (all M terms per evaluation)
+                     # would need to match this kernel; above 1: exactly-zero terms skipped
+                     'reference_terms_equivalent_frac': ex2_per_launch / kern_s / 1e9 / peak,
                      'peak_source': 'MUFU ex2 probe kernel on this GPU (vg_probe_mufu_ex2)'},
         'clocks': clk,
         'time_to_1e-4': tta,
