@@ -916,6 +916,9 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
 __device__ int g_flow_status;   // set to VG_ERR_TIMEOUT when a bounded wait gave up
 
 constexpr int UST_MAX = 16;      // 128-row sub-tiles per super-tile
+constexpr int UNT = 512;         // threads of the tcgen05 pass: 16 warps
+constexpr int UNH = UNT / FROWS; // column groups of threads (4): H columns and coordinates per group
+constexpr int UCOL = FH / UNH;   // H columns per thread in the epilogues (32)
 
 struct UmmaPlan {
     int ST;                      // sub-tiles per super-tile
@@ -937,23 +940,27 @@ __host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
     p.ob2 = o; o += sizeof(float) * FH;
     p.ob3 = o; o += sizeof(float) * 8 * (2 * FMAXK + 1);
     p.oZ = o;  o += sizeof(float) * (size_t)ST * FROWS * p.zst;
-    p.oLD = o; o += sizeof(float) * 2 * (size_t)ST * FROWS;
+    p.oLD = o; o += sizeof(float) * UNH * (size_t)ST * FROWS;
     p.total = o + 1024;          // + alignment slack of the dynamic base
     return p;
 }
 
 // Inference through all layers on the 5th-generation tensor cores.  One CTA
-// (8 warps) per SM; a super-tile of ST x 128 rows stays in shared memory
+// (16 warps) per SM; a super-tile of ST x 128 rows stays in shared memory
 // while the layers go by, so each layer's weights are fetched (bulk copy)
 // once per super-tile.  Per 128-row sub-tile and layer:
 //   H1 = relu(W1 z_A + b1)           FP32 FMA, written as the bf16 A operand
 //   TMEM[0:128)   = H1 W2^T           tcgen05.mma, M=128 N=128 K=128
 //   H2 = relu(TMEM + b2)              tcgen05.ld epilogue -> bf16 A operand
-//   TMEM[buf]     = H2 W3[g]^T        two transformed coordinates per MMA
-//                                     group, double-buffered in TMEM
-//   spline of each (row, coordinate)  registers; thread = (row, half)
+//   TMEM[128:...) = H2 W3[g]^T        four transformed coordinates per group
+//                                     (two MMAs of two coordinates)
+//   spline of each (row, coordinate)  registers; thread = (row, column
+//                                     group), one spline per thread and group
+// The splines (65 exponentials and a bin search each) dominate and are
+// latency-bound: 16 warps, one (row, coordinate) each, hide twice the
+// latency of the former 8 warps doing two each.
 template <int K, int DIR>
-__global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, const float *__restrict__ theta,
+__global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, const float *__restrict__ theta,
                                                                const __nv_bfloat16 *__restrict__ mirror,
                                                                int64_t n, const float *__restrict__ zin,
                                                                float *__restrict__ zout,
@@ -986,7 +993,7 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
     umma::fence_after_sync();
     const uint32_t tmem = tslot;
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-    uint32_t ph_w = 0, ph_h = 0, ph_o0 = 0, ph_o1 = 0, ph_d = 0;
+    uint32_t ph_w = 0, ph_h = 0, ph_o0 = 0, ph_d = 0;
     const int64_t rows_per = (int64_t)ST * FROWS;
     const int64_t nsuper = (n + rows_per - 1) / rows_per;
     bool aborted = false;
@@ -994,14 +1001,13 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
         const int64_t r0 = sup * rows_per;
         const int nrows = (int)((n - r0) < rows_per ? (n - r0) : rows_per);
         const int nsub = (nrows + FROWS - 1) / FROWS;
-        for (int i = tid; i < nsub * FROWS * dim; i += FNT) {
+        for (int i = tid; i < nsub * FROWS * dim; i += UNT) {
             const int rr = i / dim, d = i % dim;
             sZ[rr * zst + d] = rr < nrows ? zin[(r0 + rr) * dim + d] : 0.5f;
         }
-        for (int i = tid; i < nsub * FROWS; i += FNT) {
-            sLD[i] = 0.f;                          // log-det partial of the h = 0 threads
-            sLD[(size_t)ST * FROWS + i] = 0.f;     // ... of the h = 1 threads
-        }
+        for (int i = tid; i < nsub * FROWS; i += UNT)
+#pragma unroll
+            for (int q = 0; q < UNH; q++) sLD[(size_t)q * ST * FROWS + i] = 0.f;   // log-det partial of column group q
         __syncthreads();
         for (int step = 0; step < g.L && !aborted; step++) {
             const int l = DIR == 0 ? step : g.L - 1 - step;
@@ -1017,15 +1023,15 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     umma::bulk_g2s(umma::smem_u32(sW3) + off, (const uint8_t *)(mirror + y.mU3) + off, sz, bar_w);
                 }
             }
-            for (int i = tid; i < FH * 8; i += FNT) {   // W1 padded to 8 columns: [128][8]
+            for (int i = tid; i < FH * 8; i += UNT) {   // W1 padded to 8 columns: [128][8]
                 const int c = i >> 3, a = i & 7;
                 sW1[i] = a < dA ? theta[y.oW1 + c * dA + a] : 0.f;
             }
-            for (int i = tid; i < FH; i += FNT) {
+            for (int i = tid; i < FH; i += UNT) {
                 sb1[i] = theta[y.ob1 + i];
                 sb2[i] = theta[y.ob2 + i];
             }
-            for (int i = tid; i < y.dB * NR; i += FNT) sb3[i] = theta[y.ob3 + i];
+            for (int i = tid; i < y.dB * NR; i += UNT) sb3[i] = theta[y.ob3 + i];
             // one thread waits on the mbarrier; the others park at the CTA barrier
             if (tid == 0 && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
             ph_w ^= 1;
@@ -1034,7 +1040,7 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
             for (int s = 0; s < nsub; s++) {
                 float *Zs = sZ + (size_t)s * FROWS * zst;
                 if (zl != nullptr) {
-                    for (int i = tid; i < FROWS * dim; i += FNT) {
+                    for (int i = tid; i < FROWS * dim; i += UNT) {
                         const int rr = i / dim, d = i % dim;
                         const int64_t grow = r0 + (int64_t)s * FROWS + rr;
                         if (grow < n) zl[((int64_t)l * n + grow) * dim + d] = Zs[rr * zst + d];
@@ -1047,7 +1053,7 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? Zs[r * zst + y.A[a]] : 0.f;
                     const bool wide = dA > 4;
 #pragma unroll 2
-                    for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 8) {
+                    for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
                         float v[8];
                         const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
                         const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
@@ -1091,7 +1097,7 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                 __syncthreads();
                 umma::fence_after_sync();
                 // ---- H2 epilogue: TMEM -> +b2, relu -> A operand
-                for (int c0 = 64 * h; c0 < 64 * h + 64; c0 += 32) {
+                for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 32) {
                     float v[32];
                     umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
 #pragma unroll
@@ -1111,35 +1117,31 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                 umma::fence_before_sync();
                 __syncthreads();
                 if (abort_flag) { aborted = true; break; }
-                // ---- output layer in groups of two coordinates, double-buffered in TMEM
-                const int ngroups = (y.dB + 1) / 2;
-                auto issue = [&](int gi) {
-                    const int ncoord = (2 * gi + 1 < y.dB) ? 2 : 1;
-                    const int N = ncoord == 2 ? 2 * CH : (CH + 15) / 16 * 16;
-                    const uint32_t dcol = (uint32_t)(FH + (gi & 1) * 2 * CH);
-                    umma::gemm_128xN(tmem + dcol, umma::smem_u32(sA),
-                                     umma::smem_u32(sW3) + (uint32_t)(2 * gi * CH) * 128u, N, FH, y.NP, 0);
-                    umma::mma_commit(bar_o0 + 8u * (uint32_t)(gi & 1));
-                };
-                if (tid == 0) {
-                    umma::fence_after_sync();
-                    issue(0);
-                    if (ngroups > 1) issue(1);
-                }
+                // ---- output layer in groups of UNH coordinates (one per column
+                // group of threads): two MMAs of up to two coordinates each
+                const int ngroups = (y.dB + UNH - 1) / UNH;
                 for (int gi = 0; gi < ngroups; gi++) {
-                    const int buf = gi & 1;
                     if (tid == 0) {
-                        const bool okw = buf == 0 ? umma::mbar_wait(bar_o0, ph_o0) : umma::mbar_wait(bar_o0 + 8u, ph_o1);
-                        if (!okw) abort_flag = 1;
+                        umma::fence_after_sync();
+#pragma unroll
+                        for (int p = 0; p < UNH / 2; p++) {
+                            const int first = UNH * gi + 2 * p;
+                            if (first >= y.dB) break;
+                            const int ncoord = (first + 1 < y.dB) ? 2 : 1;
+                            const int N = ncoord == 2 ? 2 * CH : (CH + 15) / 16 * 16;
+                            umma::gemm_128xN(tmem + (uint32_t)(FH + 2 * p * CH), umma::smem_u32(sA),
+                                             umma::smem_u32(sW3) + (uint32_t)(first * CH) * 128u, N, FH, y.NP, 0);
+                        }
+                        umma::mma_commit(bar_o0);
+                        if (!umma::mbar_wait(bar_o0, ph_o0)) abort_flag = 1;
                     }
-                    if (buf == 0) ph_o0 ^= 1;
-                    else ph_o1 ^= 1;
+                    ph_o0 ^= 1;
                     __syncthreads();
                     const bool ok = abort_flag == 0;
                     umma::fence_after_sync();
-                    const int j = 2 * gi + h;
+                    const int j = UNH * gi + h;
                     if (ok && j < y.dB) {
-                        const uint32_t col = (uint32_t)(FH + buf * 2 * CH + h * CH);
+                        const uint32_t col = (uint32_t)(FH + h * CH);
                         float o[NR];
                         {
                             float v[32];
@@ -1166,21 +1168,23 @@ __global__ void __launch_bounds__(FNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     }
                     umma::fence_before_sync();
                     __syncthreads();
-                    if (tid == 0 && gi + 2 < ngroups) {
-                        umma::fence_after_sync();
-                        issue(gi + 2);
-                    }
+                    if (!ok) break;
                 }
                 if (abort_flag) { aborted = true; break; }
             }
             __syncthreads();
         }
         if (aborted) break;
-        for (int i = tid; i < nrows * dim; i += FNT) {
+        for (int i = tid; i < nrows * dim; i += UNT) {
             const int rr = i / dim, d = i % dim;
             zout[(r0 + rr) * dim + d] = sZ[rr * zst + d];
         }
-        for (int rr = tid; rr < nrows; rr += FNT) logdet[r0 + rr] = sLD[rr] + sLD[(size_t)ST * FROWS + rr];
+        for (int rr = tid; rr < nrows; rr += UNT) {
+            float ld = 0.f;
+#pragma unroll
+            for (int q = 0; q < UNH; q++) ld += sLD[(size_t)q * ST * FROWS + rr];
+            logdet[r0 + rr] = ld;
+        }
         __syncthreads();
     }
     // drain: every MMA issued by thread 0 has completed before TMEM is freed
@@ -1321,10 +1325,10 @@ static int flow_pass_umma_k(const FlowGeom &g, const vg_flow *fl, int dir, int64
     int64_t grid = (int64_t)vg_num_sms();
     if (grid > nsuper) grid = nsuper;
     if (dir == 0)
-        flow_pass_umma_kernel<K, 0><<<(unsigned)grid, FNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+        flow_pass_umma_kernel<K, 0><<<(unsigned)grid, UNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
                                                                        n, zin, zout, logdet, zl, ST);
     else
-        flow_pass_umma_kernel<K, 1><<<(unsigned)grid, FNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
+        flow_pass_umma_kernel<K, 1><<<(unsigned)grid, UNT, smem, st>>>(g, fl->theta, (const __nv_bfloat16 *)fl->mirror,
                                                                        n, zin, zout, logdet, zl, ST);
     cudaError_t e = cudaGetLastError();
     *rc = e == cudaSuccess ? VG_OK : vg_fail(VG_ERR_CUDA, "flow umma launch: %s", cudaGetErrorString(e));
