@@ -811,9 +811,9 @@ __global__ void flow_adam_kernel(int64_t np, float *__restrict__ theta, const fl
 template <int K, int DIR>
 __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, float &lp)
 {
-    // Written for instruction-level parallelism (8 warps per SM): every
-    // reduction runs as 4 independent chains, and the bin search runs per
-    // block of 8 bins in parallel, the first block with a hit winning.
+    // Written for instruction-level parallelism: every reduction runs as 4
+    // independent chains; the bin search finds the block of 8 bins first,
+    // then scans only that block.
     static_assert(K % 8 == 0, "K must be a multiple of 8");
     constexpr int NB = K / 8;
     constexpr float c1 = 1.f - K * EPS_W;
@@ -863,39 +863,40 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
     }
     const float Z = Ps[NB - 1] + PB[NB - 1];
     const float t = DIR == 0 ? x : x * Z;
-    // per-block search
-    float bW[NB], bu[NB], bu1[NB], bE[NB], bP[NB];
-    bool bf[NB];
+    // two-level search: the block of 8 bins that holds t (compares of the
+    // block prefixes), then a scan of that block's 8 bins, whose values are
+    // selected from the NB blocks' registers (no dynamic register indexing)
+    int bsel = 0;
 #pragma unroll
-    for (int b = 0; b < NB; b++) {
-        float E = Es[b], P = Ps[b];
-        bool f = false;
-        const int kl = 8 * b + 7;   // default: last bin of the block
-        float cW = o[kl], cu = o[K + kl], cu1 = o[K + kl + 1], cE = Es[b] + EB[b] - o[kl],
-              cP = Ps[b] + PB[b] - seg[kl];
+    for (int b = 1; b < NB; b++) bsel += (DIR == 0 ? (t >= Es[b]) : (t >= Ps[b])) ? 1 : 0;
+    float E = Es[0], P = Ps[0];
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int k = 8 * b + q;
-            const bool here = !f && (DIR == 0 ? (t < E + o[k]) : (t < P + seg[k]));
-            cW = here ? o[k] : cW;
-            cu = here ? o[K + k] : cu;
-            cu1 = here ? o[K + k + 1] : cu1;
-            cE = here ? E : cE;
-            cP = here ? P : cP;
-            f = f || here;
-            E += o[k];
-            P += seg[k];
-        }
-        bW[b] = cW; bu[b] = cu; bu1[b] = cu1; bE[b] = cE; bP[b] = cP; bf[b] = f;
+    for (int b = 1; b < NB; b++) {
+        E = bsel == b ? Es[b] : E;
+        P = bsel == b ? Ps[b] : P;
     }
-    float Wb = bW[NB - 1], ub = bu[NB - 1], ub1 = bu1[NB - 1], Eb = bE[NB - 1], Pb = bP[NB - 1];
+    float Wb = 0.f, ub = 0.f, ub1 = 0.f, Eb = 0.f, Pb = 0.f;
+    bool f = false;
 #pragma unroll
-    for (int b = NB - 2; b >= 0; b--) {   // the first block with a hit wins
-        Wb = bf[b] ? bW[b] : Wb;
-        ub = bf[b] ? bu[b] : ub;
-        ub1 = bf[b] ? bu1[b] : ub1;
-        Eb = bf[b] ? bE[b] : Eb;
-        Pb = bf[b] ? bP[b] : Pb;
+    for (int q = 0; q < 8; q++) {
+        float wq = o[q], sq = seg[q], uq = o[K + q], uq1 = o[K + q + 1];
+#pragma unroll
+        for (int b = 1; b < NB; b++) {
+            wq = bsel == b ? o[8 * b + q] : wq;
+            sq = bsel == b ? seg[8 * b + q] : sq;
+            uq = bsel == b ? o[K + 8 * b + q] : uq;
+            uq1 = bsel == b ? o[K + 8 * b + q + 1] : uq1;
+        }
+        // the last bin of the block takes t when no earlier bin did
+        const bool here = !f && (q == 7 || (DIR == 0 ? (t < E + wq) : (t < P + sq)));
+        Wb = here ? wq : Wb;
+        ub = here ? uq : ub;
+        ub1 = here ? uq1 : ub1;
+        Eb = here ? E : Eb;
+        Pb = here ? P : Pb;
+        f = f || here;
+        E += wq;
+        P += sq;
     }
     float al, xo;
     if (DIR == 0) {
