@@ -604,47 +604,63 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
         const int m0 = 32 * (w8 & 3), n0 = 64 * (w8 >> 2);
         float dh2[2][8][4];
         zero_acc(dh2);
-        for (int j = 0; j < y.dB; j++) {
-            flow_out(g, y, theta, mirror, sm, j, 1);
-            const int r = tid;   // threads 0..127: one row each
-            if (tid < FROWS) {
-                float *o = sm.OUT + r * sm.ostr;
-                float Z;
-                spline_prepare(o, K, Z);
-                SplineState st;
-                const int col = y.B[j];
-                const float xin = sm.Z[r * FMAXD + col];
-                spline_cdf(o, K, Z, xin, st);
-                const float gC = sm.G[r * FMAXD + col];
-                const float gL = sm.LD[r];
-                float lterm = (r0 + r < n) ? gL * (__logf(st.pdfu) - __logf(Z)) : 0.f;
+        // coordinates in pairs: the output GEMM of two coordinates on all 8
+        // warps, their splines' backward on all 256 threads (thread = row,
+        // coordinate), dL/dout left in OUT; then per coordinate dOUT (bf16)
+        // -> global, db3, dH2 += dOUT_j W3_j
+        for (int j0 = 0; j0 < y.dB; j0 += 2) {
+            const int nj = y.dB - j0 < 2 ? y.dB - j0 : 2;
+            flow_out(g, y, theta, mirror, sm, j0, nj);
+            {
+                const int r = tid & (FROWS - 1), half = tid >> 7;
+                float lterm = 0.f;
+                if (half < nj) {
+                    const int j = j0 + half;
+                    float *o = sm.OUT + r * sm.ostr + half * g.CH;
+                    float Z;
+                    spline_prepare(o, K, Z);
+                    SplineState st;
+                    const int col = y.B[j];
+                    const float xin = sm.Z[r * FMAXD + col];
+                    spline_cdf(o, K, Z, xin, st);
+                    const float gC = sm.G[r * FMAXD + col];
+                    const float gL = sm.LD[r];
+                    lterm = (r0 + r < n) ? gL * (__logf(st.pdfu) - __logf(Z)) : 0.f;
+                    const float gx = spline_backward(o, K, st, gC, gL);
+                    sm.G[r * FMAXD + col] = gx;   // becomes dL/d(layer input) for B coordinates
+                }
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) lterm += __shfl_xor_sync(0xffffffffu, lterm, off);
                 if ((tid & 31) == 0 && lterm != 0.f) atomicAdd(loss, (double)lterm);
-                const float gx = spline_backward(o, K, st, gC, gL);
-                sm.G[r * FMAXD + col] = gx;   // becomes dL/d(layer input) for B coordinates
-                for (int q = 0; q < sm.dstr; q += 2) {
+            }
+            __syncthreads();
+            for (int jj = 0; jj < nj; jj++) {
+                const int j = j0 + jj;
+                // dL/dout of coordinate j as bf16
+                for (int i = tid; i < FROWS * (sm.dstr / 2); i += FNT) {
+                    const int r = i / (sm.dstr / 2), q = 2 * (i % (sm.dstr / 2));
+                    const float *o = sm.OUT + r * sm.ostr + jj * g.CH;
                     const float v0 = q < nreal ? o[q] : 0.f, v1 = q + 1 < nreal ? o[q + 1] : 0.f;
                     *reinterpret_cast<uint32_t *>(&sm.DOB[r * sm.dstr + q]) = pack_bf16(v0, v1);
                 }
+                __syncthreads();
+                // dOUT^T to global (rows of the transposed matrix = outputs of coordinate j)
+                {
+                    const int r = tid & (FROWS - 1), half = tid >> 7;
+                    for (int q = half; q < nreal; q += 2)
+                        dot_[((int64_t)j * nreal + q) * ldn + r0 + r] = sm.DOB[r * sm.dstr + q];
+                }
+                // db3 for coordinate j: column sums of dOUT
+                for (int q = tid; q < nreal; q += FNT) {
+                    float sacc = 0.f;
+                    for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.DOB[r * sm.dstr + q]);
+                    atomicAdd(&grad[y.ob3 + (int64_t)j * nreal + q], sacc);
+                }
+                // dH2 += dOUT_j W3_j  (K = CHK outputs)
+                warp_gemm<2, 8>(dh2, sm.DOB, sm.dstr, m0, mirror + y.mW3t + (int64_t)j * FH * (g.CHK + 8),
+                                g.CHK + 8, n0, g.CHK);
+                __syncthreads();
             }
-            __syncthreads();
-            // dOUT^T to global (rows of the transposed matrix = outputs of coordinate j)
-            {
-                const int r = tid & (FROWS - 1), half = tid >> 7;
-                for (int q = half; q < nreal; q += 2)
-                    dot_[((int64_t)j * nreal + q) * ldn + r0 + r] = sm.DOB[r * sm.dstr + q];
-            }
-            // db3 for coordinate j: column sums of dOUT
-            for (int q = tid; q < nreal; q += FNT) {
-                float sacc = 0.f;
-                for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.DOB[r * sm.dstr + q]);
-                atomicAdd(&grad[y.ob3 + (int64_t)j * nreal + q], sacc);
-            }
-            // dH2 += dOUT_j W3_j  (K = CHK outputs)
-            warp_gemm<2, 8>(dh2, sm.DOB, sm.dstr, m0, mirror + y.mW3t + (int64_t)j * FH * (g.CHK + 8),
-                            g.CHK + 8, n0, g.CHK);
-            __syncthreads();
         }
         // dH2' = dH2 * relu'(H2) -> H2 buffer (bf16) and dH2'^T to global; db2
 #pragma unroll
@@ -917,6 +933,7 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
 __device__ int g_flow_status;   // set to VG_ERR_TIMEOUT when a bounded wait gave up
 
 constexpr int UST_MAX = 16;      // 128-row sub-tiles per super-tile
+constexpr int WG_SPLIT = 64;     // split-K chunks of the weight-gradient GEMMs
 constexpr int UNT = 512;         // threads of the tcgen05 pass: 16 warps
 constexpr int UNH = UNT / FROWS; // column groups of threads (4): H columns and coordinates per group
 constexpr int UCOL = FH / UNH;   // H columns per thread in the epilogues (32)
@@ -1280,7 +1297,7 @@ extern "C" int64_t vg_flow_train_bytes(const vg_flow *fl, int64_t nrows)
     b += 2 * nrows * g.dim * 4;                   // gradient ping-pong
     b += (int64_t)FH * ldn * 2 * 4;               // h1t, h2t, dh2t, dh1t
     b += (int64_t)maxP * ldn * 2;                 // dout^T
-    b += 16 * (int64_t)(maxP > FH ? maxP : FH) * FH * 4;   // split-K partials (dW3, dW2)
+    b += WG_SPLIT * (int64_t)(maxP > FH ? maxP : FH) * FH * 4;   // split-K partials (dW3, dW2)
     b += nrows * 4 + nrows * g.dim * 4;           // logdet + zhat scratch
     return b + 4096;
 }
@@ -1406,7 +1423,7 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
     __nv_bfloat16 *dh2t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
     __nv_bfloat16 *dh1t = (__nv_bfloat16 *)take((int64_t)FH * ldn * 2);
     __nv_bfloat16 *dott = (__nv_bfloat16 *)take((int64_t)maxP * ldn * 2);
-    float *part = (float *)take(16 * (int64_t)(maxP > FH ? maxP : FH) * FH * 4);
+    float *part = (float *)take(WG_SPLIT * (int64_t)(maxP > FH ? maxP : FH) * FH * 4);
     float *ld = (float *)take(n * 4);
     float *zh = (float *)take(n * g.dim * 4);
     if (p > (char *)work + work_bytes) return vg_fail(VG_ERR_VALUE, "flow workspace layout");
@@ -1418,8 +1435,9 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
     if ((rc = set_smem((const void *)flow_bwd_kernel, smb))) return rc;
     int64_t grid = (int64_t)vg_num_sms();
     if (grid > ldn / FROWS) grid = ldn / FROWS;
-    // split-K over the batch rows: at most 16 chunks of a multiple of 16 rows
-    const int64_t kchunk = ((ldn / 16) + 15) / 16 * 16;
+    // split-K over the batch rows: at most WG_SPLIT chunks of a multiple of 16
+    // rows (enough CTAs in flight to hide the fragment loads' latency)
+    const int64_t kchunk = ((ldn / WG_SPLIT) + 15) / 16 * 16;
     float *gcur = ga, *gnext = gb;
     for (int l = g.L - 1; l >= 0; l--) {
         const FlowLayer &y = g.ly[l];
