@@ -322,7 +322,7 @@ struct FlowSmem {
     float *OUT;           // [FROWS][ostr] f32 conditioner outputs (2 chunks)
     __nv_bfloat16 *DOB;   // [FROWS][dstr] bf16 dL/dout of one chunk (backward)
     float *LD;            // [FROWS]
-    float *RED;           // [FNT] scratch for column sums
+    float *RED;           // [8 * FROWS] scratch (column sums, partial row sums)
     int ostr, dstr;
 };
 
@@ -335,7 +335,7 @@ __host__ __device__ inline size_t flow_smem_bytes(int CH, int CHK, int backward)
     o += sizeof(float) * FROWS * (2 * CH + 4);          // OUT
     if (backward) o += sizeof(__nv_bfloat16) * FROWS * (CHK + 8);   // DOB
     o += sizeof(float) * FROWS;                         // LD
-    o += sizeof(float) * FNT;                           // RED
+    o += sizeof(float) * 8 * FROWS;                     // RED
     return o;
 }
 
@@ -650,10 +650,12 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
                     for (int q = half; q < nreal; q += 2)
                         dot_[((int64_t)j * nreal + q) * ldn + r0 + r] = sm.DOB[r * sm.dstr + q];
                 }
-                // db3 for coordinate j: column sums of dOUT
-                for (int q = tid; q < nreal; q += FNT) {
+                // db3 for coordinate j: column sums of dOUT, four row quarters
+                // per column on all threads
+                for (int i = tid; i < 4 * nreal; i += FNT) {
+                    const int q = i % nreal, r0q = (i / nreal) * (FROWS / 4);
                     float sacc = 0.f;
-                    for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.DOB[r * sm.dstr + q]);
+                    for (int r = r0q; r < r0q + FROWS / 4; r++) sacc += __bfloat162float(sm.DOB[r * sm.dstr + q]);
                     atomicAdd(&grad[y.ob3 + (int64_t)j * nreal + q], sacc);
                 }
                 // dH2 += dOUT_j W3_j  (K = CHK outputs)
@@ -683,10 +685,11 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
             for (int c = 64 * half; c < 64 * half + 64; c++)
                 dh2t[(int64_t)c * ldn + r0 + r] = sm.H2[r * HSTR + c];
         }
-        if (tid < FH) {
+        {   // db2: column sums of dH2', two row halves per column
+            const int c = tid & (FH - 1), rh = (tid >> 7) * (FROWS / 2);
             float sacc = 0.f;
-            for (int r = 0; r < FROWS; r++) sacc += __bfloat162float(sm.H2[r * HSTR + tid]);
-            atomicAdd(&grad[y.ob2 + tid], sacc);
+            for (int r = rh; r < rh + FROWS / 2; r++) sacc += __bfloat162float(sm.H2[r * HSTR + c]);
+            atomicAdd(&grad[y.ob2 + c], sacc);
         }
         // dH1 = dH2' W2 ; dH1' = dH1 * relu'(H1) -> H1 buffer
         {
@@ -717,10 +720,11 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
         }
         // db1, dW1 (K = rows of the tile, FP32)
         const int dA = y.realA ? y.dA : 1;
-        for (int idx = tid; idx < FH * (dA + 1); idx += FNT) {
-            const int c = idx % FH, a2 = idx / FH;   // a2 == dA -> bias
+        for (int idx = tid; idx < 2 * FH * (dA + 1); idx += FNT) {
+            const int c = idx % FH, a2 = (idx / FH) % (dA + 1);   // a2 == dA -> bias
+            const int rh = (idx / (FH * (dA + 1))) * (FROWS / 2);   // row half
             float sacc = 0.f;
-            for (int r = 0; r < FROWS; r++) {
+            for (int r = rh; r < rh + FROWS / 2; r++) {
                 const float d1 = __bfloat162float(sm.H1[r * HSTR + c]);
                 const float xv = (a2 == dA) ? 1.f : (y.realA ? sm.Z[r * FMAXD + y.A[a2]] : 0.f);
                 sacc = fmaf(d1, xv, sacc);
@@ -729,13 +733,24 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
             else atomicAdd(&grad[y.oW1 + (int64_t)c * dA + a2], sacc);
         }
         // dL/dz_A += dH1' W1 (conditioning coordinates)
-        if (y.realA && tid < FROWS) {
-            const int r = tid;
+        if (y.realA) {   // thread (row, half): half of the hidden units, halves added in order
+            const int r = tid & (FROWS - 1), hf = tid >> 7;
             const float *W1 = theta + y.oW1;
-            for (int a2 = 0; a2 < y.dA; a2++) {
-                float sacc = 0.f;
-                for (int c = 0; c < FH; c++) sacc = fmaf(__bfloat162float(sm.H1[r * HSTR + c]), W1[c * dA + a2], sacc);
-                sm.G[r * FMAXD + y.A[a2]] += sacc;
+            for (int a0 = 0; a0 < y.dA; a0 += 8) {   // conditioning coordinates in chunks of 8
+                const int na = y.dA - a0 < 8 ? y.dA - a0 : 8;
+                float part[8];
+                for (int q = 0; q < na; q++) {
+                    float sacc = 0.f;
+                    for (int c = 64 * hf; c < 64 * hf + 64; c++)
+                        sacc = fmaf(__bfloat162float(sm.H1[r * HSTR + c]), W1[c * dA + a0 + q], sacc);
+                    part[q] = sacc;
+                }
+                if (hf == 1)
+                    for (int q = 0; q < na; q++) sm.RED[q * FROWS + r] = part[q];
+                __syncthreads();
+                if (hf == 0)
+                    for (int q = 0; q < na; q++) sm.G[r * FMAXD + y.A[a0 + q]] += part[q] + sm.RED[q * FROWS + r];
+                __syncthreads();
             }
         }
         __syncthreads();
