@@ -183,7 +183,30 @@ def batched_line(dev, reps=2):
         'setup_seconds': t_setup, 'integrals': len(fs),
         'pull_rms': float(np.sqrt(np.mean(pulls ** 2))), 'pull_max_abs': float(np.max(np.abs(pulls))),
         'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
+        # Lorentz factor per axis: subtract, FMA, reciprocal, multiply
+        'roofline': issue_roofline(dims, [n * 16 for n in nevals], secs, lambda d: 4 * d, 2070.0),
     }
+
+
+def issue_roofline(dims, nevals, seconds, integrand_ops, clock_mhz):
+    """Issue-rate model of a batched launch: thread instructions per
+    evaluation from op counts -- Philox4x32-10 (10 rounds of 2 wide
+    multiplies, 2 three-input XORs and 2 key adds, plus 4 conversions: 80
+    per 4 uniforms), the map (12 per axis: stratum coordinate, scale, floor,
+    table load, FMA, Jacobian, training bin), the integrand (integrand_ops(d))
+    and the per-sample reduction (30 + d: weight, histogram atomics,
+    float-float two-pass sums) -- against 128 thread instructions per cycle
+    and SM."""
+    import numpy as np
+    d = np.asarray(dims, np.int64)
+    ops = 80 * ((d + 3) // 4) + 12 * d + integrand_ops(d) + 30 + d
+    work = float(np.sum(ops * np.asarray(nevals, np.float64)))
+    peak = 152 * 128 * clock_mhz * 1e6
+    return {'bound': 'issue (model)', 'achieved': work / seconds / 1e12, 'peak': peak / 1e12,
+            'unit': 'T thread-instr/s', 'frac': work / seconds / peak,
+            'ops_per_evaluation_mean': float(np.sum(ops * np.asarray(nevals, np.float64)) /
+                                             np.sum(np.asarray(nevals, np.float64))),
+            'peak_source': '152 SMs x 4 schedulers x 32 lanes x %.0f MHz' % clock_mhz}
 
 
 def lattice_line(dev, reps=2):
@@ -223,6 +246,8 @@ def lattice_line(dev, reps=2):
         'pull_rms': float(np.sqrt(np.mean(pulls ** 2))), 'pull_max_abs': float(np.max(np.abs(pulls))),
         'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
         'oracle': 'transfer matrix, 400-node Gauss-Legendre, FP64 (LatticeAction.exact)',
+        # action per axis: difference, square, x^2, x^4 and the FMAs (6), plus one exp
+        'roofline': issue_roofline([16] * 64, [10 ** 7 * 16] * 64, secs, lambda d: 6 * d + 2, 2070.0),
         'fp32_vs_fp64_oracle_max_rel_dev': float(np.max(np.abs(res[:, 0] / exact - 1))),
     }
 
@@ -449,16 +474,22 @@ def gpu_arm(args):
                              'call': '%d calls Integrator(f, nitn=1), host round trip each'
                                      % args.steps}},
         'gpu_launches': 6 * args.steps,
-        'roofline': {'bound': 'sfu', 'achieved': achieved, 'peak': peak, 'unit': 'Gex2/s',
-                     'frac': achieved / peak, 'traffic': None,
+        'roofline': {'bound': 'sfu', 'achieved': ex2_per_launch / kern_s / 1e9, 'peak': peak,
+                     'unit': 'Gex2/s', 'frac': ex2_per_launch / kern_s / 1e9 / peak,
+                     'traffic': 1.70e6,
+                     'traffic_source': 'dram__bytes_read.sum + dram__bytes_write.sum of one fused '
+                                       'tile_kernel launch (ncu, bench.py --device-loop-only)',
                      'kernel': 'ridge iteration: fused tile_kernel (evaluate + reduce) + finalize '
                                '(CUDA events)',
-                     'algorithmic': 'ex2 evaluated per launch: %d (the terms that can be nonzero '
-                                    'in FP32; all M=1000 terms per evaluation = %d, the rest are '
-                                    'exactly zero and skipped)' % (executed, ex2_per_launch),
-                     # the rate the reference's algorithm (all M terms per evaluation)
-                     # would need to match this kernel; above 1: exactly-zero terms skipped
-                     'reference_terms_equivalent_frac': ex2_per_launch / kern_s / 1e9 / peak,
+                     'algorithmic': 'the integrand\'s M=1000 exponentials per evaluation: %d ex2 '
+                                    'per launch' % ex2_per_launch,
+                     # the kernel evaluates only the terms that can be nonzero in FP32 (the
+                     # others are exactly zero, so f is identical): above 1 against the
+                     # algorithmic count, and this fraction of the peak for what it executes
+                     'executed': executed, 'executed_frac': achieved / peak,
+                     'note': 'frac above 1: the kernel skips the Gaussian terms that are exactly '
+                             'zero in FP32 (identical results); executed_frac is the MUFU '
+                             'utilisation of the terms it does evaluate',
                      'peak_source': 'MUFU ex2 probe kernel on this GPU (vg_probe_mufu_ex2)'},
         'clocks': clk,
         'time_to_1e-4': tta,
