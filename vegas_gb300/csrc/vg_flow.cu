@@ -762,50 +762,96 @@ __global__ void __launch_bounds__(FNT) flow_bwd_kernel(
     }
 }
 
-// Weight gradients C[m][n] = sum_r A[m][r] B[n][r] over r in this CTA's
-// K-split (A, B bf16, K contiguous, ld = ldn); partial sums to
-// part[split][m][n].  Tile 64x64 per CTA, 8 warps of 16x32.
-__global__ void __launch_bounds__(FNT) flow_wgrad_kernel(const __nv_bfloat16 *__restrict__ A,
-                                                        const __nv_bfloat16 *__restrict__ B, int M,
-                                                        int N, int64_t ldn, int64_t kchunk,
-                                                        float *__restrict__ part)
+// Weight gradients on the 5th-generation tensor cores: part[split][m][n] =
+// sum over this CTA's K-split of A[m][k] B[n][k], A: M x ldn, B: 128 x ldn
+// (bf16, K contiguous = K-major operands), one 128-row m-tile per CTA
+// (blockIdx.x) and split (blockIdx.z).  Stages of 64 k are copied by the 128
+// threads into the SW128 layout, double-buffered; thread 0 issues the MMAs
+// (D in TMEM, 128 columns) and commits each stage to its buffer's mbarrier,
+// which is waited on before the buffer is refilled.  Every wait is bounded:
+// one that gives up sets g_flow_status, the MMAs are drained, TMEM is freed.
+__device__ int g_flow_status;   // set to VG_ERR_TIMEOUT when a bounded wait gave up
+
+constexpr int WGU_NT = 128;      // threads of the tcgen05 weight-gradient kernel
+constexpr int WGU_KS = 64;       // k per stage (one SW128 block)
+
+__global__ void __launch_bounds__(WGU_NT) flow_wgrad_umma_kernel(const __nv_bfloat16 *__restrict__ A,
+                                                                 const __nv_bfloat16 *__restrict__ B, int M,
+                                                                 int64_t ldn, int64_t kchunk,
+                                                                 float *__restrict__ part)
 {
-    const int w8 = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, t = lane & 3;
-    const int mb = blockIdx.x, nb = blockIdx.y, split = blockIdx.z;
-    const int m0 = 64 * mb + 16 * (w8 & 3), n0 = 64 * nb + 32 * (w8 >> 2);
-    const int64_t k0 = (int64_t)split * kchunk;
-    const int64_t k1 = k0 + kchunk < ldn ? k0 + kchunk : ldn;   // ldn, kchunk: multiples of 16
-    float acc[4][4];
-    for (int i = 0; i < 4; i++)
-        for (int q = 0; q < 4; q++) acc[i][q] = 0.f;
-    const int ra = m0 + gq, rb = ra + 8;
-    for (int64_t k = k0; k < k1; k += 16) {
-        uint32_t af[4];
-        const __nv_bfloat16 *pa0 = A + (int64_t)ra * ldn + k + 2 * t;
-        const __nv_bfloat16 *pa1 = A + (int64_t)rb * ldn + k + 2 * t;
-        af[0] = ra < M ? *reinterpret_cast<const uint32_t *>(pa0) : 0u;
-        af[1] = rb < M ? *reinterpret_cast<const uint32_t *>(pa1) : 0u;
-        af[2] = ra < M ? *reinterpret_cast<const uint32_t *>(pa0 + 8) : 0u;
-        af[3] = rb < M ? *reinterpret_cast<const uint32_t *>(pa1 + 8) : 0u;
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) {
-            const int cn = n0 + 8 * nt + gq;
-            uint32_t bf[2];
-            const __nv_bfloat16 *pb = B + (int64_t)cn * ldn + k + 2 * t;
-            bf[0] = cn < N ? *reinterpret_cast<const uint32_t *>(pb) : 0u;
-            bf[1] = cn < N ? *reinterpret_cast<const uint32_t *>(pb + 8) : 0u;
-            mma_bf16(acc[nt], af, bf);
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t bars[3];   // buffer 0, buffer 1, drain
+    __shared__ uint32_t slot;
+    __shared__ int s_ok;
+    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    constexpr uint32_t TILE = 128 * 128;   // bytes of a 128 x 64 bf16 tile
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * 128;
+    const int64_t k0 = (int64_t)blockIdx.z * kchunk;
+    const int64_t k1 = k0 + kchunk < ldn ? k0 + kchunk : ldn;
+    const int nstage = k1 > k0 ? (int)((k1 - k0) / WGU_KS) : 0;
+    if (warp == 0) umma::tmem_alloc(umma::smem_u32(&slot), 128);
+    if (tid == 0) {
+        for (int i = 0; i < 3; i++) umma::mbar_init(umma::smem_u32(&bars[i]), 1);
+        s_ok = 1;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = slot;
+    uint32_t ph[2] = {0u, 0u};
+    for (int st = 0; st < nstage; st++) {
+        const int b = st & 1;
+        uint8_t *sA = base + (uint32_t)b * 2u * TILE, *sB = sA + TILE;
+        if (st >= 2) {   // the MMAs of stage st - 2 read this buffer
+            if (tid == 0 && !umma::mbar_wait(umma::smem_u32(&bars[b]), ph[b])) s_ok = 0;
+            ph[b] ^= 1u;
+            __syncthreads();
+            if (!s_ok) break;
+        }
+        const int64_t kk = k0 + (int64_t)st * WGU_KS;
+        for (int i = tid; i < 128 * 8; i += WGU_NT) {
+            const int r = i >> 3, c = (i & 7) * 8;
+            uint4 va = make_uint4(0u, 0u, 0u, 0u);
+            if (m0 + r < M) va = *reinterpret_cast<const uint4 *>(A + (int64_t)(m0 + r) * ldn + kk + c);
+            *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(128, r, c)) = va;
+            *reinterpret_cast<uint4 *>(sB + umma::sw128_offset(128, r, c)) =
+                *reinterpret_cast<const uint4 *>(B + (int64_t)r * ldn + kk + c);
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {
+            umma::fence_after_sync();
+            umma::gemm_128xN(tmem, umma::smem_u32(sA), umma::smem_u32(sB), 128, WGU_KS, 128, st > 0 ? 1u : 0u);
+            umma::mma_commit(umma::smem_u32(&bars[b]));
         }
     }
-    float *P = part + (int64_t)split * M * N;
-#pragma unroll
-    for (int nt = 0; nt < 4; nt++) {
-        const int c = n0 + 8 * nt + 2 * t;
-        if (ra < M && c < N) P[(int64_t)ra * N + c] = acc[nt][0];
-        if (ra < M && c + 1 < N) P[(int64_t)ra * N + c + 1] = acc[nt][1];
-        if (rb < M && c < N) P[(int64_t)rb * N + c] = acc[nt][2];
-        if (rb < M && c + 1 < N) P[(int64_t)rb * N + c + 1] = acc[nt][3];
+    // drain: every MMA issued has completed before TMEM is read or freed
+    if (tid == 0) {
+        umma::mma_commit(umma::smem_u32(&bars[2]));
+        if (!umma::mbar_wait(umma::smem_u32(&bars[2]), 0)) s_ok = 0;
     }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const bool ok = s_ok != 0;
+    if (!ok && tid == 0) atomicExch(&g_flow_status, VG_ERR_TIMEOUT);
+    const int m = m0 + 32 * warp + (tid & 31);
+    float *P = part + (int64_t)blockIdx.z * M * 128;
+    for (int c = 0; c < 128; c += 16) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+        if (m < M) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) P[(int64_t)m * 128 + c + i] = (ok && nstage > 0) ? v[i] : 0.f;
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (warp == 0) umma::tmem_dealloc(tmem, 128);
 }
 
 __global__ void flow_wgrad_reduce_kernel(const float *__restrict__ part, int nsplit, int64_t MN,
@@ -945,7 +991,6 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
     return xo;
 }
 
-__device__ int g_flow_status;   // set to VG_ERR_TIMEOUT when a bounded wait gave up
 
 constexpr int UST_MAX = 16;      // 128-row sub-tiles per super-tile
 constexpr int WG_SPLIT = 64;     // split-K chunks of the weight-gradient GEMMs
@@ -1450,9 +1495,11 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
     if ((rc = set_smem((const void *)flow_bwd_kernel, smb))) return rc;
     int64_t grid = (int64_t)vg_num_sms();
     if (grid > ldn / FROWS) grid = ldn / FROWS;
-    // split-K over the batch rows: at most WG_SPLIT chunks of a multiple of 16
-    // rows (enough CTAs in flight to hide the fragment loads' latency)
-    const int64_t kchunk = ((ldn / WG_SPLIT) + 15) / 16 * 16;
+    // split-K over the batch rows: at most WG_SPLIT chunks of a multiple of 64
+    // rows (one tcgen05 stage), enough CTAs in flight
+    const int64_t kchunk = ((ldn / WG_SPLIT) + WGU_KS - 1) / WGU_KS * WGU_KS;
+    const size_t wgu_smem = 4 * 128 * 128 + 1024;   // two stages of A and B tiles + alignment
+    if ((rc = set_smem((const void *)flow_wgrad_umma_kernel, wgu_smem))) return rc;
     float *gcur = ga, *gnext = gb;
     for (int l = g.L - 1; l >= 0; l--) {
         const FlowLayer &y = g.ly[l];
@@ -1463,13 +1510,13 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
         // dW3 = dOUT^T H2  (M = P, N = hidden), dW2 = dH2'^T H1 (M = N = hidden)
         const int64_t ks = kchunk;
         const int ns = (int)((ldn + ks - 1) / ks);
-        dim3 g3((y.P + 63) / 64, (FH + 63) / 64, ns);
-        flow_wgrad_kernel<<<g3, FNT, 0, st>>>(dott, h2t, y.P, FH, ldn, ks, part);
+        // dW3 = dOUT^T H2 and dW2 = dH2'^T H1 over the rows (split-K), on tcgen05
+        flow_wgrad_umma_kernel<<<dim3((y.P + 127) / 128, 1, ns), WGU_NT, wgu_smem, st>>>(
+            dott, h2t, y.P, ldn, ks, part);
         VG_LAUNCH_CHECK();
         flow_wgrad_reduce_kernel<<<256, 256, 0, st>>>(part, ns, (int64_t)y.P * FH, fl->grad + y.oW3);
         VG_LAUNCH_CHECK();
-        dim3 g2((FH + 63) / 64, (FH + 63) / 64, ns);
-        flow_wgrad_kernel<<<g2, FNT, 0, st>>>(dh2t, h1t, FH, FH, ldn, ks, part);
+        flow_wgrad_umma_kernel<<<dim3(1, 1, ns), WGU_NT, wgu_smem, st>>>(dh2t, h1t, FH, ldn, ks, part);
         VG_LAUNCH_CHECK();
         flow_wgrad_reduce_kernel<<<256, 256, 0, st>>>(part, ns, (int64_t)FH * FH, fl->grad + y.oW2);
         VG_LAUNCH_CHECK();
