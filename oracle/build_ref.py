@@ -16,9 +16,10 @@ Recipe (nothing is written into the reference tree):
 3. cythonize + compile with gcc through setuptools, then copy the extension
    and an empty ``vegas/__init__.py`` into ``oracle/_ref/vegas/``.
 
-The reference's pure-Python ``vegas/__init__.py`` (PDFIntegrator etc.) is not
-needed for the hot path and is not built.  ``gvar`` (not installed) is
-replaced by ``oracle/gvar_stub``.
+The reference's pure-Python ``vegas/__init__.py`` (restratify, PDFIntegrator
+etc.) is not compiled; ``import_reference_package`` loads it straight from the
+reference tree on top of the compiled module when a golden generator needs
+``restratify``.  ``gvar`` (not installed) is replaced by ``oracle/gvar_stub``.
 
 Usage:  python oracle/build_ref.py [--reference /root/reference]
 """
@@ -92,6 +93,22 @@ def import_reference():
             sys.path.insert(0, p)
     from vegas import _vegas  # noqa: E402
     return _vegas
+
+
+def import_reference_package(reference='/root/reference'):
+    """The reference package ``vegas`` (src/vegas/__init__.py, read from the
+    reference tree) with ``vegas._vegas`` resolved to the compiled module."""
+    import importlib.util
+    stub = os.path.join(HERE, 'gvar_stub')
+    if stub not in sys.path:
+        sys.path.insert(0, stub)
+    spec = importlib.util.spec_from_file_location(
+        'vegas', os.path.join(reference, 'src', 'vegas', '__init__.py'),
+        submodule_search_locations=[OUT])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules['vegas'] = mod
+    spec.loader.exec_module(mod)
+    return mod
 
 
 if __name__ == '__main__':

@@ -18,8 +18,12 @@ It restates only what the reference's hot path touches:
 * ``gammaQ`` = regularised upper incomplete gamma (scipy ``gammaincc``),
   ``SVD`` (eigen-decomposition with a negative ``svdcut`` that drops small
   modes), ``mean``/``sdev``/``evalcov``, ``dumps``/``loads`` = pickle.
-* ``BufferDict`` is a bare placeholder: dict-valued integrands are not run
-  through the reference here.
+* ``BufferDict`` supports only what ``vegas.restratify``'s internal
+  integrand uses (src/vegas/__init__.py:1390-1419): an empty dictionary
+  filled with rbatch arrays (batch index last) and flattened by
+  ``_r2lbatch()`` to one lbatch array ``[nbatch, size]`` in key order, which
+  the reference then integrates as an array-valued integrand.  Any other use
+  raises.
 """
 import itertools
 import math
@@ -94,6 +98,25 @@ class GVar(object):
         if isinstance(o, GVar):
             return self._lin(o, 1.0 / o._mean, -self._mean / o._mean ** 2, self._mean / o._mean)
         return GVar(self._mean / o, {k: v / o for k, v in self._der.items()})
+
+    def __pow__(self, p):
+        p = float(p)
+        m = self._mean ** p
+        dm = p * self._mean ** (p - 1.0) if p != 0.0 else 0.0
+        return GVar(m, {k: dm * v for k, v in self._der.items()})
+
+    # comparisons act on the means, as in gvar
+    def __lt__(self, o):
+        return self._mean < (o._mean if isinstance(o, GVar) else o)
+
+    def __gt__(self, o):
+        return self._mean > (o._mean if isinstance(o, GVar) else o)
+
+    def __le__(self, o):
+        return self._mean <= (o._mean if isinstance(o, GVar) else o)
+
+    def __ge__(self, o):
+        return self._mean >= (o._mean if isinstance(o, GVar) else o)
 
     def __str__(self):
         return fmt(self._mean, self.sdev)
@@ -268,11 +291,20 @@ def tabulate(x, **kargs):
 
 
 class BufferDict(dict):
-    """Placeholder: dict-valued integrands are not exercised through this stub."""
+    """Empty dictionary of rbatch arrays, flattened by ``_r2lbatch``."""
     shape = None
 
     def __init__(self, *args, **kargs):
-        raise NotImplementedError('BufferDict is not provided by the oracle gvar stand-in')
+        if args or kargs:
+            raise NotImplementedError('BufferDict is not provided by the oracle gvar stand-in')
+        super(BufferDict, self).__init__()
+
+    def _r2lbatch(self):
+        cols = []
+        for k in self:
+            v = numpy.asarray(self[k], float)
+            cols.append(v.reshape(-1, v.shape[-1]).T)
+        return (numpy.ascontiguousarray(numpy.concatenate(cols, axis=1)),)
 
 
 def asbufferdict(x):

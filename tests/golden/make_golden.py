@@ -243,9 +243,76 @@ def alloc_cases(v):
     return out
 
 
-def main():
+def restrat_f(x):
+    """Integrand whose structure sits in directions 0 and 1 (weak in 2)."""
+    return np.exp(-40.0 * (x[:, 0] - 0.3) ** 2 - 25.0 * (x[:, 1] - 0.6) ** 2) * (1.0 + 0.2 * x[:, 2])
+
+
+RESTRAT_CASES = [
+    dict(seed=11, train=dict(nitn=4), args=dict(nitn=2, ndy=5)),
+    dict(seed=12, train=dict(nitn=3), args=dict(nitn=1, ndy=4, below_avg_nstrat=1, gamma=0.5)),
+]
+
+
+def restratify_cases(V):
+    """vegas.restratify (src/vegas/__init__.py:1313-1592) on a trained dim-6
+    integrator, in injected-sample mode.  The reference's internal I/dI
+    integrand returns a gvar BufferDict; the stand-in flattens it to an
+    array-valued integrand (same numbers, key order I then dI[mu, i]), and
+    the wrapper below hands restratify the dictionary view it indexes."""
+
+    class Restrat(V.restratifyIntegrator):
+        def __call__(self, fcn, **kargs):
+            r = V.Integrator.__call__(self, fcn, **kargs)
+            phase = self.__dict__.get('_phase', 0)
+            self._phase = phase + 1
+            if phase == 0:
+                flat = np.asarray(r, dtype=object)
+                d = _ResultDict(I=flat[0], dI=flat[1:].reshape(self.dim, self.ndy))
+                d.Q = r.Q
+                d.summary = r.summary
+                return d
+            self._training = r
+            return r
+
+    out = {}
+    for c, case in enumerate(RESTRAT_CASES):
+        rec = Recorder(case['seed'])
+        integ = V.Integrator(6 * [[0, 1]], neval=4000, alpha=0.5, ran_array_generator=rec)
+        f = V.lbatchintegrand(restrat_f)
+        r0 = integ(f, **case['train'])
+        R = Restrat(integ, f, **case['args'])
+        pre = 'c%d_' % c
+        out[pre + 'nstrat_before'] = np.asarray(R.old_nstrat, np.int64)
+        out[pre + 'train_mean'] = np.array(r0.mean)
+        out[pre + 'I'] = np.array([R.I.mean, R.I.sdev])
+        out[pre + 'dI_mean'] = np.array([[g.mean for g in row] for row in R.dI])
+        out[pre + 'dI_sdev'] = np.array([[g.sdev for g in row] for row in R.dI])
+        out[pre + 'weight_mean'] = np.array([g.mean for g in R.weight])
+        out[pre + 'weight_sdev'] = np.array([g.sdev for g in R.weight])
+        out[pre + 'Q'] = np.array(R.Q)
+        out[pre + 'nstrat_after'] = np.asarray(R.nstrat, np.int64)
+        out[pre + 'neval_after'] = np.array(R.neval)
+        tr = R._training
+        out[pre + 'itn_mean'] = np.array([g.mean for g in tr.itn_results])
+        out[pre + 'itn_sdev'] = np.array([g.sdev for g in tr.itn_results])
+        out[pre + 'grid_after'] = valid_grid(R.map)
+        out[pre + 'sum_sigf_after'] = np.array(R.sum_sigf)
+    out['ncases'] = np.array(len(RESTRAT_CASES))
+    return out
+
+
+class _ResultDict(dict):
+    pass
+
+
+def main(only=None):
     build_ref.build()
     v = build_ref.import_reference()
+    if only == ['restratify']:
+        V = build_ref.import_reference_package()
+        np.savez_compressed(os.path.join(HERE, 'ref_restratify.npz'), **restratify_cases(V))
+        return
     np.savez_compressed(os.path.join(HERE, 'ref_gauss4_injected.npz'),
                         **trace(v, 4 * [[0, 1]], gauss4, nitn=3, neval=10000, seed=1,
                                 alpha=0.5, beta=0.75))
@@ -267,4 +334,5 @@ def main():
 
 
 if __name__ == '__main__':
-    main()
+    # no argument: every fixture; "restratify": that fixture only
+    main(sys.argv[1:] or None)

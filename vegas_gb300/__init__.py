@@ -11,6 +11,7 @@ from .integrands import (BatchIntegrand, Constant, Gaussian, GaussianMixture, La
                          batchintegrand, lbatchintegrand, rbatchintegrand)
 from .integrator import Integrator, reporter, strata
 from .ravg import RAvg, RAvgArray, RAvgDict
+from .restratify import restratify, restratifyIntegrator
 from ._gvar import GVar, gvar
 
 __version__ = '0.1.0'
@@ -18,4 +19,5 @@ __version__ = '0.1.0'
 __all__ = ['AdaptiveMap', 'Integrator', 'RAvg', 'RAvgArray', 'RAvgDict', 'reporter', 'lbatchintegrand',
            'batchintegrand', 'rbatchintegrand', 'LBatchIntegrand', 'BatchIntegrand',
            'RBatchIntegrand', 'Gaussian', 'Ridge', 'LorentzianProduct', 'GaussianMixture',
-           'LatticeAction', 'Constant', 'GVar', 'gvar', 'strata']
+           'LatticeAction', 'Constant', 'GVar', 'gvar', 'strata', 'restratify',
+           'restratifyIntegrator']

@@ -5,7 +5,8 @@ The reference returns results built on the third-party ``gvar`` package
 dependency here: this module provides the small part of that interface the
 results need -- a mean, a linear combination of independent unit "primary"
 noises (so correlated arrays and ``evalcov`` work), linear error propagation
-through + - * /, and the compact ``mean(err)`` string format.
+through + - * / and powers, comparisons of means, and the compact
+``mean(err)`` string format.
 """
 import itertools
 import math
@@ -83,6 +84,25 @@ class GVar(object):
         o = float(o)
         m = o / self._mean
         return GVar(m, {k: -m / self._mean * v for k, v in self._der.items()})
+
+    def __pow__(self, p):
+        p = float(p)
+        m = self._mean ** p
+        dm = p * self._mean ** (p - 1.0) if p != 0.0 else 0.0
+        return GVar(m, {k: dm * v for k, v in self._der.items()})
+
+    # comparisons act on the means, as gvar's do
+    def __lt__(self, o):
+        return self._mean < float(o)
+
+    def __gt__(self, o):
+        return self._mean > float(o)
+
+    def __le__(self, o):
+        return self._mean <= float(o)
+
+    def __ge__(self, o):
+        return self._mean >= float(o)
 
     def __float__(self):
         return self._mean
