@@ -13,6 +13,7 @@ from .integrator import Integrator, reporter, strata
 from .ravg import RAvg, RAvgArray, RAvgDict
 from .restratify import restratify, restratifyIntegrator
 from ._gvar import GVar, gvar
+from . import checkpoint
 
 __version__ = '0.1.0'
 
