@@ -73,6 +73,25 @@ def test_array_reduction_matches_reference_loops(correlate):
     np.testing.assert_allclose(var, rv, rtol=1e-11, atol=1e-300)
 
 
+def test_array_reduction_many_uncorrelated_components():
+    """More than 16 uncorrelated components: reduced 16 columns at a time."""
+    I = vg.Integrator(3 * [[0, 1]], neval=3000, precision='fp64', seed=6,
+                      correlate_integrals=False)
+    it, ncap = I._struct()
+    I._allocate(it)
+    n = int(I._read_stats().neval)
+    x, _, w, hc = I._points(it, ncap, 1, None, want_hc=True)
+    base = _f3(x[:n])
+    cols = [base[:, k % 3] * (1.0 + 0.1 * k) * (x[:n, k % 3] if k >= 3 else 1.0) for k in range(37)]
+    f = torch.stack(cols, dim=1)
+    fbuf = torch.zeros((ncap, 37), dtype=torch.float64, device=x.device)
+    fbuf[:n] = f
+    mean, var = I._reduce_array(it, fbuf, N.VG_F64, w)
+    rm, rv = _ref_array_reduce(w[:n].cpu().numpy(), f.cpu().numpy(), hc[:n].cpu().numpy(), False)
+    np.testing.assert_allclose(mean, rm, rtol=1e-12)
+    np.testing.assert_allclose(var, rv, rtol=1e-11, atol=1e-300)
+
+
 def test_array_integrand_results():
     for correlate in (True, False):
         I = vg.Integrator(3 * [[0, 1]], neval=20000, seed=9, correlate_integrals=correlate)

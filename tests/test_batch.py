@@ -28,12 +28,13 @@ def test_batch_abi_sizes():
 
 
 @pytest.mark.gpu
-def test_batch_matches_single_integral_path():
+@pytest.mark.parametrize('variant', [0, 1, 2, 3])
+def test_batch_matches_single_integral_path(variant):
     from vegas_gb300.batch import BatchIntegrator
     rng = np.random.default_rng(3)
     dims, nevals = [3, 5, 9, 4], [10000, 30000, 20000, 50000]
     fs = [_lorentz(rng, d) for d in dims]
-    B = BatchIntegrator(fs, nevals, nitn=4, nwarm=1, seed=77, variant=0)
+    B = BatchIntegrator(fs, nevals, nitn=4, nwarm=1, seed=77, variant=variant)
     B.run()
     torch.cuda.synchronize()
     out = B.iterations()

@@ -14,7 +14,9 @@
 //
 // One warp per hypercube (static assignment), FP64 throughout; per-warp
 // totals in a fixed order, then one block sums the warps' partials with
-// Neumaier compensation -- deterministic.
+// Neumaier compensation -- deterministic.  Uncorrelated components are
+// independent, so more than 16 of them are reduced 16 at a time (one pair
+// of launches per group of columns).
 #include <string.h>
 
 #include "vg_tile.cuh"
@@ -31,14 +33,16 @@ struct ArrArgs {
     const double *wgt;
     const void *f;
     int f64;
-    int s;
+    int s;                         // components in this launch
+    int c0, ld;                    // first column of this launch, row length of f
     double *parts;                 // [nwarps][nval]
     int nval;
 };
 
 __device__ __forceinline__ double fval(const ArrArgs &a, int64_t j, int c)
 {
-    return a.f64 ? ((const double *)a.f)[j * a.s + c] : (double)((const float *)a.f)[j * a.s + c];
+    const int64_t i = j * a.ld + a.c0 + c;
+    return a.f64 ? ((const double *)a.f)[i] : (double)((const float *)a.f)[i];
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -148,17 +152,21 @@ __global__ void __launch_bounds__(ANT) array_hcube_kernel(ArrArgs a)
 
 // Fixed-order compensated sum of the warps' partials (one thread per value),
 // unpacked into mean[s] and the s x s (co)variance matrix.
+// Components c0 .. c0+s-1 of an s_all-component integrand; the first launch
+// (zero = 1) clears the whole matrix.
 __global__ void array_total_kernel(const double *__restrict__ parts, int64_t nw, int nval, int s, int corr,
-                                   double *__restrict__ mean_out, double *__restrict__ var_out)
+                                   int c0, int s_all, int zero, double *__restrict__ mean_out,
+                                   double *__restrict__ var_out)
 {
-    for (int i = threadIdx.x; i < s * s; i += blockDim.x) var_out[i] = 0.0;
+    if (zero)
+        for (int i = threadIdx.x; i < s_all * s_all; i += blockDim.x) var_out[i] = 0.0;
     __syncthreads();
     for (int v = threadIdx.x; v < nval; v += blockDim.x) {
         VgKSum k = {0.0, 0.0};
         for (int64_t w = 0; w < nw; w++) k.add(parts[w * nval + v]);
         const double tot = k.value();
         if (v < s) {
-            mean_out[v] = tot;
+            mean_out[c0 + v] = tot;
         } else if (corr) {
             int p = v - s, c = 0;
             while ((c + 1) * (c + 2) / 2 <= p) c++;
@@ -166,8 +174,8 @@ __global__ void array_total_kernel(const double *__restrict__ parts, int64_t nw,
             var_out[c * s + t] = tot;
             var_out[t * s + c] = tot;
         } else {
-            const int c = v - s;
-            var_out[c * s + c] = tot;
+            const int c = c0 + v - s;
+            var_out[(int64_t)c * s_all + c] = tot;
         }
     }
 }
@@ -185,8 +193,8 @@ extern "C" int vg_reduce_array(const vg_integrator *it, const void *f, int f_dty
     int rc = vg::fill_iter_args(a, it, 0, nullptr);
     if (rc) return rc;
     if (s < 1) return vg_fail(VG_ERR_VALUE, "s < 1");
-    if ((correlate && s > 6) || s > 16)
-        return vg_fail(VG_ERR_UNSUPPORTED, "array integrands: s <= 6 correlated, s <= 16 uncorrelated");
+    if (correlate && s > 6)
+        return vg_fail(VG_ERR_UNSUPPORTED, "array integrands: s <= 6 correlated components");
     const int np = correlate ? s * (s + 1) / 2 : s;
     const int nval = s + np;
     const int grid = vg_num_sms() * 2;
@@ -200,16 +208,31 @@ extern "C" int vg_reduce_array(const vg_integrator *it, const void *f, int f_dty
     A.wgt = wgt;
     A.f = f;
     A.f64 = (f_dtype == VG_F64);
-    A.s = s;
-    A.parts = (double *)work;
-    A.nval = nval;
+    A.ld = s;
     cudaStream_t st = (cudaStream_t)stream;
-    if (correlate) array_hcube_kernel<6, true><<<grid, ANT, 0, st>>>(A);
-    else if (s <= 8) array_hcube_kernel<8, false><<<grid, ANT, 0, st>>>(A);
-    else array_hcube_kernel<16, false><<<grid, ANT, 0, st>>>(A);
-    VG_LAUNCH_CHECK();
-    array_total_kernel<<<1, 128, 0, st>>>((const double *)work, nw, nval, s, correlate, mean_out, var_out);
-    VG_LAUNCH_CHECK();
+    if (correlate) {
+        A.s = s;
+        A.c0 = 0;
+        A.parts = (double *)work;
+        A.nval = nval;
+        array_hcube_kernel<6, true><<<grid, ANT, 0, st>>>(A);
+        VG_LAUNCH_CHECK();
+        array_total_kernel<<<1, 128, 0, st>>>((const double *)work, nw, nval, s, 1, 0, s, 1, mean_out, var_out);
+        VG_LAUNCH_CHECK();
+        return VG_OK;
+    }
+    for (int c0 = 0; c0 < s; c0 += 16) {   // groups of 16 independent columns
+        const int sc = s - c0 < 16 ? s - c0 : 16;
+        A.s = sc;
+        A.c0 = c0;
+        A.nval = 2 * sc;
+        A.parts = (double *)work + (size_t)nw * 2 * c0;
+        if (sc <= 8) array_hcube_kernel<8, false><<<grid, ANT, 0, st>>>(A);
+        else array_hcube_kernel<16, false><<<grid, ANT, 0, st>>>(A);
+        VG_LAUNCH_CHECK();
+        array_total_kernel<<<1, 128, 0, st>>>(A.parts, nw, A.nval, sc, 0, c0, s, c0 == 0, mean_out, var_out);
+        VG_LAUNCH_CHECK();
+    }
     return VG_OK;
 }
 

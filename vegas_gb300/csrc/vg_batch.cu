@@ -31,21 +31,26 @@ namespace {
 using namespace vgbatch;
 
 // Tile-shape variants: samples per thread of the dimension buckets 4 / 8 /
-// 16 and the shared-memory budget of the plan (above about 113 KB one CTA
-// per SM; below it two, with the training histogram in global memory when
-// it does not fit, and a kernel compiled for 128 registers per thread).
+// 16, the shared-memory budget of the plan (above about 113 KB one CTA per
+// SM; below it two, with a kernel compiled for 128 registers per thread) and
+// what leaves shared memory first when the plan is over budget: the training
+// histogram (its atomics then go to global memory) or the grid table (then
+// read through L1, the histogram keeps shared-memory atomics).
 struct Variant {
     int S4, S8, S16;
     size_t budget;
+    int table_first;   // over budget: drop the staged grid table before the histogram
+    int kernel;        // instantiation: 0 = k442, 1 = k221, 2 = k222
 };
 const Variant VARIANTS[] = {
-    {4, 4, 2, 220 * 1024},   // kernel k442, one CTA per SM
-    {2, 2, 1, 220 * 1024},   // kernel k221, one CTA per SM
-    {2, 2, 2, 110 * 1024},   // kernel k222, two CTAs per SM
+    {4, 4, 2, 220 * 1024, 0, 0},   // one CTA per SM, everything staged
+    {2, 2, 1, 220 * 1024, 0, 1},   // one CTA per SM, everything staged
+    {2, 2, 2, 110 * 1024, 0, 2},   // two CTAs per SM, histogram in global memory
+    {2, 2, 2, 110 * 1024, 1, 2},   // two CTAs per SM, grid table through L1
 };
 constexpr int NVARIANTS = (int)(sizeof(VARIANTS) / sizeof(VARIANTS[0]));
 
-int kernel_of(int v) { return v; }
+int kernel_of(int v) { return VARIANTS[v].kernel; }
 
 size_t table_jobs_bytes(int njobs) { return ((size_t)njobs * sizeof(BatchJob) + 255) & ~(size_t)255; }
 
@@ -99,11 +104,15 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
         a.table_smem = 1;
         a.hist_smem = bins;
         vg::SmemPlan p = vg::smem_plan<float>(dim, a.maxK, TT, 1, a.hist_smem, tab_len, bins, 1);
+        if (V.table_first && p.total > V.budget) {
+            a.table_smem = 0;
+            p = vg::smem_plan<float>(dim, a.maxK, TT, 0, a.hist_smem, tab_len, bins, 1);
+        }
         if (p.total > V.budget && a.hist_smem) {
             a.hist_smem = 0;
-            p = vg::smem_plan<float>(dim, a.maxK, TT, 1, 0, tab_len, bins, 1);
+            p = vg::smem_plan<float>(dim, a.maxK, TT, a.table_smem, 0, tab_len, bins, 1);
         }
-        if (p.total > V.budget) {
+        if (p.total > V.budget && a.table_smem) {
             a.table_smem = 0;
             p = vg::smem_plan<float>(dim, a.maxK, TT, 0, a.hist_smem, tab_len, bins, 1);
         }

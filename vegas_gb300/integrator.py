@@ -626,11 +626,13 @@ class Integrator(object):
         torch.cuda.current_stream(self.device).synchronize()
         raw = host[:nitn].numpy().tobytes()
         sz = ctypes.sizeof(N.VgStats)
+        gs = []
         for k in range(nitn):
             st = N.VgStats.from_buffer_copy(raw, k * sz)
             self._take_record(st)
-            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            gs.append(gv.gvar(st.mean, st.var ** 0.5))
             result.sum_neval += self.last_neval
+        result.add_many(gs)
         return result
 
     # --------------------------------------------------------------- report

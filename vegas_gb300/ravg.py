@@ -53,17 +53,29 @@ class RAvg(GVar):
 
     def add(self, g):
         """Add estimate ``g`` (a GVar) to the running average (pyx:2392-2410)."""
-        self.itn_results.append(g)
-        self._mlist.append(g.mean)
+        self.add_many((g,))
+
+    def add_many(self, gs):
+        """Add several estimates in order.  The weighted average after the
+        last one depends only on the full lists (the reference recomputes it
+        from them at every ``add``), so it is formed once, with the same
+        numpy sums; the unweighted running sums are accumulated in order."""
+        for g in gs:
+            self.itn_results.append(g)
+            self._mlist.append(g.mean)
+            if self.weighted:
+                self._wlist.append(1 / (g.var if g.var > TINY else TINY))
+            else:
+                self._msum += g.mean
+                self._varsum += g.var
+                self._n += 1
+        if not self._mlist:
+            return
         if self.weighted:
-            self._wlist.append(1 / (g.var if g.var > TINY else TINY))
             var = 1. / np.sum(self._wlist)
             sdev = np.sqrt(var)
             mean = np.sum([w * m for w, m in zip(self._wlist, self._mlist)]) * var
         else:
-            self._msum += g.mean
-            self._varsum += g.var
-            self._n += 1
             mean = self._msum / self._n
             sdev = np.sqrt(self._varsum / self._n ** 2)
         g2 = gv.gvar(mean, sdev)
