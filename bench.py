@@ -127,7 +127,7 @@ def profile_case(args, dev):
     elif args.case == 'batch':
         from vegas_gb300.batch import BatchIntegrator
         fs, nevals, _ = batch_workload(256)
-        B = BatchIntegrator(fs, nevals, nitn=2, nwarm=1, seed=99, device=dev, variant=0)
+        B = BatchIntegrator(fs, nevals, nitn=2, nwarm=1, seed=99, device=dev, variant=(1, 1, 0))
         for _ in range(args.warmup + args.steps):
             B.launch()
     torch.cuda.synchronize()

@@ -323,11 +323,18 @@ int vg_weight_points(int64_t n, const float *f, const float *jac, const float *l
  * described by its own vg_integrator (dimension <= 16, FP32, its own device
  * grid, inc, sigf, training histogram, stats and workspace) and built-in
  * integrand parameters (kind VG_F_LORENTZ or VG_F_LATTICE; params + j*ldp,
- * nparams[j] values) -- run nitn iterations each in ONE persistent kernel.
- * Queue mode (group <= 1): one CTA per integral at a time, integrals taken
- * from a queue in the order `order` (device int[njobs], e.g. largest
- * first).  Group mode (group = G >= 2, njobs*G <= the co-resident CTAs
- * vg_batch_prepare reports): a cooperative launch in which G CTAs share
+ * nparams[j] values) -- run nitn iterations each in one persistent kernel
+ * per dimension bucket (bucket 0: dim <= 4, 1: dim <= 8, 2: dim <= 16),
+ * the buckets' kernels on forked streams joined back into `stream`.
+ * cfg[3] picks each bucket's tile configuration (0 .. vg_batch_variants()-1:
+ * samples per thread and CTAs per SM); vg_batch_prepare copies the job table
+ * (vg_batch_table_bytes) to the device and returns each bucket's dynamic
+ * shared memory smem[3] and co-resident grid grid[3] (0 for a bucket
+ * without integrals).  Queue mode (group[b] <= 1): one CTA per integral at a
+ * time, bucket b's integrals taken from a queue (queue: device uint[3]) in
+ * the order order[seg[2b] .. seg[2b] + seg[2b+1]) (device int[njobs],
+ * e.g. largest first).  Group mode (group[b] = G >= 2, one bucket only,
+ * its integrals * G <= grid[b]): a cooperative launch in which G CTAs share
  * each integral's tiles (sync: device uint[njobs] barrier counters).  Each
  * iteration is the same allocation / fused evaluation + reduction / adapt
  * as vg_fused_iteration; out (device double[njobs][nitn][2]) receives every
@@ -335,20 +342,18 @@ int vg_weight_points(int64_t n, const float *f, const float *jac, const float *l
  * average over the iterations after the first nwarm (mean, sdev, chi2, dof).
  * stats->sum_sigf of each integral must hold its starting value (nhcube for
  * a fresh one).  status (device int) becomes VG_ERR_TIMEOUT if a bounded
- * group barrier gave up.  vg_batch_prepare copies the job table
- * (vg_batch_table_bytes) to the device and returns the launch's dynamic
- * shared memory and co-resident grid for the tile variant (0 ..
- * vg_batch_variants()-1); vg_batch_launch neither allocates nor
- * synchronises, so it can be captured in a CUDA graph.
+ * group barrier gave up.  vg_batch_launch neither allocates nor
+ * synchronises, so it can be captured in a CUDA graph (after a
+ * vg_batch_prepare on the same device, which creates the forked streams).
  */
 int vg_batch_variants(void);
 size_t vg_batch_table_bytes(int njobs);
 int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
-                     const int *nparams, int nitn, double *out, double *res, unsigned int *sync, int variant,
+                     const int *nparams, int nitn, double *out, double *res, unsigned int *sync, const int *cfg,
                      void *table, size_t table_bytes, size_t *smem, int *grid, void *stream);
 int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm, uint32_t itn0, const int *order,
-                    unsigned int *queue, unsigned int *sync, int group, int *status, size_t smem, int grid,
-                    int variant, void *stream);
+                    const int *seg, unsigned int *queue, unsigned int *sync, const int *group, int *status,
+                    const size_t *smem, const int *grid, const int *cfg, void *stream);
 
 /* Instrumentation: while set (device counter, NULL = off), the FP32 ridge
  * adds the number of Gaussian terms it evaluates -- the ones that can be

@@ -28,7 +28,7 @@ def test_batch_abi_sizes():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('variant', [0, 1, 2, 3])
+@pytest.mark.parametrize('variant', [0, 1, 2])
 def test_batch_matches_single_integral_path(variant):
     from vegas_gb300.batch import BatchIntegrator
     rng = np.random.default_rng(3)
@@ -80,10 +80,11 @@ def test_batch_accuracy_and_graph_replay():
 @pytest.mark.gpu
 def test_batch_group_mode_matches_queue_mode():
     """Cooperative groups of CTAs per integral give the queue mode's first
-    iteration (same samples) and the closed-form answers."""
+    iteration (same samples) and the closed-form answers (groups need the
+    integrals of one dimension bucket)."""
     from vegas_gb300.batch import BatchIntegrator
     rng = np.random.default_rng(21)
-    dims, nevals = [4, 6, 8], [200000, 300000, 100000]
+    dims, nevals = [5, 6, 8], [200000, 300000, 100000]
     fs = [_lorentz(rng, d) for d in dims]
     A = BatchIntegrator(fs, nevals, nitn=6, nwarm=2, seed=8, variant=0, group=1)
     B = BatchIntegrator(fs, nevals, nitn=6, nwarm=2, seed=8, variant=0, group=2)
@@ -93,6 +94,9 @@ def test_batch_group_mode_matches_queue_mode():
     exact = np.array([f.exact(d) for f, d in zip(fs, dims)])
     for r in (ra, rb):
         assert np.max(np.abs((r[:, 0] - exact) / r[:, 1])) < 5
+    with pytest.raises(ValueError):
+        BatchIntegrator([_lorentz(rng, 3), _lorentz(rng, 6)], [10000, 10000], nitn=2, nwarm=1,
+                        variant=0, group=2)
 
 
 @pytest.mark.gpu

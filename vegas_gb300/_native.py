@@ -163,8 +163,8 @@ SIGNATURES = {
     'vg_flow_set_path': (I32, [I32]),
     'vg_batch_variants': (I32, []),
     'vg_batch_table_bytes': (SZ, [I32]),
-    'vg_batch_prepare': (I32, [P, I32, I32, P, I32, P, I32, P, P, P, I32, P, SZ, P, P, P]),
-    'vg_batch_launch': (I32, [P, I32, I32, I32, I32, U32, P, P, P, I32, P, SZ, I32, I32, P]),
+    'vg_batch_prepare': (I32, [P, I32, I32, P, I32, P, I32, P, P, P, P, P, SZ, P, P, P]),
+    'vg_batch_launch': (I32, [P, I32, I32, I32, I32, U32, P, P, P, P, P, P, P, P, P, P]),
     'vg_eval_points': (I32, [I32, P, I32, I32, I64, P, P, P, P, P, P, P]),
     'vg_weight_points': (I32, [I64, P, P, P, P, P]),
     'vg_flow_zero_grad': (I32, [P, P]),

@@ -5,9 +5,11 @@ integrand).  ``BatchIntegrator`` holds the state of every integral -- the
 same per-integral state an ``Integrator`` has (AdaptiveMap grid, strata and
 their sigf, training histogram, iteration record) -- in a few device arenas,
 and runs ``nitn`` vegas+ iterations of all of them in one kernel
-(``vg_batch_launch``), optionally replayed from a CUDA graph.  The tile
-shape of that kernel is picked by a small autotuner that times each variant
-on a sample of the integrals.
+(``vg_batch_launch``: one persistent kernel per dimension bucket -- dim
+<= 4, <= 8, <= 16 -- on forked streams), optionally replayed from a CUDA
+graph.  The tile configuration of each bucket's kernel (samples per thread,
+CTAs per SM) is picked by a small autotuner that times each configuration on
+a sample of the bucket's integrals.
 """
 import ctypes
 import math
@@ -39,12 +41,14 @@ class BatchIntegrator(object):
         dims: dimension of each integral (needed for ``LatticeAction``).
         limits: (lo, hi) of every axis (default (0, 1)).
         group: CTAs per integral (None: as many as fit when every integral
-            gets at least two, else 1 = one CTA per integral from a queue).
+            gets at least two, else 1 = one CTA per integral from a queue);
+            more than one only when all integrals share a dimension bucket.
         nitn, nwarm: iterations per launch and warm-up iterations excluded
             from the weighted average (the reference's ``nitn`` of an adapt
             call followed by a final call).
         alpha, beta, seed: as ``Integrator``; integral j uses Philox stream j.
-        variant: tile variant of the kernel (None: autotune).
+        variant: tile configuration per dimension bucket, a sequence of 3
+            (or one int for all buckets); None: autotune.
     """
 
     def __init__(self, integrands, nevals, nitn=16, nwarm=8, alpha=0.5, beta=0.75, seed=1,
@@ -163,41 +167,62 @@ class BatchIntegrator(object):
         self.out = torch.zeros((nj, self.nitn, 2), dtype=torch.float64, device=self.device)
         self.res = torch.zeros((nj, 4), dtype=torch.float64, device=self.device)
         self.table = torch.empty(int(L.vg_batch_table_bytes(nj)), dtype=torch.uint8, device=self.device)
+        # queue order: grouped by dimension bucket, largest first in each
+        self.bucket = np.where(self.dims <= 4, 0, np.where(self.dims <= 8, 1, 2))
         cost = np.array([self.neval[j] * (1 + self.dims[j]) for j in range(nj)])
-        self.order = torch.tensor(np.argsort(-cost, kind='stable').astype(np.int32), device=self.device)
-        self.queue = torch.zeros(1, dtype=torch.int32, device=self.device)
+        order = np.lexsort((-cost, self.bucket)).astype(np.int32)
+        self.seg = np.zeros(6, np.int32)
+        for b in range(3):
+            pos = np.nonzero(self.bucket[order] == b)[0]
+            self.seg[2 * b] = int(pos[0]) if len(pos) else 0
+            self.seg[2 * b + 1] = len(pos)
+        self.order = torch.tensor(order, device=self.device)
+        self.queue = torch.zeros(3, dtype=torch.int32, device=self.device)
         self.sync = torch.zeros(nj, dtype=torch.int32, device=self.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
 
     # ----------------------------------------------------------- launching
     def set_variant(self, variant):
+        if np.ndim(variant) == 0:
+            variant = (int(variant),) * 3
+        cfg = np.array([int(v) for v in variant], np.int32)
+        if cfg.shape != (3,):
+            raise ValueError('variant: one configuration per dimension bucket (3)')
         L = N.load()
-        smem = ctypes.c_size_t(0)
-        grid = ctypes.c_int(0)
+        smem = np.zeros(3, np.uint64)
+        grid = np.zeros(3, np.int32)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
         N.check(L.vg_batch_prepare(ctypes.cast(self.its, ctypes.c_void_p), self.njobs, self.kind,
-                                   self.params.ctypes.data_as(ctypes.c_void_p), _LDP,
-                                   self.nparams.ctypes.data_as(ctypes.c_void_p), self.nitn,
-                                   N.ptr(self.out), N.ptr(self.res), N.ptr(self.sync), int(variant),
-                                   N.ptr(self.table),
-                                   self.table.numel(), ctypes.byref(smem), ctypes.byref(grid),
+                                   vp(self.params), _LDP, vp(self.nparams), self.nitn,
+                                   N.ptr(self.out), N.ptr(self.res), N.ptr(self.sync), vp(cfg),
+                                   N.ptr(self.table), self.table.numel(), vp(smem), vp(grid),
                                    N.stream_ptr(self.device)))
-        self.variant = int(variant)
-        self.smem = smem.value
-        self.grid = grid.value
-        if self.group_req is None:
-            g = self.grid // self.njobs
-            self.group = g if g >= 2 else 1
-        else:
-            self.group = int(self.group_req)
+        self._cfg, self._smem, self._grid = cfg, smem, grid
+        self.variant = tuple(int(v) for v in cfg)
+        present = [b for b in range(3) if self.seg[2 * b + 1] > 0]
+        self.groups = np.ones(3, np.int32)
+        if len(present) == 1:
+            b = present[0]
+            if self.group_req is None:
+                g = int(grid[b]) // int(self.seg[2 * b + 1])
+                self.groups[b] = g if g >= 2 else 1
+            else:
+                self.groups[b] = int(self.group_req)
+        elif self.group_req is not None and int(self.group_req) > 1:
+            raise ValueError('groups of CTAs per integral need integrals of one dimension bucket')
+        self.group = int(self.groups.max())
+        self.grid = int(grid.max())
         self._graph = None
 
     def launch(self):
-        """One persistent kernel: nitn iterations of every integral (asynchronous)."""
+        """nitn iterations of every integral (asynchronous): one persistent
+        kernel per dimension bucket."""
         L = N.load()
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
         N.check(L.vg_batch_launch(N.ptr(self.table), self.njobs, self.kind, self.nitn, self.nwarm,
-                                  (self._itn + 1) & 0xffffffff, N.ptr(self.order), N.ptr(self.queue),
-                                  N.ptr(self.sync), self.group, N.ptr(self.status), self.smem,
-                                  self.grid, self.variant, N.stream_ptr(self.device)))
+                                  (self._itn + 1) & 0xffffffff, N.ptr(self.order), vp(self.seg),
+                                  N.ptr(self.queue), N.ptr(self.sync), vp(self.groups), N.ptr(self.status),
+                                  vp(self._smem), vp(self._grid), vp(self._cfg), N.stream_ptr(self.device)))
         self._itn += self.nitn
 
     def capture(self):
@@ -242,35 +267,40 @@ class BatchIntegrator(object):
 
     # ------------------------------------------------------------ autotune
     def autotune(self, sample=256, reps=2):
-        """Time every tile variant of the batched kernel on a sample of the
-        integrals (fresh copies, one launch each after a warm-up launch) and
-        return the fastest."""
+        """Time every tile configuration of each dimension bucket's kernel on
+        a sample of that bucket's integrals (fresh copies, one launch each
+        after a warm-up launch) and return the fastest per bucket."""
         L = N.load()
         nv = int(L.vg_batch_variants())
         rng = np.random.default_rng(12345)
-        idx = np.sort(rng.choice(self.njobs, size=min(sample, self.njobs), replace=False))
-        best, best_t = 0, float('inf')
+        best = [0, 0, 0]
         self.tuning = {}
-        for v in range(nv):
-            try:
-                probe = BatchIntegrator([self.integrands[i] for i in idx], [self.neval[i] for i in idx],
-                                        nitn=2, nwarm=1, alpha=self.alpha, beta=self.beta,
-                                        seed=self.seed, variant=v, device=self.device,
-                                        neval_frac=self.neval_frac,
-                                        max_neval_hcube=self.max_neval_hcube,
-                                        dims=[int(self.dims[i]) for i in idx], limits=self.limits,
-                                        group=self.group_req)
-            except (ValueError, MemoryError, NotImplementedError, N.VegasError):
-                continue   # variant unavailable for this family / size
-            probe.launch()
-            torch.cuda.synchronize(self.device)
-            t0 = time.perf_counter()
-            for _ in range(reps):
+        for b in range(3):
+            members = np.nonzero(self.bucket == b)[0]
+            if len(members) == 0:
+                continue
+            idx = np.sort(rng.choice(members, size=min(sample, len(members)), replace=False))
+            best_t = float('inf')
+            for v in range(nv):
+                try:
+                    probe = BatchIntegrator([self.integrands[i] for i in idx], [self.neval[i] for i in idx],
+                                            nitn=2, nwarm=1, alpha=self.alpha, beta=self.beta,
+                                            seed=self.seed, variant=v, device=self.device,
+                                            neval_frac=self.neval_frac,
+                                            max_neval_hcube=self.max_neval_hcube,
+                                            dims=[int(self.dims[i]) for i in idx], limits=self.limits,
+                                            group=self.group_req)
+                except (ValueError, MemoryError, NotImplementedError, N.VegasError):
+                    continue   # configuration unavailable for this family / size
                 probe.launch()
-            torch.cuda.synchronize(self.device)
-            t = (time.perf_counter() - t0) / reps
-            self.tuning[v] = t
-            if t < best_t:
-                best, best_t = v, t
-            del probe
-        return best
+                torch.cuda.synchronize(self.device)
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    probe.launch()
+                torch.cuda.synchronize(self.device)
+                t = (time.perf_counter() - t0) / reps
+                self.tuning['%d/%d' % (b, v)] = t
+                if t < best_t:
+                    best[b], best_t = v, t
+                del probe
+        return tuple(best)

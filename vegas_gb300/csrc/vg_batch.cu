@@ -1,12 +1,15 @@
 // vg_batch.cu -- host side of the batched many-integral launch.
 //
 // vg_batch_prepare builds the device job table (per integral: its iteration
-// arguments, adapt arguments, integrand parameters, output slots) and picks
-// the shared-memory plan of a tile-shape variant; vg_batch_launch is one
-// persistent kernel over all integrals (no host synchronisation, no
-// allocation: it can be captured in a CUDA graph).  No counterpart in the
-// reference, which integrates one integrand per Integrator call; each
-// integral here runs the same vegas+ iteration as vg_fused_iteration.
+// arguments, adapt arguments, integrand parameters, output slots) and the
+// shared-memory plan of each dimension bucket's tile configuration;
+// vg_batch_launch runs one persistent kernel per bucket present (integrals of
+// dim <= 4, <= 8, <= 16), the buckets on forked streams so that the SMs one
+// bucket's kernel leaves at its end are taken by the next (no host
+// synchronisation, no allocation: it can be captured in a CUDA graph).  No
+// counterpart in the reference, which integrates one integrand per Integrator
+// call; each integral here runs the same vegas+ iteration as
+// vg_fused_iteration.
 #include <string.h>
 
 #include <vector>
@@ -16,47 +19,78 @@
 int vg_build_params(int kind, int dim, const double *params, int nparams, VgParams *Pp, int *tab_len_out);
 
 namespace vgbatch {
-int launch_k442(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, int, int *, cudaStream_t);
-int launch_k221(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, int, int *, cudaStream_t);
-int launch_k222(int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t,
-                int, int, int *, cudaStream_t);
-int occupancy_k442(int, size_t, int *);
-int occupancy_k221(int, size_t, int *);
-int occupancy_k222(int, size_t, int *);
+int launch_b4(int, int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *,
+              size_t, int, int, int *, cudaStream_t);
+int launch_b8(int, int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *,
+              size_t, int, int, int *, cudaStream_t);
+int launch_b16(int, int, const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *,
+               size_t, int, int, int *, cudaStream_t);
+int occupancy_b4(int, int, size_t, int *);
+int occupancy_b8(int, int, size_t, int *);
+int occupancy_b16(int, int, size_t, int *);
 }  // namespace vgbatch
 
 namespace {
 using namespace vgbatch;
 
-// Tile-shape variants: samples per thread of the dimension buckets 4 / 8 /
-// 16, the shared-memory budget of the plan (above about 113 KB one CTA per
-// SM; below it two, with a kernel compiled for 128 registers per thread) and
-// what leaves shared memory first when the plan is over budget: the training
-// histogram (its atomics then go to global memory) or the grid table (then
-// read through L1, the histogram keeps shared-memory atomics).
-struct Variant {
-    int S4, S8, S16;
-    size_t budget;
-    int table_first;   // over budget: drop the staged grid table before the histogram
-    int kernel;        // instantiation: 0 = k442, 1 = k221, 2 = k222
-};
-const Variant VARIANTS[] = {
-    {4, 4, 2, 220 * 1024, 0, 0},   // one CTA per SM, everything staged
-    {2, 2, 1, 220 * 1024, 0, 1},   // one CTA per SM, everything staged
-    {2, 2, 2, 110 * 1024, 0, 2},   // two CTAs per SM, histogram in global memory
-    {2, 2, 2, 110 * 1024, 1, 2},   // two CTAs per SM, grid table through L1
-};
-constexpr int NVARIANTS = (int)(sizeof(VARIANTS) / sizeof(VARIANTS[0]));
-
-int kernel_of(int v) { return VARIANTS[v].kernel; }
-
 size_t table_jobs_bytes(int njobs) { return ((size_t)njobs * sizeof(BatchJob) + 255) & ~(size_t)255; }
+
+// Shared-memory budget of a plan for `minb` CTAs per SM: the SM's 228 KB
+// less the per-CTA reservation and the kernel's static shared memory.
+size_t smem_budget(int minb)
+{
+    const size_t per = (size_t)228 * 1024 / (size_t)minb;
+    const size_t cap = (size_t)220 * 1024;
+    const size_t b = per > 6 * 1024 ? per - 6 * 1024 : 0;
+    return b < cap ? b : cap;
+}
+
+int bucket_of(int dim) { return dim <= 4 ? 0 : (dim <= 8 ? 1 : 2); }
+
+int occupancy_dispatch(int b, int kind, int cfg, size_t smem, int *per_sm)
+{
+    if (b == 0) return occupancy_b4(kind, cfg, smem, per_sm);
+    if (b == 1) return occupancy_b8(kind, cfg, smem, per_sm);
+    return occupancy_b16(kind, cfg, smem, per_sm);
+}
+
+int launch_dispatch(int b, int kind, int cfg, const BatchJob *jobs, const VgParams *prm, const int *order, int njobs,
+                    int nitn, int nwarm, uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group,
+                    int *status, cudaStream_t st)
+{
+    if (b == 0)
+        return launch_b4(kind, cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status, st);
+    if (b == 1)
+        return launch_b8(kind, cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status, st);
+    return launch_b16(kind, cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status, st);
+}
+
+// Streams the bucket kernels run on besides the caller's, and the events of
+// the fork and the join (created outside any capture, by vg_batch_prepare).
+struct AuxStreams {
+    int dev = -1;
+    cudaStream_t s[NBUCKET];
+    cudaEvent_t fork, join[NBUCKET];
+};
+AuxStreams g_aux;
+
+int ensure_aux()
+{
+    int dev = 0;
+    VG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (g_aux.dev == dev) return VG_OK;
+    for (int b = 0; b < NBUCKET; b++) {
+        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_aux.s[b], cudaStreamNonBlocking));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_aux.join[b], cudaEventDisableTiming));
+    }
+    VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_aux.fork, cudaEventDisableTiming));
+    g_aux.dev = dev;
+    return VG_OK;
+}
 
 }  // namespace
 
-extern "C" int vg_batch_variants(void) { return NVARIANTS; }
+extern "C" int vg_batch_variants(void) { return NCONFIG; }
 
 extern "C" size_t vg_batch_table_bytes(int njobs)
 {
@@ -65,56 +99,57 @@ extern "C" size_t vg_batch_table_bytes(int njobs)
 
 extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
                                 const int *nparams, int nitn, double *out, double *res, unsigned int *sync,
-                                int variant, void *table, size_t table_bytes, size_t *smem_out, int *grid_out,
+                                const int *cfg, void *table, size_t table_bytes, size_t *smem_out, int *grid_out,
                                 void *stream)
 {
     vg_clear_error();
     if (njobs < 1) return vg_fail(VG_ERR_VALUE, "no integrals");
     if (kind != VG_F_LORENTZ && kind != VG_F_LATTICE)
         return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: Lorentzian products and the lattice action only");
-    if (variant < 0 || variant >= NVARIANTS) return vg_fail(VG_ERR_VALUE, "variant %d", variant);
+    for (int b = 0; b < NBUCKET; b++)
+        if (cfg[b] < 0 || cfg[b] >= NCONFIG) return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
     if (nitn < 1) return vg_fail(VG_ERR_VALUE, "nitn < 1");
     if (table_bytes < vg_batch_table_bytes(njobs)) return vg_fail(VG_ERR_VALUE, "job table too small");
-    const Variant V = VARIANTS[variant];
+    int rc = ensure_aux();
+    if (rc) return rc;
     std::vector<BatchJob> jobs((size_t)njobs);
     std::vector<VgParams> prm((size_t)njobs);
-    size_t smem_max = 0;
+    size_t smem_max[NBUCKET] = {0, 0, 0};
+    int present[NBUCKET] = {0, 0, 0};
     for (int j = 0; j < njobs; j++) {
         const vg_integrator *it = &its[j];
         if (it->precision != VG_F32) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch computes in FP32");
         BatchJob &J = jobs[(size_t)j];
         memset(&J, 0, sizeof(J));
-        int rc = vg::fill_iter_args(J.a, it, 0, nullptr);
-        if (rc) return rc;
+        if ((rc = vg::fill_iter_args(J.a, it, 0, nullptr))) return rc;
         int tab_len = 0;
         if ((rc = vg_build_params(kind, it->dim, params + (size_t)j * ldp, nparams[j], &prm[(size_t)j], &tab_len)))
             return rc;
         const int dim = it->dim;
-        int S;
-        if (dim <= 4) { J.dimb = 4; S = V.S4; }
-        else if (dim <= 8) { J.dimb = 8; S = V.S8; }
-        else if (dim <= 16) { J.dimb = 16; S = V.S16; }
-        else return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: dim %d above 16", dim);
+        if (dim > 16) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: dim %d above 16", dim);
+        const int b = bucket_of(dim);
+        const BucketConfig C = BUCKET_CONFIGS[b][cfg[b]];
+        J.bucket = b;
+        present[b] = 1;
         IterArgs &a = J.a;
-        const int TT = vg::NT * S;
+        const int TT = vg::NT * C.S;
+        const size_t budget = smem_budget(C.minb);
         a.tab_len = tab_len;
         a.T = TT;
         a.ncta = 1;
         const int bins = a.train;
+        // over budget: the grid table goes first (read through L1), then the
+        // training histogram (global atomics)
         a.table_smem = 1;
         a.hist_smem = bins;
         vg::SmemPlan p = vg::smem_plan<float>(dim, a.maxK, TT, 1, a.hist_smem, tab_len, bins, 1);
-        if (V.table_first && p.total > V.budget) {
+        if (p.total > budget) {
             a.table_smem = 0;
             p = vg::smem_plan<float>(dim, a.maxK, TT, 0, a.hist_smem, tab_len, bins, 1);
         }
-        if (p.total > V.budget && a.hist_smem) {
+        if (p.total > budget && a.hist_smem) {
             a.hist_smem = 0;
-            p = vg::smem_plan<float>(dim, a.maxK, TT, a.table_smem, 0, tab_len, bins, 1);
-        }
-        if (p.total > V.budget && a.table_smem) {
-            a.table_smem = 0;
-            p = vg::smem_plan<float>(dim, a.maxK, TT, 0, a.hist_smem, tab_len, bins, 1);
+            p = vg::smem_plan<float>(dim, a.maxK, TT, 0, 0, tab_len, bins, 1);
         }
         if (p.total > 220 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
         size_t need = p.total;
@@ -147,7 +182,7 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
         J.out = out + (size_t)j * 2 * nitn;
         J.res = res + (size_t)j * 4;
         J.sync = sync != nullptr ? sync + j : nullptr;
-        smem_max = need > smem_max ? need : smem_max;
+        smem_max[b] = need > smem_max[b] ? need : smem_max[b];
     }
     cudaStream_t st = (cudaStream_t)stream;
     char *tb = (char *)table;
@@ -155,43 +190,80 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
     VG_CUDA_CHECK(cudaMemcpyAsync(tb + table_jobs_bytes(njobs), prm.data(), sizeof(VgParams) * (size_t)njobs,
                                   cudaMemcpyHostToDevice, st));
     VG_CUDA_CHECK(cudaStreamSynchronize(st));   // the host staging buffers go out of scope
-    int per_sm = 0, rc = 0;
-    switch (kernel_of(variant)) {
-    case 0: rc = occupancy_k442(kind, smem_max, &per_sm); break;
-    case 1: rc = occupancy_k221(kind, smem_max, &per_sm); break;
-    default: rc = occupancy_k222(kind, smem_max, &per_sm); break;
+    for (int b = 0; b < NBUCKET; b++) {
+        smem_out[b] = 0;
+        grid_out[b] = 0;
+        if (!present[b]) continue;
+        int per_sm = 0;
+        if ((rc = occupancy_dispatch(b, kind, cfg[b], smem_max[b], &per_sm))) return rc;
+        if (per_sm < 1) return vg_fail(VG_ERR_UNSUPPORTED, "batched kernel (bucket %d) does not fit on an SM", b);
+        smem_out[b] = smem_max[b];
+        grid_out[b] = vg_num_sms() * per_sm;
     }
-    if (rc) return rc;
-    if (per_sm < 1) return vg_fail(VG_ERR_UNSUPPORTED, "batched kernel does not fit on an SM");
-    *smem_out = smem_max;
-    *grid_out = vg_num_sms() * per_sm;
     return VG_OK;
 }
 
+// seg[2b], seg[2b+1]: first position and count of bucket b's integrals in
+// `order`; queue[3]: one counter per bucket; group[b] > 1 (cooperative groups
+// of CTAs per integral) only when a single bucket is present.
 extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm, uint32_t itn0,
-                               const int *order, unsigned int *queue, unsigned int *sync, int group, int *status,
-                               size_t smem, int grid, int variant, void *stream)
+                               const int *order, const int *seg, unsigned int *queue, unsigned int *sync,
+                               const int *group, int *status, const size_t *smem, const int *grid, const int *cfg,
+                               void *stream)
 {
     vg_clear_error();
-    if (variant < 0 || variant >= NVARIANTS) return vg_fail(VG_ERR_VALUE, "variant %d", variant);
     if (nwarm < 0 || nwarm >= nitn) return vg_fail(VG_ERR_VALUE, "need 0 <= nwarm < nitn");
+    int dev = 0;
+    VG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (g_aux.dev != dev) return vg_fail(VG_ERR_VALUE, "vg_batch_prepare was not called on this device");
     cudaStream_t st = (cudaStream_t)stream;
     const BatchJob *jobs = (const BatchJob *)table;
     const VgParams *prm = (const VgParams *)((const char *)table + table_jobs_bytes(njobs));
-    int g;
-    if (group > 1) {   // njobs groups of `group` co-resident CTAs
-        if ((int64_t)njobs * group > grid)
-            return vg_fail(VG_ERR_VALUE, "group launch needs njobs*group <= %d co-resident CTAs", grid);
+    int npresent = 0, anygroup = 0;
+    for (int b = 0; b < NBUCKET; b++) {
+        if (seg[2 * b + 1] <= 0) continue;
+        npresent++;
+        if (cfg[b] < 0 || cfg[b] >= NCONFIG) return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
+        if (seg[2 * b] < 0 || seg[2 * b] + seg[2 * b + 1] > njobs) return vg_fail(VG_ERR_VALUE, "bucket segment");
+        if (grid[b] < 1) return vg_fail(VG_ERR_VALUE, "bucket %d was not prepared", b);
+        if (group[b] > 1) {
+            anygroup = 1;
+            if ((int64_t)seg[2 * b + 1] * group[b] > grid[b])
+                return vg_fail(VG_ERR_VALUE, "group launch needs integrals*group <= %d co-resident CTAs", grid[b]);
+        }
+    }
+    if (npresent == 0) return vg_fail(VG_ERR_VALUE, "no integrals in the buckets");
+    if (anygroup && npresent > 1)
+        return vg_fail(VG_ERR_VALUE, "groups of CTAs per integral need integrals of one dimension bucket");
+    if (anygroup) {
         if (sync == nullptr) return vg_fail(VG_ERR_VALUE, "group launch needs the sync counters");
-        g = njobs * group;
         VG_CUDA_CHECK(cudaMemsetAsync(sync, 0, sizeof(unsigned int) * (size_t)njobs, st));
-    } else {
-        g = grid < njobs ? grid : njobs;
     }
-    VG_CUDA_CHECK(cudaMemsetAsync(queue, 0, sizeof(unsigned int), st));
-    switch (kernel_of(variant)) {
-    case 0: return launch_k442(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
-    case 1: return launch_k221(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
-    default: return launch_k222(kind, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, g, group, status, st);
+    VG_CUDA_CHECK(cudaMemsetAsync(queue, 0, sizeof(unsigned int) * NBUCKET, st));
+    // fork: the first bucket (largest dimension first) runs on the caller's
+    // stream, the others on their own streams after it was enqueued
+    if (npresent > 1) VG_CUDA_CHECK(cudaEventRecord(g_aux.fork, st));
+    int first = 1;
+    int joined[NBUCKET] = {0, 0, 0};
+    for (int b = NBUCKET - 1; b >= 0; b--) {
+        const int n = seg[2 * b + 1];
+        if (n <= 0) continue;
+        cudaStream_t sb = st;
+        if (!first) {
+            sb = g_aux.s[b];
+            VG_CUDA_CHECK(cudaStreamWaitEvent(sb, g_aux.fork, 0));
+        }
+        const int g = group[b] > 1 ? n * group[b] : (grid[b] < n ? grid[b] : n);
+        int rc = launch_dispatch(b, kind, cfg[b], jobs, prm, order + seg[2 * b], n, nitn, nwarm, itn0, queue + b,
+                                 smem[b], g, group[b] > 1 ? group[b] : 1, status, sb);
+        if (rc) return rc;
+        if (!first) {
+            VG_CUDA_CHECK(cudaEventRecord(g_aux.join[b], sb));
+            joined[b] = 1;
+        }
+        first = 0;
     }
+    for (int b = 0; b < NBUCKET; b++)
+        if (joined[b]) VG_CUDA_CHECK(cudaStreamWaitEvent(st, g_aux.join[b], 0));
+    return VG_OK;
 }

@@ -24,7 +24,7 @@ struct BatchJob {
     double *out;                 // [nitn][2] iteration mean, variance
     double *res;                 // [4] weighted mean, sdev, chi2, dof
     unsigned int *sync;          // group barrier counter (group mode)
-    int dimb;                    // dimension bucket: 4, 8 or 16
+    int bucket;                  // dimension bucket: 0 (dim <= 4), 1 (<= 8), 2 (<= 16)
     int adapt;                   // adapt the map after each iteration
 };
 
@@ -242,16 +242,18 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
     J.res[3] = (double)(cnt > 0 ? cnt - 1 : 0);
 }
 
-// The persistent kernel: S4, S8, S16 are the samples per thread of the
-// dimension buckets and MINB the CTAs per SM it is compiled for (the tile
-// shape and occupancy the autotuner picks).
+// The persistent kernel of one dimension bucket (every integral it takes has
+// dim <= DIMB): S samples per thread and MINB CTAs per SM it is compiled for
+// (the tile shape and occupancy the autotuner picks per bucket; one kernel
+// per bucket lets the small-dimension integrals run at the occupancy their
+// registers and shared memory allow).
 //
 // Queue mode (group <= 1): each CTA takes whole integrals from the queue.
 // Group mode (group = G >= 2, cooperative launch): CTA c works on integral
 // order[c / G] as rank c % G; rank 0 allocates, finalizes and adapts, all G
 // ranks share the tiles (rank r takes tiles r, r + G, ...), with two group
 // barriers per iteration.
-template <int KIND, int S4, int S8, int S16, int MINB>
+template <int KIND, int DIMB, int S, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restrict__ jobs,
                                                    const VgParams *__restrict__ params,
                                                    const int *__restrict__ order, int njobs, int nitn,
@@ -289,7 +291,6 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
             for (int i = tid; i < nw; i += NT) dst[i] = src[i];
         }
         __syncthreads();
-        const int dimb = J.dimb;
         unsigned int rounds = 0;
         bool ok = true;
         for (int it = 0; it < nitn && ok; it++) {
@@ -297,11 +298,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
             __syncthreads();
             if (rank == 0) cta_alloc(sa, scan);
             if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
-            if (sa.stats->ntiles > 0) {
-                if (dimb == 4) tile_body<float, MODE_FUSED, KIND, 4, S4>(sa, params[j], smem, rank, G, rank);
-                else if (dimb == 8) tile_body<float, MODE_FUSED, KIND, 8, S8>(sa, params[j], smem, rank, G, rank);
-                else tile_body<float, MODE_FUSED, KIND, 16, S16>(sa, params[j], smem, rank, G, rank);
-            }
+            if (sa.stats->ntiles > 0) tile_body<float, MODE_FUSED, KIND, DIMB, S>(sa, params[j], smem, rank, G, rank);
             __syncthreads();
             if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
             if (rank == 0) {
@@ -322,5 +319,98 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
         __syncthreads();
     }
 }
+
+// Launch (queue mode, or cooperative for co-resident groups) and occupancy
+// of one instantiation; the bucket files dispatch to these.
+template <int KIND, int DIMB, int S, int MINB>
+int launch_one(const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn, int nwarm,
+               uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group, int *status, cudaStream_t st)
+{
+    auto k = batch_kernel<KIND, DIMB, S, MINB>;
+    if (group > 1) {
+        void *args[] = {(void *)&jobs, (void *)&prm, (void *)&order, (void *)&njobs, (void *)&nitn, (void *)&nwarm,
+                        (void *)&itn0, (void *)&queue, (void *)&group, (void *)&status};
+        VG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)k, dim3((unsigned)grid), dim3(NT), args, smem, st));
+        return VG_OK;
+    }
+    k<<<grid, NT, smem, st>>>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, group, status);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
+// sets the kernel's shared-memory attribute (outside any stream capture)
+template <int KIND, int DIMB, int S, int MINB>
+int occupancy_one(size_t smem, int *per_sm)
+{
+    auto k = batch_kernel<KIND, DIMB, S, MINB>;
+    VG_CUDA_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, NT, smem));
+    return VG_OK;
+}
+
+// Tile configurations of each bucket: samples per thread and CTAs per SM.
+struct BucketConfig {
+    int S, minb;
+};
+constexpr int NCONFIG = 3;
+constexpr int NBUCKET = 3;
+constexpr int BUCKET_DIM[NBUCKET] = {4, 8, 16};
+constexpr BucketConfig BUCKET_CONFIGS[NBUCKET][NCONFIG] = {
+    {{2, 4}, {4, 2}, {2, 2}},   // dim <= 4
+    {{2, 2}, {4, 1}, {2, 3}},   // dim <= 8
+    {{2, 1}, {1, 2}, {2, 2}},   // dim <= 16
+};
+
+// One bucket's launch and occupancy for configuration cfg (instantiated by
+// the bucket's own translation unit, vg_batch_b<DIMB>.cu).
+template <int KIND, int DIMB>
+int bucket_launch(int cfg, const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn,
+                  int nwarm, uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group, int *status,
+                  cudaStream_t st)
+{
+    constexpr int b = DIMB == 4 ? 0 : (DIMB == 8 ? 1 : 2);
+    constexpr BucketConfig c0 = BUCKET_CONFIGS[b][0], c1 = BUCKET_CONFIGS[b][1], c2 = BUCKET_CONFIGS[b][2];
+    switch (cfg) {
+    case 0:
+        return launch_one<KIND, DIMB, c0.S, c0.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+                                                     group, status, st);
+    case 1:
+        return launch_one<KIND, DIMB, c1.S, c1.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+                                                     group, status, st);
+    default:
+        return launch_one<KIND, DIMB, c2.S, c2.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+                                                     group, status, st);
+    }
+}
+
+template <int KIND, int DIMB>
+int bucket_occupancy(int cfg, size_t smem, int *per_sm)
+{
+    constexpr int b = DIMB == 4 ? 0 : (DIMB == 8 ? 1 : 2);
+    constexpr BucketConfig c0 = BUCKET_CONFIGS[b][0], c1 = BUCKET_CONFIGS[b][1], c2 = BUCKET_CONFIGS[b][2];
+    switch (cfg) {
+    case 0: return occupancy_one<KIND, DIMB, c0.S, c0.minb>(smem, per_sm);
+    case 1: return occupancy_one<KIND, DIMB, c1.S, c1.minb>(smem, per_sm);
+    default: return occupancy_one<KIND, DIMB, c2.S, c2.minb>(smem, per_sm);
+    }
+}
+
+// The entry points of each bucket's translation unit.
+#define VG_BATCH_BUCKET_ENTRY(DIMB)                                                                             \
+    int launch_b##DIMB(int kind, int cfg, const BatchJob *jobs, const VgParams *prm, const int *order,          \
+                       int njobs, int nitn, int nwarm, uint32_t itn0, unsigned int *queue, size_t smem,         \
+                       int grid, int group, int *status, cudaStream_t st)                                       \
+    {                                                                                                           \
+        if (kind == VG_F_LATTICE)                                                                               \
+            return bucket_launch<VG_F_LATTICE, DIMB>(cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue,    \
+                                                     smem, grid, group, status, st);                            \
+        return bucket_launch<VG_F_LORENTZ, DIMB>(cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem,  \
+                                                 grid, group, status, st);                                      \
+    }                                                                                                           \
+    int occupancy_b##DIMB(int kind, int cfg, size_t smem, int *per_sm)                                          \
+    {                                                                                                           \
+        if (kind == VG_F_LATTICE) return bucket_occupancy<VG_F_LATTICE, DIMB>(cfg, smem, per_sm);               \
+        return bucket_occupancy<VG_F_LORENTZ, DIMB>(cfg, smem, per_sm);                                         \
+    }
 
 }  // namespace vgbatch
