@@ -16,7 +16,11 @@ JSON keys follow the benchmark contract: value = evaluations/s with inputs
 resident in HBM (device loop, CUDA events on the launching stream); e2e = the
 same through the public API (Integrator.__call__ per step, host buffers for
 the integrand parameters and the result); roofline of the dominant kernel;
-cpu_baseline; clocks sampled during the timed region.
+cpu_baseline; clocks sampled during the timed region.  Further lines: the
+time to 1e-4 relative error (plain and flow-augmented vegas+), the batched
+launch of 4096 integrals, the 64-coupling lattice scan, the FP64 dim-4 case
+and the drop-in path (a torch integrand through the public API, with the HBM
+roofline of the sampling and reduction kernels).
 """
 import argparse
 import ctypes
@@ -147,6 +151,100 @@ def batch_workload(njobs=4096, seed=2024):
         fs.append(vg.LorentzianProduct(c, w))
     nevals = np.exp(rng.uniform(np.log(1e4), np.log(1e6), njobs)).astype(np.int64)
     return fs, nevals, dims
+
+
+def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
+    """The drop-in path: a torch lbatch integrand (the dim-4 Gaussian
+    (100/pi)^2 exp(-100 sum (x-1/2)^2) written in torch ops) through
+    Integrator.__call__ -- sampling + map kernel (vg_sample), the integrand's
+    own torch kernels, reduction + training histogram kernel (vg_reduce),
+    adapt.  Evaluations/s through the API, and the HBM roofline of the
+    sampling and reduction kernels: algorithmic bytes per evaluation (x
+    written 4 dim + weight 8 by the sampler; f read 4 by the reduction, which
+    regenerates y from Philox instead of reading it) over their CUDA-event
+    times, against the measured copy bandwidth."""
+    import math
+    import numpy as np
+    import torch
+    import vegas_gb300 as vg
+    from vegas_gb300 import _native as N
+    dim = 4
+
+    @vg.lbatchintegrand
+    def gauss(x):
+        return (100.0 / math.pi) ** 2 * torch.exp(-100.0 * ((x - 0.5) ** 2).sum(dim=1))
+
+    integ = vg.Integrator(dim * [[0, 1]], neval=neval, seed=31, device=dev)
+    integ(gauss, nitn=3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = integ(gauss, nitn=nitn)
+    torch.cuda.synchronize()
+    api_s = time.perf_counter() - t0
+    # kernel timings on the launching stream
+    L = N.load()
+    stream = N.stream_ptr(dev)
+    it, ncap = integ._struct()
+    integ._allocate(it)
+    n = int(integ._read_stats().neval)
+    x = torch.empty((ncap, dim), dtype=torch.float32, device=dev)
+    w = torch.empty(ncap, dtype=torch.float64, device=dev)
+    cur = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+
+    def sample():
+        N.check(L.vg_sample(ctypes.byref(it), 7, None, N.ptr(x), None, N.ptr(w), None, ncap, stream))
+
+    sample()
+    f = gauss(x[:n])
+    fb = torch.zeros(ncap, dtype=torch.float32, device=dev)
+    fb[:n] = f
+
+    def reduce():
+        N.check(L.vg_reduce(ctypes.byref(it), 7, None, N.ptr(fb), N.VG_F32, stream))
+
+    reduce()
+    torch.cuda.synchronize()
+    ev[0].record(cur)
+    for _ in range(reps):
+        sample()
+    ev[1].record(cur)
+    for _ in range(reps):
+        f = gauss(x[:n])
+    ev[2].record(cur)
+    for _ in range(reps):
+        reduce()
+    ev[3].record(cur)
+    torch.cuda.synchronize()
+    t_s = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+    t_f = ev[1].elapsed_time(ev[2]) / 1e3 / reps
+    t_r = ev[2].elapsed_time(ev[3]) / 1e3 / reps
+    peaks = {}
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'MEASURED_PEAKS.json')) as fh:
+            peaks = json.load(fh)
+    except (OSError, ValueError):
+        pass
+    hbm = float(peaks.get('hbm_gbs', 6800.0))
+    b_s, b_r = 4 * dim + 8, 4
+    return {
+        'workload': 'drop-in path: torch lbatch integrand (dim-4 Gaussian, torch ops) through '
+                    'Integrator.__call__, neval %.0e/itn, FP32 sampling, FP64 sums' % neval,
+        'value': r.sum_neval / api_s, 'unit': 'evals/s', 'neval_per_iteration': n,
+        'result': str(r),
+        'seconds_per_iteration': {'api': api_s / nitn, 'sample_kernel': t_s, 'integrand_torch': t_f,
+                                  'reduce_kernel': t_r},
+        'roofline': {
+            'bound': 'hbm', 'unit': 'GB/s', 'peak': hbm,
+            'peak_source': 'MEASURED_PEAKS.json hbm_gbs' if 'hbm_gbs' in peaks else 'fallback',
+            'sample_kernel': {'bytes_per_eval': b_s, 'achieved': b_s * n / t_s / 1e9,
+                              'frac': b_s * n / t_s / 1e9 / hbm},
+            'reduce_kernel': {'bytes_per_eval': b_r, 'achieved': b_r * n / t_r / 1e9,
+                              'frac': b_r * n / t_r / 1e9 / hbm,
+                              'note': 'regenerates each sample (Philox, map) and forms the two-pass '
+                                      'hypercube sums and the training histogram: bound by that '
+                                      'work, not by its 4 bytes per evaluation'}},
+    }
 
 
 def batched_line(dev, reps=2):
@@ -447,9 +545,10 @@ def gpu_arm(args):
             'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
         if rank == 0:
             tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
-    batched = lattice = small = None
+    batched = lattice = small = dropin = None
     if rank == 0:
         small = config1_line(dev)
+        dropin = dropin_line(dev)
     if not args.no_batch and rank == 0:
         batched = batched_line(dev)
         lattice = lattice_line(dev)
@@ -496,6 +595,7 @@ def gpu_arm(args):
         'batched': batched,
         'lattice_scan': lattice,
         'small_fp64': small,
+        'dropin': dropin,
     }
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)

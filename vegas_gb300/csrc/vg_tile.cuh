@@ -872,12 +872,31 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         float jn[S];   // FP32 mode: wgt * neval_h = jac * dv_y
         int lhs[S];
         int cur = lh;
+        // the uniforms of all the thread's samples first (into xs): the
+        // draws do not depend on the hypercube walk below, so the S samples'
+        // Philox rounds interleave instead of waiting on one another
+#pragma unroll
+        for (int k = 0; k < S; k++) {
+#pragma unroll
+            for (int d = 0; d < DIMB; d++) xs[k][d] = (T)0.5;
+            if (k < nmine) {
+                const int64_t ig = tile_start + li0 + k;
+                if (a.u != nullptr) {
+#pragma unroll
+                    for (int d = 0; d < DIMB; d++)
+                        if (d < dim) xs[k][d] = (T)a.u[ig * dim + d];
+                } else {
+                    VgUniform<T>::template draw<DIMB>(a.seed, a.stream, a.itn, (uint64_t)ig, dim, xs[k]);
+#pragma unroll
+                    for (int d = 0; d < DIMB; d++)
+                        if (d >= dim) xs[k][d] = (T)0.5;
+                }
+            }
+        }
 #pragma unroll
         for (int k = 0; k < S; k++) {
             lhs[k] = cur;
             wg[k] = 0.0;
-#pragma unroll
-            for (int d = 0; d < DIMB; d++) xs[k][d] = (T)0.5;
             if (k < nmine) {
                 const int li = li0 + k;
                 while (li >= win_off[cur + 1]) {   // next hypercube: mixed-radix increment
@@ -899,14 +918,6 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 lhs[k] = cur;
                 const int64_t ig = tile_start + li;
                 const int nh = win_n[cur];
-                T u[DIMB];
-                if (a.u != nullptr) {
-#pragma unroll
-                    for (int d = 0; d < DIMB; d++)
-                        if (d < dim) u[d] = (T)a.u[ig * dim + d];
-                } else {
-                    VgUniform<T>::template draw<DIMB>(a.seed, a.stream, a.itn, (uint64_t)ig, dim, u);
-                }
                 T jac = (T)1;
                 T yv[DIMB];
 #pragma unroll
@@ -914,7 +925,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     if (d >= dim) continue;
                     const int K = a.ninc[d];
                     T yd, yn, yfl;
-                    const int iy = sample_y<T>(y0[d], y0f[d], u[d], a.nstrat[d], rstrat[d], K, Kf[d], yd, yn, yfl);
+                    const int iy = sample_y<T>(y0[d], y0f[d], xs[k][d], a.nstrat[d], rstrat[d], K, Kf[d], yd, yn, yfl);
                     const T dy = yn - yfl;
                     yv[d] = yd;
                     const int clamp = iy >= K;
