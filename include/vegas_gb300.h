@@ -203,6 +203,18 @@ int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, i
 int vg_end_iteration(const vg_integrator *it, void *stream);
 
 /*
+ * One full iteration for a built-in integrand (pyx:2086-2217: allocation,
+ * the fused batch loop, the iteration sums, the map adapt) in one call:
+ * vg_allocate + vg_fused_iteration + vg_end_iteration, with the adapt on a
+ * forked stream concurrently with the finalize when adapt_to_errors is off
+ * (the adapt needs only the tile kernel's training histogram); joined back
+ * into `stream` before returning.  Call it once outside any stream capture
+ * before capturing it (the first call on a device creates the forked stream).
+ */
+int vg_iterate(const vg_integrator *it, uint32_t itn, int kind, const double *params, int nparams,
+               void *stream);
+
+/*
  * One vegas+ iteration (allocation, fused evaluation + reduction, adapt) for
  * a built-in integrand that allocates no device memory.  No counterpart in
  * the reference: it exists for callers that cannot allocate device memory --

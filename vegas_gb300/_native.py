@@ -147,6 +147,7 @@ SIGNATURES = {
     'vg_reduce': (I32, [P, U32, P, P, I32, P]),
     'vg_fused_iteration': (I32, [P, U32, P, I32, P, I32, P]),
     'vg_end_iteration': (I32, [P, P]),
+    'vg_iterate': (I32, [P, U32, I32, P, I32, P]),
     'vg_reduce_array': (I32, [P, P, I32, I32, I32, P, P, P, P, SZ, P]),
     'vg_reduce_array_work_bytes': (SZ, [I32, I32]),
     'vg_iteration_noalloc': (I32, [P, U32, P, I32, P, I32, P]),

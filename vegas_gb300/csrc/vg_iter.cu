@@ -719,6 +719,9 @@ extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const d
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
+// forward declaration: one full iteration (below)
+extern "C" int vg_end_iteration(const vg_integrator *it, void *stream);
+
 int vg_adapt_launch(int dim, const int64_t *old_ninc, const int64_t *new_ninc, const double *grid,
                     const double *inc, int64_t ldg, int64_t ldi, const double *sum_f,
                     const uint64_t *n_f, double alpha, double *new_grid, double *new_inc,
@@ -755,4 +758,57 @@ extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
     VG_CUDA_CHECK(cudaMemsetAsync(it->sum_f, 0, sizeof(double) * it->dim * it->ldi, st));
     VG_CUDA_CHECK(cudaMemsetAsync(it->n_f, 0, sizeof(uint64_t) * it->dim * it->ldi, st));
     return VG_OK;
+}
+
+// One full vegas+ iteration = vg_allocate + vg_fused_iteration +
+// vg_end_iteration, enqueued by one call.  The map adapt needs only the
+// training histogram the tile kernel completed, so (unless adapt_to_errors,
+// whose finalize adds to that histogram) it runs on a forked stream while the
+// finalize merges the hypercubes cut by tile boundaries; both join back into
+// `stream` before the call returns.  The forked stream and events are created
+// on the first call on a device (outside any stream capture).
+namespace {
+struct IterAux {
+    int dev = -1;
+    cudaStream_t s;
+    cudaEvent_t fork, join;
+};
+IterAux g_iter_aux;
+}  // namespace
+
+extern "C" int vg_iterate(const vg_integrator *it, uint32_t itn, int kind, const double *params, int nparams,
+                          void *stream)
+{
+    int rc = vg_allocate(it, stream);
+    if (rc) return rc;
+    vg_clear_error();
+    IterArgs a;
+    if ((rc = fill_args(a, it, itn, nullptr))) return rc;
+    static VgParams P;
+    int tab_len = 0;
+    if ((rc = vg_build_params(kind, it->dim, params, nparams, &P, &tab_len))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = vg::launch_fused(a, kind, P, tab_len, it->precision == VG_F64, st))) return rc;
+    int64_t kmax = 0;
+    for (int d = 0; d < it->dim; d++) kmax = it->ninc[d] > kmax ? it->ninc[d] : kmax;
+    const int overlap = it->adapt && it->alpha > 0 && !it->adapt_to_errors && vg_adapt_in_place_ok((int)kmax);
+    if (!overlap) {
+        if ((rc = vg::finalize_launch(a, st, it->precision == VG_F32))) return rc;
+        return vg_end_iteration(it, stream);
+    }
+    int dev = 0;
+    VG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (g_iter_aux.dev != dev) {
+        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_iter_aux.s, cudaStreamNonBlocking));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_iter_aux.fork, cudaEventDisableTiming));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_iter_aux.join, cudaEventDisableTiming));
+        g_iter_aux.dev = dev;
+    }
+    VG_CUDA_CHECK(cudaEventRecord(g_iter_aux.fork, st));
+    VG_CUDA_CHECK(cudaStreamWaitEvent(g_iter_aux.s, g_iter_aux.fork, 0));
+    rc = vg_end_iteration(it, g_iter_aux.s);
+    VG_CUDA_CHECK(cudaEventRecord(g_iter_aux.join, g_iter_aux.s));
+    if (rc == VG_OK) rc = vg::finalize_launch(a, st, it->precision == VG_F32);
+    VG_CUDA_CHECK(cudaStreamWaitEvent(st, g_iter_aux.join, 0));
+    return rc;
 }

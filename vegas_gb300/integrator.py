@@ -9,8 +9,11 @@ Python face of the reference's ``vegas.Integrator`` (src/vegas/_vegas.pyx:
   one persistent kernel per iteration, no host round trip except reading the
   80-byte iteration record;
 * lbatch integrands receive CUDA tensors ``x[n, dim]`` (FP32 by default, FP64
-  with ``precision='fp64'``) in batches of ``min_neval_batch`` points and
-  return ``f[n]``; the reduction then runs on the device.
+  with ``precision='fp64'``) and return ``f[n]``; the reduction then runs on
+  the device.  The points of an iteration are all in HBM already, so a batch
+  holds as many as ``max_mem`` allows (at least ``min_neval_batch``, the
+  reference's lower bound on a batch): normally the whole iteration in one
+  call.
 
 Extra settings beyond the reference's: ``precision`` ('fp32' | 'fp64'),
 ``seed`` (Philox key), ``device``.
@@ -390,6 +393,13 @@ class Integrator(object):
             return 'rbatch'
         return 'scalar'
 
+    def _eval_batch_size(self):
+        """Points per integrand call: at least min_neval_batch (the
+        reference's lower bound on a batch, pyx:1692-1710), as many as
+        max_mem (floats) allows for x, jac and f."""
+        per_point = 2 * self.dim + 2
+        return max(1, int(self.min_neval_batch), int(self.max_mem // per_point))
+
     def _eval_batch(self, fcn, kind, x, jac=None, layout=None):
         """fcn on a batch; with uses_jac, jac[n, dim] = dx/dy per direction is
         passed as ``jac=`` (transposed for rbatch, per point for scalar
@@ -516,7 +526,7 @@ class Integrator(object):
                     x, yv, w, _ = self._points(it, ncap, itn_word, u, want_y=self.uses_jac)
                     jac = self.map.jac1d(yv[:n]) if self.uses_jac else None
                     f = None
-                    nb = max(1, int(self.min_neval_batch))
+                    nb = self._eval_batch_size()
                     for lo in range(0, n, nb):
                         hi = min(n, lo + nb)
                         if fshape is None:
@@ -603,7 +613,8 @@ class Integrator(object):
     def _call_pipelined(self, fcn, result):
         """__call__ for a built-in integrand when no iteration needs a host
         decision (no rtol/atol stop, analyzer or save): every iteration --
-        allocation, fused evaluate+reduce, adapt -- is enqueued without
+        allocation, fused evaluate+reduce, adapt, one ``vg_iterate`` call
+        that overlaps the adapt with the iteration sums -- is enqueued without
         waiting, and each iteration's record is copied to pinned host memory
         on the same stream; the records are read once after the last
         iteration.  Same kernels and results as the iteration-by-iteration
@@ -617,11 +628,9 @@ class Integrator(object):
         nitn = int(self.nitn)
         host = self._records_host(nitn)
         for k in range(nitn):
-            N.check(L.vg_allocate(ctypes.byref(it), stream))
             self._itn += 1
-            N.check(L.vg_fused_iteration(ctypes.byref(it), self._itn & 0xffffffff, None, int(fcn.kind),
-                                         params, len(p), stream))
-            N.check(L.vg_end_iteration(ctypes.byref(it), stream))
+            N.check(L.vg_iterate(ctypes.byref(it), self._itn & 0xffffffff, int(fcn.kind), params, len(p),
+                                 stream))
             host[k].copy_(self._stats, non_blocking=True)
         torch.cuda.current_stream(self.device).synchronize()
         raw = host[:nitn].numpy().tobytes()
