@@ -4,9 +4,10 @@
 // (pyx:1636-1765) and the batch loop of Integrator.__call__ (pyx:2096-2197).
 //
 // Layout of an iteration (all device-resident, no host round trip):
-//   1. allocation (3 small kernels): neval_h[h] from sigf (pyx:1692-1706),
-//      exclusive scan -> offsets[h], neval_hcube_range, the tile schedule
-//      tile_h0[t] (first hypercube of each tile of TILE samples).
+//   1. allocation (one single-pass kernel): neval_h[h] from sigf
+//      (pyx:1692-1706), exclusive scan -> offsets[h], neval_hcube_range, the
+//      tile schedule tile_h0[t] (first hypercube of each tile of TILE
+//      samples).
 //   2. a persistent tile kernel: each CTA walks tiles t = blockIdx.x,
 //      += gridDim.x.  A tile is TILE consecutive samples (samples are ordered
 //      by hypercube, as in the reference).  Per sample: Philox uniforms (or
@@ -81,122 +82,131 @@ __device__ __forceinline__ int64_t block_max(int64_t v, int64_t *wtot /* NTB/32 
     return m;
 }
 
-// pyx:1692-1706 for the block's ALLOC_NT * ALLOC_PER hypercubes (coalesced);
-// block totals for the scan.  The per-iteration constants are formed once
-// per block (FP64 divisions are slow on GB300).  With build_table the grid
-// also builds the FP32 grid table of the iteration.
-__global__ void __launch_bounds__(ALLOC_NT) alloc_count_kernel(IterArgs a, int build_table)
+// Allocation, pyx:1692-1706, in one pass over the hypercubes: block b
+// (numbered by the order in which blocks start, so it only waits on blocks
+// already running) counts neval_h for its ALLOC_NT * ALLOC_PER hypercubes,
+// publishes its total, looks back over its predecessors' published totals
+// for its offset (decoupled look-back: a predecessor that already knows its
+// inclusive prefix ends the walk), publishes its inclusive prefix, and writes
+// offsets[h] and the tile schedule.  The last block writes the iteration's
+// totals and resets the pass for the next iteration.  Published words hold
+// (epoch, state, value) so nothing has to be cleared between iterations;
+// every wait is bounded and a timeout is reported as VG_ERR_TIMEOUT with no
+// tiles scheduled.  With build_table the grid also builds the FP32 grid table.
+struct AllocSync {
+    unsigned int ticket, epoch, err, pad;
+    unsigned long long maxacc;
+};
+
+constexpr int FLAG_AGG = 1, FLAG_INC = 2;
+
+__device__ __forceinline__ unsigned long long flag_word(unsigned int epoch, int state, int64_t v)
 {
-    __shared__ int64_t ssum[ALLOC_NT / 32];
+    return ((unsigned long long)(epoch & 0x3fffffu) << 42) | ((unsigned long long)state << 40) |
+           ((unsigned long long)v & ((1ull << 40) - 1));
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(ALLOC_NT) alloc_kernel(IterArgs a, int64_t nblk, int build_table)
+{
+    __shared__ int64_t wtot[ALLOC_NT / 32];
     __shared__ double s_nsf;
-    __shared__ int64_t s_avg;
-    if (threadIdx.x == 0) {
+    __shared__ int64_t s_avg, s_prefix;
+    __shared__ unsigned int s_b, s_epoch;
+    AllocSync *sy = reinterpret_cast<AllocSync *>(a.alloc_sync);
+    unsigned long long *flags = reinterpret_cast<unsigned long long *>(a.bsum);
+    const int t = threadIdx.x;
+    if (t == 0) {
+        s_b = atomicAdd(&sy->ticket, 1u);
+        s_epoch = *(volatile unsigned int *)&sy->epoch;
         const double sum_sigf = a.stats->sum_sigf;
         s_nsf = (a.adaptive_alloc && sum_sigf > 0) ? __ddiv_rn(__dmul_rn(a.neval_frac, (double)a.neval), sum_sigf)
-                                             : 0.0;
+                                                 : 0.0;
         s_avg = (int64_t)((double)a.neval / (double)a.H);
-        if (blockIdx.x == 0) a.stats->neval_sigf = s_nsf;
+        if (s_b == 0) a.stats->neval_sigf = s_nsf;
     }
     if (build_table)
-        build_tablef(a, (int64_t)blockIdx.x * ALLOC_NT + threadIdx.x, (int64_t)gridDim.x * ALLOC_NT);
+        build_tablef(a, (int64_t)blockIdx.x * ALLOC_NT + t, (int64_t)gridDim.x * ALLOC_NT);
     __syncthreads();
+    const int64_t b = (int64_t)(s_b % (unsigned int)nblk);
+    const unsigned int epoch = s_epoch;
     const double nsf = s_nsf;
     const int64_t avg = s_avg;
     const int64_t mx = a.max_neval_hcube > a.min_neval_hcube ? a.max_neval_hcube : a.min_neval_hcube;
-    const int64_t hb = (int64_t)blockIdx.x * ALLOC_NT * ALLOC_PER + threadIdx.x;
-    int64_t s = 0, m = 0;
+    // counts of this thread's ALLOC_PER consecutive hypercubes
+    const int64_t h0 = (b * ALLOC_NT + t) * ALLOC_PER;
+    int64_t loc[ALLOC_PER];
+    int64_t sum = 0, m = 0;
 #pragma unroll
     for (int k = 0; k < ALLOC_PER; k++) {
-        const int64_t h = hb + k * ALLOC_NT;
-        if (h >= a.H) break;
-        int64_t n;
-        if (a.adaptive_alloc) {
-            n = (int64_t)__dmul_rn(a.sigf[h], nsf) + a.min_neval_hcube;
-            if (n > mx) n = mx;
-        } else {
-            n = avg;
+        const int64_t h = h0 + k;
+        int64_t n = 0;
+        if (h < a.H) {
+            if (a.adaptive_alloc) {
+                n = (int64_t)__dmul_rn(a.sigf[h], nsf) + a.min_neval_hcube;
+                if (n > mx) n = mx;
+            } else {
+                n = avg;
+            }
         }
-        a.neval_h[h] = (int32_t)n;
-        s += n;
+        loc[k] = n;
+        sum += n;
         m = n > m ? n : m;
     }
-    int64_t tot;
-    block_excl_scan<ALLOC_NT>(s, ssum, &tot);
-    const int64_t bm = block_max<ALLOC_NT>(m, ssum);
-    if (threadIdx.x == 0) {
-        a.bsum[blockIdx.x] = tot;
-        a.bmax[blockIdx.x] = bm;
-    }
-}
-
-// Exclusive scan of block totals (one CTA), totals, range, tile count.
-__global__ void __launch_bounds__(SCAN_NT) alloc_scan_kernel(IterArgs a, int64_t nblk)
-{
-    __shared__ int64_t wtot[SCAN_NT / 32];
-    const int t = threadIdx.x;
-    const int64_t per = (nblk + SCAN_NT - 1) / SCAN_NT;
-    const int64_t b = t * per, e = b + per < nblk ? b + per : nblk;
-    int64_t s = 0, m = 0;
-    for (int64_t i = b; i < e; i++) {
-        s += a.bsum[i];
-        m = a.bmax[i] > m ? a.bmax[i] : m;
-    }
-    int64_t N;
-    int64_t run = block_excl_scan<SCAN_NT>(s, wtot, &N);
-    const int64_t mx = block_max<SCAN_NT>(m, wtot);
-    for (int64_t i = b; i < e; i++) {
-        const int64_t v = a.bsum[i];
-        a.bsum[i] = run;   // becomes the block offset
-        run += v;
-    }
-    if (t == 0) {
-        vg_stats *st = a.stats;
-        st->neval = N;
-        // neval_hcube_range starts at [mnh, mnh] and every count is >= mnh
-        // (pyx:1681, 1701-1704)
-        st->range_lo = a.min_neval_hcube;
-        st->range_hi = a.adaptive_alloc ? (mx > a.min_neval_hcube ? mx : a.min_neval_hcube)
-                                        : a.min_neval_hcube;
-        int64_t ntiles = (N + BASE_TILE - 1) / BASE_TILE;
-        if (N > a.ncap || ntiles + 1 > a.ntiles_cap) {
-            st->status = VG_ERR_MEMORY;
-            ntiles = 0;
-        } else {
-            st->status = VG_OK;
-        }
-        st->ntiles = ntiles;
-        st->nan_seen = 0;
-        *a.counter = 0ull;
-        *a.fin_counter = 0u;
-    }
-}
-
-// Offsets (exclusive scan within the block + block offset) and tile heads;
-// each thread owns ALLOC_PER consecutive hypercubes.
-__global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
-{
-    __shared__ int64_t wtot[ALLOC_NT / 32];
-    const int t = threadIdx.x;
-    const int64_t h0 = ((int64_t)blockIdx.x * ALLOC_NT + t) * ALLOC_PER;
-    int64_t loc[ALLOC_PER];
-    int64_t s = 0;
     if (h0 + ALLOC_PER <= a.H) {   // 16-byte aligned: h0 is a multiple of 4
-        const int4 q = *reinterpret_cast<const int4 *>(a.neval_h + h0);
-        loc[0] = q.x;
-        loc[1] = q.y;
-        loc[2] = q.z;
-        loc[3] = q.w;
+        *reinterpret_cast<int4 *>(a.neval_h + h0) = make_int4((int)loc[0], (int)loc[1], (int)loc[2], (int)loc[3]);
     } else {
 #pragma unroll
-        for (int k = 0; k < ALLOC_PER; k++) loc[k] = (h0 + k < a.H) ? (int64_t)a.neval_h[h0 + k] : 0;
+        for (int k = 0; k < ALLOC_PER; k++)
+            if (h0 + k < a.H) a.neval_h[h0 + k] = (int32_t)loc[k];
     }
-#pragma unroll
-    for (int k = 0; k < ALLOC_PER; k++) s += loc[k];
     int64_t tot;
-    int64_t run = a.bsum[blockIdx.x] + block_excl_scan<ALLOC_NT>(s, wtot, &tot);
-    const vg_stats *st = a.stats;
-    const int64_t N = st->neval;
-    const int64_t ntiles = st->ntiles;
+    int64_t run = block_excl_scan<ALLOC_NT>(sum, wtot, &tot);
+    const int64_t bm = block_max<ALLOC_NT>(m, wtot);
+    if (t == 0) {
+        atomicMax(&sy->maxacc, (unsigned long long)bm);
+        __threadfence();
+        int64_t prefix = 0;
+        if (b == 0) {
+            st_release_u64(&flags[0], flag_word(epoch, FLAG_INC, tot));
+        } else {
+            st_release_u64(&flags[b], flag_word(epoch, FLAG_AGG, tot));
+            int ok = 1;
+            for (int64_t p = b - 1; p >= 0;) {
+                unsigned long long w = 0;
+                uint32_t i = 0;
+                for (; i < (1u << 24); i++) {
+                    w = ld_acquire_u64(&flags[p]);
+                    if ((unsigned int)(w >> 42) == (epoch & 0x3fffffu) && ((w >> 40) & 3u) != 0) break;
+                    if (i >= 64) __nanosleep(64);
+                }
+                if (i == (1u << 24)) {   // gave up: report, and let the later blocks finish
+                    ok = 0;
+                    break;
+                }
+                prefix += (int64_t)(w & ((1ull << 40) - 1));
+                if (((w >> 40) & 3u) == (unsigned)FLAG_INC) break;
+                p--;
+            }
+            if (!ok) atomicOr(&sy->err, 1u);
+            __threadfence();
+            st_release_u64(&flags[b], flag_word(epoch, FLAG_INC, prefix + tot));
+        }
+        s_prefix = prefix;
+    }
+    __syncthreads();
+    run += s_prefix;
 #pragma unroll
     for (int k = 0; k < ALLOC_PER; k++) {
         const int64_t h = h0 + k;
@@ -204,16 +214,43 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_offsets_kernel(IterArgs a)
         a.offsets[h] = run;
         // tiles whose first sample falls in [run, run + n)
         const int64_t n = loc[k];
-        for (int64_t tt = (run + BASE_TILE - 1) / BASE_TILE; tt * BASE_TILE < run + n && tt < ntiles; tt++)
+        for (int64_t tt = (run + BASE_TILE - 1) / BASE_TILE; tt * BASE_TILE < run + n && tt < a.ntiles_cap; tt++)
             a.tile_h0[tt] = h;
         run += n;
-        if (h == a.H - 1) {
-            a.offsets[a.H] = N;
+    }
+    if (b == nblk - 1 && t == 0) {   // every other block has published: totals, reset
+        __threadfence();
+        const int64_t N = s_prefix + tot;
+        const int64_t mxn = (int64_t)*(volatile unsigned long long *)&sy->maxacc;
+        const unsigned int err = *(volatile unsigned int *)&sy->err;
+        vg_stats *st = a.stats;
+        st->neval = N;
+        // neval_hcube_range starts at [mnh, mnh] and every count is >= mnh
+        // (pyx:1681, 1701-1704)
+        st->range_lo = a.min_neval_hcube;
+        st->range_hi = a.adaptive_alloc ? (mxn > a.min_neval_hcube ? mxn : a.min_neval_hcube) : a.min_neval_hcube;
+        int64_t ntiles = (N + BASE_TILE - 1) / BASE_TILE;
+        if (err) {
+            st->status = VG_ERR_TIMEOUT;
+            ntiles = 0;
+        } else if (N > a.ncap || ntiles + 1 > a.ntiles_cap) {
+            st->status = VG_ERR_MEMORY;
+            ntiles = 0;
+        } else {
+            st->status = VG_OK;
             a.tile_h0[ntiles] = a.H;   // sentinel
         }
+        a.offsets[a.H] = N;
+        st->ntiles = ntiles;
+        st->nan_seen = 0;
+        *a.counter = 0ull;
+        *a.fin_counter = 0u;
+        sy->maxacc = 0ull;
+        sy->err = 0u;
+        sy->epoch = epoch + 1u;
+        sy->ticket = 0u;
     }
 }
-
 
 // FP32 mode: the grid as an FP32 (x_node, inc) table for the tile CTAs.
 __global__ void tablef_kernel(IterArgs a)
@@ -413,7 +450,7 @@ __global__ void __launch_bounds__(FIN_TILES) finalize1_kernel(IterArgs a)
 
 // ================================================================ host
 struct WorkLayout {
-    size_t neval_h, offsets, bsum, bmax, tile_h0, counter, recs, parts, part2, feval, newgrid,
+    size_t neval_h, offsets, bsum, tile_h0, counter, recs, parts, part2, feval, newgrid,
         newinc, tablef, total;
     int64_t nblk, ntiles_cap, ncap;
 };
@@ -440,9 +477,8 @@ WorkLayout layout(const vg_integrator *it, int64_t ncap)
     L.neval_h = o; o = align256(o + sizeof(int32_t) * H);
     L.offsets = o; o = align256(o + sizeof(int64_t) * (H + 1));
     L.bsum = o;    o = align256(o + sizeof(int64_t) * L.nblk);
-    L.bmax = o;    o = align256(o + sizeof(int64_t) * L.nblk);
     L.tile_h0 = o; o = align256(o + sizeof(int64_t) * (L.ntiles_cap + 1));
-    L.counter = o; o = align256(o + sizeof(unsigned long long) + sizeof(unsigned int));
+    L.counter = o; o = align256(o + 16 + sizeof(AllocSync));
     L.recs = o;    o = align256(o + sizeof(TileRec) * 2 * L.ntiles_cap);
     L.parts = o;   o = align256(o + sizeof(TilePart) * L.ntiles_cap);
     L.part2 = o;   o = align256(o + sizeof(TilePart) * (L.ntiles_cap / FIN_TILES + 4096 / FIN_TILES + 2));
@@ -499,10 +535,10 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     a.neval_h = (int32_t *)(w + L.neval_h);
     a.offsets = (int64_t *)(w + L.offsets);
     a.bsum = (int64_t *)(w + L.bsum);
-    a.bmax = (int64_t *)(w + L.bmax);
     a.tile_h0 = (int64_t *)(w + L.tile_h0);
     a.counter = (unsigned long long *)(w + L.counter);
     a.fin_counter = (unsigned int *)(w + L.counter + sizeof(unsigned long long));
+    a.alloc_sync = (unsigned int *)(w + L.counter + 16);
     a.recs = (TileRec *)(w + L.recs);
     a.parts = (TilePart *)(w + L.parts);
     a.part2 = (TilePart *)(w + L.part2);
@@ -576,11 +612,7 @@ extern "C" int vg_allocate(const vg_integrator *it, void *stream)
     // grid has too few threads for it
     const int64_t ntab = (int64_t)a.dim * (a.maxK + 1);
     const int table_in_count = (it->precision == VG_F32) && ntab <= L.nblk * ALLOC_NT;
-    alloc_count_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a, table_in_count);
-    VG_LAUNCH_CHECK();
-    alloc_scan_kernel<<<1, SCAN_NT, 0, st>>>(a, L.nblk);
-    VG_LAUNCH_CHECK();
-    alloc_offsets_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a);
+    alloc_kernel<<<(unsigned)L.nblk, ALLOC_NT, 0, st>>>(a, L.nblk, table_in_count);
     VG_LAUNCH_CHECK();
     if (it->precision == VG_F32 && !table_in_count) {
         tablef_kernel<<<(unsigned)((ntab + 255) / 256), 256, 0, st>>>(a);

@@ -27,7 +27,6 @@ constexpr int NT = 256;          // threads per tile CTA
 constexpr int BASE_TILE = 256;   // granularity of the tile schedule tile_h0[]
 constexpr int ALLOC_NT = 256;    // allocation count / offsets blocks
 constexpr int ALLOC_PER = 4;     // hypercubes per thread there
-constexpr int SCAN_NT = 1024;    // the one-CTA scan of their block totals
 constexpr int FIN_NT = 1024;
 
 // POINTS: write points for a torch integrand; REDUCE: read f and reduce;
@@ -70,10 +69,11 @@ struct IterArgs {
     vg_stats *stats;
     int32_t *neval_h;
     int64_t *offsets;
-    int64_t *bsum, *bmax;
+    int64_t *bsum;            // allocation: published block totals / prefixes
     int64_t *tile_h0;         // first hypercube of each BASE_TILE samples
     unsigned long long *counter;  // dynamic tile counter (reset by allocation)
     unsigned int *fin_counter;    // finalize blocks done (reset by allocation)
+    unsigned int *alloc_sync;     // single-pass allocation: ticket, epoch, error, count maximum
     TileRec *recs;
     TilePart *parts;
     int64_t ntiles_cap;       // in BASE_TILE units
