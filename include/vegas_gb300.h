@@ -125,7 +125,9 @@ int vg_set_strata(int dim, int mode, int64_t *neval, int neval_given, const int6
 int64_t vg_neval_cap(const vg_integrator *it);
 
 /* Workspace for an iteration of at most neval_cap evaluations (bytes);
- * neval_cap <= 0 uses vg_neval_cap(it). */
+ * neval_cap <= 0 uses vg_neval_cap(it).  Zero it before its first use (and
+ * after a change of the strata): the single-pass allocation keeps its block
+ * ticket and epoch words in it. */
 size_t vg_workspace_bytes(const vg_integrator *it, int64_t neval_cap);
 
 /* -------------------------------------------------------- AdaptiveMap ops */
