@@ -621,6 +621,19 @@ extern "C" int vg_allocate(const vg_integrator *it, void *stream)
     return VG_OK;
 }
 
+// Clears the single-pass allocation's published block words and its
+// ticket / epoch for a workspace that other geometries have used (the
+// static scratch of vg_iteration_noalloc).
+int vg_alloc_sync_reset(const vg_integrator *it, void *stream)
+{
+    WorkLayout L = layout(it, neval_cap(it));
+    char *w = (char *)it->work;
+    cudaStream_t st = (cudaStream_t)stream;
+    VG_CUDA_CHECK(cudaMemsetAsync(w + L.bsum, 0, sizeof(int64_t) * (size_t)L.nblk, st));
+    VG_CUDA_CHECK(cudaMemsetAsync(w + L.counter, 0, 16 + sizeof(AllocSync), st));
+    return VG_OK;
+}
+
 static int reset_counter(IterArgs &a, cudaStream_t st)
 {
     VG_CUDA_CHECK(cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st));

@@ -19,6 +19,8 @@
 
 static __device__ __align__(256) unsigned char g_vg_noalloc_scratch[VG_NOALLOC_SCRATCH_BYTES];
 
+int vg_alloc_sync_reset(const vg_integrator *it, void *stream);   // vg_iter.cu
+
 namespace {
 std::mutex g_mutex;
 void *g_scratch[VG_MAX_DIM];   // device address of the array, per device ordinal
@@ -63,6 +65,9 @@ extern "C" int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const
                        need, VG_NOALLOC_SCRATCH_BYTES);
     local.work = scratch;
     local.work_bytes = (size_t)VG_NOALLOC_SCRATCH_BYTES;
+    // the scratch is shared by every geometry: start the allocation's
+    // published words afresh
+    if ((rc = vg_alloc_sync_reset(&local, stream))) return rc;
     if ((rc = vg_allocate(&local, stream))) return rc;
     if ((rc = vg_fused_iteration(&local, itn, u, kind, params, nparams, stream))) return rc;
     return vg_end_iteration(&local, stream);
