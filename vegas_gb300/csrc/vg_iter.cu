@@ -174,16 +174,24 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_kernel(IterArgs a, int64_t nbl
     int64_t tot;
     int64_t run = block_excl_scan<ALLOC_NT>(sum, wtot, &tot);
     const int64_t bm = block_max<ALLOC_NT>(m, wtot);
-    if (t == 0) {
-        atomicMax(&sy->maxacc, (unsigned long long)bm);
-        __threadfence();
+    // warp 0: publish the block total, then look back 32 predecessors at a
+    // time (each lane waits for one published word; the nearest inclusive
+    // prefix ends the walk)
+    if (t < 32) {
+        const int lane = t;
+        if (lane == 0) {
+            atomicMax(&sy->maxacc, (unsigned long long)bm);
+            __threadfence();
+            st_release_u64(&flags[b], flag_word(epoch, b == 0 ? FLAG_INC : FLAG_AGG, tot));
+        }
+        __syncwarp();
         int64_t prefix = 0;
-        if (b == 0) {
-            st_release_u64(&flags[0], flag_word(epoch, FLAG_INC, tot));
-        } else {
-            st_release_u64(&flags[b], flag_word(epoch, FLAG_AGG, tot));
-            int ok = 1;
-            for (int64_t p = b - 1; p >= 0;) {
+        int ok = 1;
+        for (int64_t hi = b - 1; hi >= 0; hi -= 32) {
+            const int64_t p = hi - lane;
+            int64_t v = 0;
+            int inc = 1;   // before block 0: an inclusive prefix of 0
+            if (p >= 0) {
                 unsigned long long w = 0;
                 uint32_t i = 0;
                 for (; i < (1u << 24); i++) {
@@ -191,19 +199,27 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_kernel(IterArgs a, int64_t nbl
                     if ((unsigned int)(w >> 42) == (epoch & 0x3fffffu) && ((w >> 40) & 3u) != 0) break;
                     if (i >= 64) __nanosleep(64);
                 }
-                if (i == (1u << 24)) {   // gave up: report, and let the later blocks finish
-                    ok = 0;
-                    break;
-                }
-                prefix += (int64_t)(w & ((1ull << 40) - 1));
-                if (((w >> 40) & 3u) == (unsigned)FLAG_INC) break;
-                p--;
+                if (i == (1u << 24)) ok = 0;   // gave up: reported below, the walk goes on
+                v = (int64_t)(w & ((1ull << 40) - 1));
+                inc = ((w >> 40) & 3u) == (unsigned)FLAG_INC;
             }
-            if (!ok) atomicOr(&sy->err, 1u);
-            __threadfence();
-            st_release_u64(&flags[b], flag_word(epoch, FLAG_INC, prefix + tot));
+            const unsigned int incm = __ballot_sync(0xffffffffu, inc);
+            const int first = incm ? __ffs(incm) - 1 : 32;
+            int64_t c = lane <= first ? v : 0;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+            prefix += c;
+            if (incm) break;
         }
-        s_prefix = prefix;
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) {
+            if (b > 0) {
+                if (!ok) atomicOr(&sy->err, 1u);
+                __threadfence();
+                st_release_u64(&flags[b], flag_word(epoch, FLAG_INC, prefix + tot));
+            }
+            s_prefix = prefix;
+        }
     }
     __syncthreads();
     run += s_prefix;
