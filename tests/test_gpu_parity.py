@@ -177,6 +177,39 @@ def test_fused_fp64_matches_oracle_philox():
             assert rel(r.itn_results[0].mean, out['mean']) <= 1e-9
 
 
+@pytest.mark.parametrize('dim,neval,alpha,beta,adapt', [
+    (1, 500, 0.5, 0.75, True),     # one axis
+    (3, 60, 0.5, 0.75, True),      # a handful of evaluations: few hypercubes, few increments
+    (6, 3000, 0.5, 0.0, True),     # beta = 0: uniform allocation, no sigf
+    (9, 4000, 0.5, 0.75, True),    # above 8 dimensions: the generic-dimension kernel
+    (12, 3000, 0.0, 0.75, True),   # alpha = 0: the map stays as it is
+    (4, 3000, 0.5, 0.75, False),   # adapt = False: neither sigf nor the map change
+])
+def test_fused_fp64_edge_shapes_match_oracle(dim, neval, alpha, beta, adapt):
+    """Fused FP64 iterations (Philox draws, one vg_iterate call each) ==
+    oracle on the same draws, for shapes and settings at the edges of the
+    sizing and adapt logic; each iteration starts from the oracle's state."""
+    f = vg.Gaussian(a=20.0, c=0.45, dim=dim)
+    I = vg.Integrator(dim * [[0, 1]], neval=neval, precision='fp64', seed=5, alpha=alpha, beta=beta,
+                      adapt=adapt)
+    st = O.State(dim * [[0, 1]], neval, alpha=alpha, beta=beta)
+    assert list(I.nstrat) == list(st.nstrat)
+    assert list(I.map.ninc) == list(st.ninc)
+    for itn in range(1, 4):
+        set_state(I, st.grid, st.sigf, st.sum_sigf)
+        r = I(f, nitn=1)
+        out = st.iterate(f.kind, f.params(dim), seed=5, stream=0, itn=itn, adapt=adapt)
+        assert I.last_neval == out['neval']
+        assert list(I.neval_hcube_range) == list(out['range'])
+        assert rel(r.itn_results[0].mean, out['mean']) <= RTOL
+        assert rel(r.itn_results[0].var, out['var']) <= RTOL
+        assert rel(I.sigf, st.sigf) <= RTOL
+        g = I.map.grid
+        for d in range(dim):
+            K = st.ninc[d]
+            assert np.max(np.abs(g[d, :K + 1] - st.grid[d, :K + 1])) <= RTOL
+
+
 def test_dropin_matches_fused_fp64():
     """lbatch torch integrand path == fused built-in path (same draws)."""
     f = vg.Ridge(M=40, s=0.05)
