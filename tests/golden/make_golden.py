@@ -302,6 +302,32 @@ def restratify_cases(V):
     return out
 
 
+def arr_f(x):
+    """Three-component integrand (correlated components)."""
+    x = np.asarray(x)
+    g = np.exp(-20.0 * np.sum((x - 0.45) ** 2, axis=1))
+    return np.stack([g, x[:, 0] * g, x[:, 1] * x[:, 2] * g], axis=1)
+
+
+def array_cases(v):
+    """Array-valued integrand, correlated and not (RAvgArray, pyx:2579-2879;
+    per-hypercube covariance sums, pyx:2149-2172), injected-sample mode."""
+    from gvar import evalcov
+    out = {}
+    for c, corr in enumerate((True, False)):
+        rec = Recorder(40 + c)
+        integ = v.Integrator(3 * [[0, 1]], neval=3000, ran_array_generator=rec, correlate_integrals=corr)
+        r = integ(v.lbatchintegrand(arr_f), nitn=3)
+        pre = 'c%d_' % c
+        out[pre + 'itn_mean'] = np.array([[g.mean for g in res] for res in r.itn_results])
+        out[pre + 'itn_cov'] = np.array([evalcov(list(res)) for res in r.itn_results])
+        out[pre + 'mean'] = np.array([g.mean for g in r])
+        out[pre + 'cov'] = evalcov(list(r))
+        out[pre + 'chi2'] = np.array(r.chi2)
+        out[pre + 'Q'] = np.array(r.Q)
+    return out
+
+
 class _ResultDict(dict):
     pass
 
@@ -312,6 +338,9 @@ def main(only=None):
     if only == ['restratify']:
         V = build_ref.import_reference_package()
         np.savez_compressed(os.path.join(HERE, 'ref_restratify.npz'), **restratify_cases(V))
+        return
+    if only == ['array']:
+        np.savez_compressed(os.path.join(HERE, 'ref_array.npz'), **array_cases(v))
         return
     np.savez_compressed(os.path.join(HERE, 'ref_gauss4_injected.npz'),
                         **trace(v, 4 * [[0, 1]], gauss4, nitn=3, neval=10000, seed=1,
@@ -334,5 +363,5 @@ def main(only=None):
 
 
 if __name__ == '__main__':
-    # no argument: every fixture; "restratify": that fixture only
+    # no argument: every fixture; "restratify" or "array": that fixture only
     main(sys.argv[1:] or None)

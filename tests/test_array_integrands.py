@@ -3,12 +3,16 @@
 GPU: the per-hypercube (co)variance kernel against a numpy restatement of
 the reference loops on the same samples, FP64 (1e-12 relative); an
 Integrator run returning an RAvgArray of the integrand's shape whose
-components agree with their exact values (5 sigma), correlated and not."""
+components agree with their exact values (5 sigma), correlated and not; and
+the same integrator, on the reference's injected uniforms, against the
+compiled reference's own results (tests/golden/ref_array.npz): means and
+covariance matrices per iteration and of the average, chi2 and Q."""
 import numpy as np
 import pytest
 import torch
 
 import vegas_gb300 as vg
+from vegas_gb300 import _gvar as gv
 from vegas_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
@@ -90,6 +94,46 @@ def test_array_reduction_many_uncorrelated_components():
     rm, rv = _ref_array_reduce(w[:n].cpu().numpy(), f.cpu().numpy(), hc[:n].cpu().numpy(), False)
     np.testing.assert_allclose(mean, rm, rtol=1e-12)
     np.testing.assert_allclose(var, rv, rtol=1e-11, atol=1e-300)
+
+
+class _Draws(object):
+    """The fixture's injected uniforms: u = k / 2^24, k from default_rng(seed)."""
+
+    def __init__(self, seed):
+        self.rng = np.random.default_rng(seed)
+
+    def __call__(self, size):
+        return self.rng.integers(0, 2 ** 24, size=size, dtype=np.uint32).astype(np.float64) * 2.0 ** -24
+
+
+@pytest.mark.parametrize('c,corr', [(0, True), (1, False)])
+def test_array_integrand_matches_reference_golden(c, corr):
+    """Three-component integrand against the compiled reference
+    (tests/golden/ref_array.npz, make_golden.py array), injected uniforms,
+    FP64: per-iteration means and covariance matrices, and the RAvgArray
+    average, chi2 and Q."""
+    import os
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'ref_array.npz')))
+    p = 'c%d_' % c
+
+    @vg.lbatchintegrand
+    def f(x):
+        gg = torch.exp(-20.0 * ((x - 0.45) ** 2).sum(dim=1))
+        return torch.stack([gg, x[:, 0] * gg, x[:, 1] * x[:, 2] * gg], dim=1)
+
+    I = vg.Integrator(3 * [[0, 1]], neval=3000, precision='fp64', ran_array_generator=_Draws(40 + c),
+                      correlate_integrals=corr)
+    r = I(f, nitn=3)
+    for k, res in enumerate(r.itn_results):
+        np.testing.assert_allclose([x.mean for x in res], g[p + 'itn_mean'][k], rtol=1e-10)
+        cov = gv.evalcov(list(res))
+        ref = g[p + 'itn_cov'][k]
+        assert np.max(np.abs(cov - ref)) <= 1e-9 * np.max(np.abs(ref))
+    np.testing.assert_allclose([x.mean for x in r], g[p + 'mean'], rtol=1e-10)
+    cov = gv.evalcov(list(r))
+    assert np.max(np.abs(cov - g[p + 'cov'])) <= 1e-9 * np.max(np.abs(g[p + 'cov']))
+    assert abs(r.chi2 - float(g[p + 'chi2'])) <= 1e-8 * max(1.0, abs(float(g[p + 'chi2'])))
+    assert abs(r.Q - float(g[p + 'Q'])) <= 1e-8
 
 
 def test_array_integrand_results():
