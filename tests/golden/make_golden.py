@@ -328,6 +328,25 @@ def array_cases(v):
     return out
 
 
+def jac_f(x, jac):
+    """Integrand that uses dx/dy per direction (uses_jac, pyx:265-295, 2127)."""
+    x = np.asarray(x)
+    jac = np.asarray(jac)
+    return np.exp(-x[:, 0]) * jac[:, 0] / (1.0 + jac[:, 1])
+
+
+def uses_jac_cases(v):
+    """uses_jac=True on a map adapted to peak2 (injected uniforms): the
+    integrand receives jac[n, dim] = dx/dy per direction."""
+    rec = Recorder(60)
+    integ = v.Integrator(2 * [[0, 1]], neval=2000, ran_array_generator=rec)
+    integ(v.lbatchintegrand(peak2), nitn=3)
+    r = integ(v.lbatchintegrand(jac_f), nitn=2, uses_jac=True)
+    return dict(itn_mean=np.array([g.mean for g in r.itn_results]),
+                itn_sdev=np.array([g.sdev for g in r.itn_results]),
+                mean=np.array(r.mean), sdev=np.array(r.sdev))
+
+
 class _ResultDict(dict):
     pass
 
@@ -341,6 +360,9 @@ def main(only=None):
         return
     if only == ['array']:
         np.savez_compressed(os.path.join(HERE, 'ref_array.npz'), **array_cases(v))
+        return
+    if only == ['uses_jac']:
+        np.savez_compressed(os.path.join(HERE, 'ref_uses_jac.npz'), **uses_jac_cases(v))
         return
     np.savez_compressed(os.path.join(HERE, 'ref_gauss4_injected.npz'),
                         **trace(v, 4 * [[0, 1]], gauss4, nitn=3, neval=10000, seed=1,
@@ -363,5 +385,5 @@ def main(only=None):
 
 
 if __name__ == '__main__':
-    # no argument: every fixture; "restratify" or "array": that fixture only
+    # no argument: every fixture; "restratify", "array" or "uses_jac": that fixture only
     main(sys.argv[1:] or None)

@@ -154,6 +154,29 @@ def test_array_integrand_results():
             assert 0.0 < c <= 1.0
 
 
+def test_uses_jac_matches_reference_golden():
+    """uses_jac=True on a map adapted to a peak, against the compiled
+    reference on the same injected uniforms (tests/golden/ref_uses_jac.npz,
+    make_golden.py uses_jac): the integrand gets dx/dy per direction."""
+    import os
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'ref_uses_jac.npz')))
+
+    @vg.lbatchintegrand
+    def peak2(x):
+        return torch.exp(-50.0 * (x[:, 0] - 0.3) ** 2) * (1.0 + x[:, 1] ** 2)
+
+    @vg.lbatchintegrand
+    def jac_f(x, jac):
+        return torch.exp(-x[:, 0]) * jac[:, 0] / (1.0 + jac[:, 1])
+
+    I = vg.Integrator(2 * [[0, 1]], neval=2000, precision='fp64', ran_array_generator=_Draws(60))
+    I(peak2, nitn=3)
+    r = I(jac_f, nitn=2, uses_jac=True)
+    np.testing.assert_allclose([x.mean for x in r.itn_results], g['itn_mean'], rtol=1e-10)
+    np.testing.assert_allclose([x.sdev for x in r.itn_results], g['itn_sdev'], rtol=1e-9)
+    np.testing.assert_allclose([r.mean, r.sdev], [g['mean'], g['sdev']], rtol=1e-9)
+
+
 def test_uses_jac_like_reference():
     """uses_jac=True: the integrand receives dx/dy per direction (reference
     test_vegas.py test_uses_jac: the integral of 1/prod(jac) over the map's
