@@ -53,10 +53,11 @@ def parse():
     ap.add_argument('--no-tta', action='store_true')
     ap.add_argument('--device-loop-only', action='store_true',
                     help='run only the device-resident iteration loop (for profilers)')
-    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch'],
+    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch', 'dropin'],
                     help='with --device-loop-only: which kernel family to run (for profilers): '
                          'ridge = the fused vegas+ iteration, flow = the flow sampling pass '
-                         '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals')
+                         '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals, '
+                         'dropin = the drop-in path (torch integrand, sampling and reduction kernels)')
     ap.add_argument('--no-batch', action='store_true', help='skip the batched many-integral line')
     return ap.parse_args()
 
@@ -128,6 +129,9 @@ def profile_case(args, dev):
         u = torch.rand(1 << 18, 8, device=dev, generator=g)
         for _ in range(args.warmup + args.steps):
             fl.sample(u)
+    elif args.case == 'dropin':
+        # the drop-in path's sampling and reduction kernels, 1e7 evaluations
+        dropin_line(dev, neval=10 ** 7, nitn=1, reps=max(1, args.steps))
     elif args.case == 'batch':
         from vegas_gb300.batch import BatchIntegrator
         fs, nevals, _ = batch_workload(256)

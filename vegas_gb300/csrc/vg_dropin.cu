@@ -11,7 +11,7 @@ int launch_points(IterArgs &a, int f64, cudaStream_t st)
         if (a.dim <= 8) return launch_tile<double, MODE_POINTS, 0, 8, 1>(a, nullptr, 0, st);
         return launch_tile<double, MODE_POINTS, 0, 64, 1>(a, nullptr, 0, st);
     }
-    if (a.dim <= 4) return launch_tile<float, MODE_POINTS, 0, 4, 1>(a, nullptr, 0, st);
+    if (a.dim <= 4) return launch_tile<float, MODE_POINTS, 0, 4, 2>(a, nullptr, 0, st);
     if (a.dim <= 8) return launch_tile<float, MODE_POINTS, 0, 8, 1>(a, nullptr, 0, st);
     if (a.dim <= 16) return launch_tile<float, MODE_POINTS, 0, 16, 1>(a, nullptr, 0, st);
     return launch_tile<float, MODE_POINTS, 0, 64, 1>(a, nullptr, 0, st);
@@ -23,7 +23,7 @@ int launch_reduce(IterArgs &a, int f64, cudaStream_t st)
         if (a.dim <= 8) return launch_tile<double, MODE_REDUCE, 0, 8, 2>(a, nullptr, 0, st);
         return launch_tile<double, MODE_REDUCE, 0, 64, 1>(a, nullptr, 0, st);
     }
-    if (a.dim <= 4) return launch_tile<float, MODE_REDUCE, 0, 4, 4>(a, nullptr, 0, st);
+    if (a.dim <= 4) return launch_tile<float, MODE_REDUCE, 0, 4, 2>(a, nullptr, 0, st);
     if (a.dim <= 8) return launch_tile<float, MODE_REDUCE, 0, 8, 4>(a, nullptr, 0, st);
     if (a.dim <= 16) return launch_tile<float, MODE_REDUCE, 0, 16, 2>(a, nullptr, 0, st);
     return launch_tile<float, MODE_REDUCE, 0, 64, 1>(a, nullptr, 0, st);

@@ -1369,13 +1369,17 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     }
 }
 
-// Resident CTAs per SM the register allocation targets for the fused FP32
-// ridge at dim <= 4: 4 with 2 samples per thread (64 registers; its shared
-// memory then holds no grid table), 2 with 4; 1 (no limit) otherwise.
+// Resident CTAs per SM the register allocation targets at dim <= 4 in FP32
+// for the fused ridge and for the drop-in path's sampling and reduction
+// kernels: 4 with 2 samples per thread (64 registers; the shared memory then
+// holds no grid table), 2 with 4; 1 (no limit) otherwise.
 template <typename T, int MODE, int KIND, int DIMB, int S>
 constexpr int tile_min_blocks()
 {
-    return (sizeof(T) == 4 && MODE == MODE_FUSED && KIND == VG_F_RIDGE && DIMB <= 4) ? (S == 2 ? 4 : 2) : 1;
+    return (sizeof(T) == 4 && DIMB <= 4 &&
+            ((MODE == MODE_FUSED && KIND == VG_F_RIDGE) || MODE == MODE_REDUCE || MODE == MODE_POINTS))
+               ? (S == 2 ? 4 : 2)
+               : 1;
 }
 
 template <typename T, int MODE, int KIND, int DIMB, int S>
