@@ -241,10 +241,12 @@ def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
         'roofline': {
             'bound': 'hbm', 'unit': 'GB/s', 'peak': hbm,
             'peak_source': 'MEASURED_PEAKS.json hbm_gbs' if 'hbm_gbs' in peaks else 'fallback',
+            'traffic_source': 'dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu, '
+                              'bench.py --device-loop-only --case dropin, 9.33e6 evaluations)',
             'sample_kernel': {'bytes_per_eval': b_s, 'achieved': b_s * n / t_s / 1e9,
-                              'frac': b_s * n / t_s / 1e9 / hbm},
+                              'frac': b_s * n / t_s / 1e9 / hbm, 'traffic': 181.6e6},
             'reduce_kernel': {'bytes_per_eval': b_r, 'achieved': b_r * n / t_r / 1e9,
-                              'frac': b_r * n / t_r / 1e9 / hbm,
+                              'frac': b_r * n / t_r / 1e9 / hbm, 'traffic': 54.0e6,
                               'note': 'regenerates each sample (Philox, map) and forms the two-pass '
                                       'hypercube sums and the training histogram: bound by that '
                                       'work, not by its 4 bytes per evaluation'}},
