@@ -228,8 +228,10 @@ int vg_iterate(const vg_integrator *it, uint32_t itn, int kind, const double *pa
  * array of VG_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
  * until the process exits; an iteration whose vg_workspace_bytes() exceeds it
  * fails with VG_ERR_MEMORY.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the one array: calls that overlap on the
+ * device address (cudaGetSymbolAddress) and caches it per device; make that
+ * first call before any stream capture.  The cache assumes the device's
+ * primary context stays alive (after a cudaDeviceReset the address may
+ * change).  All calls share the one array: calls that overlap on the
  * GPU (other streams, other threads) race and must be serialised by the
  * caller.  Every scratch region is rewritten before it is read; the tile
  * counter is zeroed on every call.
@@ -355,11 +357,16 @@ int vg_weight_points(int64_t n, const float *f, const float *jac, const float *l
  * iteration's mean and variance, res (device double[njobs][4]) the weighted
  * average over the iterations after the first nwarm (mean, sdev, chi2, dof).
  * stats->sum_sigf of each integral must hold its starting value (nhcube for
- * a fresh one).  status (device int) becomes VG_ERR_TIMEOUT if a bounded
+ * a fresh one).  cfg[b] = VG_BATCH_CFG_F64 selects the FP64 parity
+ * configuration instead: integrals with precision VG_F64 (Lorentzian
+ * products of dim <= 8), sampling, map, evaluation and every sum in FP64, the
+ * arithmetic of vg_fused_iteration's FP64 mode, for checks against the CPU
+ * oracle; FP32 integrals need one of the FP32 configurations.  status (device int) becomes VG_ERR_TIMEOUT if a bounded
  * group barrier gave up.  vg_batch_launch neither allocates nor
  * synchronises, so it can be captured in a CUDA graph (after a
  * vg_batch_prepare on the same device, which creates the forked streams).
  */
+#define VG_BATCH_CFG_F64 16
 int vg_batch_variants(void);
 size_t vg_batch_table_bytes(int njobs);
 int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, const double *params, int ldp,
@@ -373,6 +380,17 @@ int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm,
  * adds the number of Gaussian terms it evaluates -- the ones that can be
  * nonzero in FP32; the rest are exactly zero and skipped. */
 int vg_set_term_counter(unsigned long long *count);
+
+/* Bounded device-side waits (the allocation's look-back over its
+ * predecessors' published totals; the batched launch's group barriers, four
+ * times as many polls): how many polls a wait makes before it gives up and
+ * the iteration reports VG_ERR_TIMEOUT in its vg_stats.status (the batched
+ * launch in its status word) with no tiles scheduled.  Negative: the default
+ * (2^24).  Read when an iteration's arguments are filled (vg_allocate,
+ * vg_iterate, vg_iteration_noalloc, vg_batch_prepare).  No counterpart in the
+ * reference, which has no device waits; its errors surface as exceptions
+ * (pyx:2133-2134, 1355-1356), which the Python layer raises for a status. */
+int vg_set_wait_budget(int64_t iters);
 
 /* Tuning: how FP32 iterations of the many-term ridge run -- 0 automatic
  * (currently the fused kernel), 1 the single fused evaluate+reduce kernel,

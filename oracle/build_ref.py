@@ -21,7 +21,11 @@ etc.) is not compiled; ``import_reference_package`` loads it straight from the
 reference tree on top of the compiled module when a golden generator needs
 ``restratify``.  ``gvar`` (not installed) is replaced by ``oracle/gvar_stub``.
 
-Usage:  python oracle/build_ref.py [--reference /root/reference]
+The reference tree is taken from ``--reference``, else from the environment
+variable ``VEGAS_REFERENCE``, else from a directory named ``reference`` beside
+this repository's root (``default_reference()``).
+
+Usage:  python oracle/build_ref.py [--reference DIR]
 """
 import argparse
 import glob
@@ -33,6 +37,14 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, '_ref', 'vegas')
+
+
+def default_reference():
+    """The reference tree: $VEGAS_REFERENCE, else ``reference`` beside the repository root."""
+    env = os.environ.get('VEGAS_REFERENCE')
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), 'reference')
 
 PATCHES = [
     ("answer = (x[:neval_batch, :],)", "answer = (numpy.asarray(x[:neval_batch, :]),)"),
@@ -53,9 +65,10 @@ def built():
     return bool(glob.glob(os.path.join(OUT, '_vegas*.so')))
 
 
-def build(reference='/root/reference', force=False):
+def build(reference=None, force=False):
     if built() and not force:
         return OUT
+    reference = reference or default_reference()
     src = os.path.join(reference, 'src', 'vegas')
     if not os.path.isdir(src):
         raise FileNotFoundError('reference sources not found at %s' % src)
@@ -95,10 +108,11 @@ def import_reference():
     return _vegas
 
 
-def import_reference_package(reference='/root/reference'):
+def import_reference_package(reference=None):
     """The reference package ``vegas`` (src/vegas/__init__.py, read from the
     reference tree) with ``vegas._vegas`` resolved to the compiled module."""
     import importlib.util
+    reference = reference or default_reference()
     stub = os.path.join(HERE, 'gvar_stub')
     if stub not in sys.path:
         sys.path.insert(0, stub)
@@ -113,7 +127,7 @@ def import_reference_package(reference='/root/reference'):
 
 if __name__ == '__main__':
     ap = argparse.ArgumentParser()
-    ap.add_argument('--reference', default='/root/reference')
+    ap.add_argument('--reference', default=None)
     ap.add_argument('--force', action='store_true')
     a = ap.parse_args()
     print(build(a.reference, a.force))

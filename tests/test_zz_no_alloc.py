@@ -5,9 +5,16 @@ that must not allocate on their iteration path).
 
 Checked through the C ABI against the ordinary path (vg_allocate +
 vg_fused_iteration + vg_end_iteration with a caller workspace) on two calls
-in a row, both paths starting each call from the same state, at the
-tolerance of the other parity tests (1e-12 relative).  This file is
-collected last so that a failure here does not hide any other test."""
+in a row, both paths starting each call from the same state, in both
+precision modes.  FP64: the tolerance of the other FP64 parity tests (1e-12
+relative).  FP32 (which also uses the FP32 grid table and the split
+evaluation buffer of the scratch): the iteration sums are deterministic
+(static per-tile partials summed in a fixed order), 1e-12 as well; the
+adapted grid comes from an FP32 training histogram summed with atomics in
+arrival order, so it is compared at 1e-5 relative, the FP32 first-iteration
+tolerance of the batched tests widened by the adapt's cumulative sums.
+This file is collected last so that a failure here does not hide any other
+test."""
 import ctypes
 
 import numpy as np
@@ -39,12 +46,14 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
-def test_noalloc_matches_workspace_path():
+@pytest.mark.parametrize('precision', ['fp32', 'fp64'])
+def test_noalloc_matches_workspace_path(precision):
     L = N.load()
     f = vg.Ridge(M=200, s=0.02)
     params = N.dbl_array(f.params(4))
-    ref = vg.Integrator(4 * [[0, 1]], neval=20000, precision='fp64', seed=31)
-    new = vg.Integrator(4 * [[0, 1]], neval=20000, precision='fp64', seed=31)
+    ref = vg.Integrator(4 * [[0, 1]], neval=20000, precision=precision, seed=31)
+    new = vg.Integrator(4 * [[0, 1]], neval=20000, precision=precision, seed=31)
+    grid_tol = RTOL if precision == 'fp64' else 1e-5
     stream = N.stream_ptr(ref.device)
     for call in range(2):
         _load(new, _state(ref))
@@ -67,7 +76,7 @@ def test_noalloc_matches_workspace_path():
         assert _rel(st_n.sum_sigf, st_r.sum_sigf) <= RTOL
         assert _rel(new.sigf, ref.sigf) <= RTOL
         g_n, g_r = new.map.grid, ref.map.grid
-        assert np.max(np.abs(g_n - g_r)) <= RTOL * np.max(np.abs(g_r))
+        assert np.max(np.abs(g_n - g_r)) <= grid_tol * np.max(np.abs(g_r))
         ref.sum_sigf = float(st_r.sum_sigf)
 
 

@@ -27,6 +27,7 @@ NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-r
 
 VG_MAX_DIM = 64
 VG_NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
+VG_BATCH_CFG_F64 = 16
 VG_F32, VG_F64 = 0, 1
 VG_OK, VG_ERR_VALUE, VG_ERR_MEMORY, VG_ERR_CUDA, VG_ERR_NAN, VG_ERR_UNSUPPORTED, VG_ERR_TIMEOUT = range(7)
 (VG_F_GAUSS, VG_F_RIDGE, VG_F_LORENTZ, VG_F_MIXTURE, VG_F_LATTICE, VG_F_CONST) = range(6)
@@ -85,7 +86,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=max(2, min(len(cmds), os.cpu_count() or 4))) as ex:
         list(ex.map(run, cmds))
     tmp = LIBPATH + '.%d.tmp' % os.getpid()
-    run([nvcc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lm'])
+    run([nvcc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lm', '-ldl'])
     os.replace(tmp, LIBPATH)
     return LIBPATH
 
@@ -172,6 +173,7 @@ SIGNATURES = {
     'vg_flow_train_batch': (I32, [I64, I64, U64, U32, I32, P, P, P, P, P, I32, P, P, P, P]),
     'vg_set_term_counter': (I32, [P]),
     'vg_set_eval_split': (I32, [I32]),
+    'vg_set_wait_budget': (I32, [I64]),
     'vg_set_tile_tuning': (I32, [I32, I32, I32]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),
@@ -206,6 +208,10 @@ class VegasError(RuntimeError):
     pass
 
 
+class VegasTimeout(VegasError):
+    """A bounded device-side wait gave up (VG_ERR_TIMEOUT)."""
+
+
 def check(rc):
     """Map a C-ABI status onto the exception the reference raises."""
     if rc == VG_OK:
@@ -217,6 +223,8 @@ def check(rc):
         raise MemoryError(msg)
     if rc == VG_ERR_UNSUPPORTED:
         raise NotImplementedError(msg)
+    if rc == VG_ERR_TIMEOUT:
+        raise VegasTimeout('vegas_gb300 error %d: %s' % (rc, msg))
     raise VegasError('vegas_gb300 error %d: %s' % (rc, msg))
 
 

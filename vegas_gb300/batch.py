@@ -49,12 +49,19 @@ class BatchIntegrator(object):
         alpha, beta, seed: as ``Integrator``; integral j uses Philox stream j.
         variant: tile configuration per dimension bucket, a sequence of 3
             (or one int for all buckets); None: autotune.
+        precision: 'fp32' (default: FP32 sampling, map and evaluation,
+            float-float and FP64 sums) or 'fp64' (the parity configuration:
+            everything in FP64, the arithmetic of ``Integrator(precision=
+            'fp64')``; Lorentzian products of dim <= 8 only, no autotuning).
     """
 
     def __init__(self, integrands, nevals, nitn=16, nwarm=8, alpha=0.5, beta=0.75, seed=1,
                  variant=None, device=None, neval_frac=0.75, max_neval_hcube=50000, dims=None,
-                 limits=(0.0, 1.0), group=None):
+                 limits=(0.0, 1.0), group=None, precision='fp32'):
         self.device = _device(device)
+        if precision not in ('fp32', 'fp64'):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.precision = precision
         self.integrands = list(integrands)
         self.njobs = len(self.integrands)
         if self.njobs < 1:
@@ -79,7 +86,9 @@ class BatchIntegrator(object):
         self._itn = 0
         self.variant = None
         self._graph = None
-        if variant is None:
+        if precision == 'fp64':
+            variant = (N.VG_BATCH_CFG_F64,) * 3
+        elif variant is None:
             variant = self.autotune()
         self.set_variant(variant)
 
@@ -95,7 +104,7 @@ class BatchIntegrator(object):
             sz = strata(d, 0, int(nevals[j]), True, np.zeros(d, np.int64), self.neval_frac, self.beta)
             it = self.its[j]
             it.dim = d
-            it.precision = N.VG_F32
+            it.precision = N.VG_F64 if self.precision == 'fp64' else N.VG_F32
             H = int(np.prod(sz['nstrat']))
             it.nhcube = H
             K = int(sz['ninc'].max())
@@ -253,13 +262,51 @@ class BatchIntegrator(object):
         """Per integral: mean, sdev, chi2, dof of the weighted average over the
         iterations after the warm-up ones (numpy [njobs, 4])."""
         if int(self.status.item()) != 0:
-            raise N.VegasError('batched launch: a group barrier timed out (status %d)'
-                               % int(self.status.item()))
+            raise N.VegasTimeout('batched launch: a group barrier timed out (status %d)'
+                                 % int(self.status.item()))
         return self.res.cpu().numpy()
 
     def iterations(self):
         """Every iteration's (mean, variance) (numpy [njobs, nitn, 2])."""
         return self.out.cpu().numpy()
+
+    def integrator_struct(self, j):
+        """The C-ABI record of integral j (device pointers into the arena:
+        grid, inc, sigf, training histogram, stats, workspace)."""
+        return self.its[j]
+
+    def state(self, j):
+        """Views into the arena of integral j's device state: ``grid``
+        [dim, ldg] and ``inc`` [dim, ldi] (FP64), ``sigf`` [nhcube], the
+        ``stats`` record (bytes, ``N.VgStats``) and ``neval_h`` [nhcube]
+        (int32, the last iteration's allocation, at the start of its
+        workspace).  Writing into them changes the integral's state."""
+        it = self.its[j]
+        base = self.arena.data_ptr()
+        d, H = int(it.dim), int(it.nhcube)
+
+        def view(ptr, nbytes):
+            o = int(ptr) - base
+            return self.arena[o:o + nbytes]
+
+        return {
+            'grid': view(it.grid, 8 * d * it.ldg).view(torch.float64).view(d, int(it.ldg)),
+            'inc': view(it.inc, 8 * d * it.ldi).view(torch.float64).view(d, int(it.ldi)),
+            'sigf': view(it.sigf, 8 * H).view(torch.float64),
+            'stats': view(it.stats, ctypes.sizeof(N.VgStats)),
+            'neval_h': view(it.work, 4 * H).view(torch.int32),
+        }
+
+    def read_stats(self, j):
+        """Integral j's iteration record (``N.VgStats``: sum_sigf, neval, range...)."""
+        b = self.state(j)['stats'].cpu().numpy().tobytes()
+        return N.VgStats.from_buffer_copy(b)
+
+    def put_sum_sigf(self, j, value):
+        """Set integral j's carried sum_sigf (the allocation's normaliser)."""
+        st = self.read_stats(j)
+        st.sum_sigf = float(value)
+        self.state(j)['stats'].copy_(torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8))
 
     def evaluations(self):
         """Evaluations of the last launch summed over integrals and iterations."""

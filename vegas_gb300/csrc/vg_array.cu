@@ -188,6 +188,7 @@ extern "C" int vg_reduce_array(const vg_integrator *it, const void *f, int f_dty
                                const double *wgt, double *mean_out, double *var_out, void *work,
                                size_t work_bytes, void *stream)
 {
+    VG_RANGE("vg_reduce_array");
     vg_clear_error();
     vg::IterArgs a;
     int rc = vg::fill_iter_args(a, it, 0, nullptr);

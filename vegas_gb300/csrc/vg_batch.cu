@@ -12,6 +12,7 @@
 // vg_fused_iteration.
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "vg_batch.cuh"
@@ -28,6 +29,9 @@ int launch_b16(int, int, const BatchJob *, const VgParams *, const int *, int, i
 int occupancy_b4(int, int, size_t, int *);
 int occupancy_b8(int, int, size_t, int *);
 int occupancy_b16(int, int, size_t, int *);
+int launch_f64(const BatchJob *, const VgParams *, const int *, int, int, int, uint32_t, unsigned int *, size_t, int,
+               int, int *, cudaStream_t);
+int occupancy_f64(size_t, int *);
 }  // namespace vgbatch
 
 namespace {
@@ -49,6 +53,7 @@ int bucket_of(int dim) { return dim <= 4 ? 0 : (dim <= 8 ? 1 : 2); }
 
 int occupancy_dispatch(int b, int kind, int cfg, size_t smem, int *per_sm)
 {
+    if (cfg == VG_BATCH_CFG_F64) return occupancy_f64(smem, per_sm);
     if (b == 0) return occupancy_b4(kind, cfg, smem, per_sm);
     if (b == 1) return occupancy_b8(kind, cfg, smem, per_sm);
     return occupancy_b16(kind, cfg, smem, per_sm);
@@ -58,6 +63,8 @@ int launch_dispatch(int b, int kind, int cfg, const BatchJob *jobs, const VgPara
                     int nitn, int nwarm, uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group,
                     int *status, cudaStream_t st)
 {
+    if (cfg == VG_BATCH_CFG_F64)
+        return launch_f64(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status, st);
     if (b == 0)
         return launch_b4(kind, cfg, jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid, group, status, st);
     if (b == 1)
@@ -66,26 +73,45 @@ int launch_dispatch(int b, int kind, int cfg, const BatchJob *jobs, const VgPara
 }
 
 // Streams the bucket kernels run on besides the caller's, and the events of
-// the fork and the join (created outside any capture, by vg_batch_prepare).
+// the fork and the join, per device ordinal (created once, outside any
+// capture, by vg_batch_prepare; never replaced).
 struct AuxStreams {
-    int dev = -1;
     cudaStream_t s[NBUCKET];
     cudaEvent_t fork, join[NBUCKET];
 };
-AuxStreams g_aux;
+std::mutex g_aux_mutex;
+AuxStreams *g_aux[VG_MAX_DEVICES];
+
+int current_device(int *dev)
+{
+    VG_CUDA_CHECK(cudaGetDevice(dev));
+    if (*dev < 0 || *dev >= VG_MAX_DEVICES) return vg_fail(VG_ERR_UNSUPPORTED, "device ordinal %d", *dev);
+    return VG_OK;
+}
 
 int ensure_aux()
 {
-    int dev = 0;
-    VG_CUDA_CHECK(cudaGetDevice(&dev));
-    if (g_aux.dev == dev) return VG_OK;
+    int dev = 0, rc = current_device(&dev);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_aux_mutex);
+    if (g_aux[dev] != nullptr) return VG_OK;
+    AuxStreams a;
     for (int b = 0; b < NBUCKET; b++) {
-        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_aux.s[b], cudaStreamNonBlocking));
-        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_aux.join[b], cudaEventDisableTiming));
+        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&a.s[b], cudaStreamNonBlocking));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&a.join[b], cudaEventDisableTiming));
     }
-    VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_aux.fork, cudaEventDisableTiming));
-    g_aux.dev = dev;
+    VG_CUDA_CHECK(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
+    g_aux[dev] = new AuxStreams(a);
     return VG_OK;
+}
+
+// The current device's streams, or nullptr before vg_batch_prepare ran on it.
+AuxStreams *aux_of_current()
+{
+    int dev = 0;
+    if (current_device(&dev)) return nullptr;
+    std::lock_guard<std::mutex> lock(g_aux_mutex);
+    return g_aux[dev];
 }
 
 }  // namespace
@@ -102,12 +128,14 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
                                 const int *cfg, void *table, size_t table_bytes, size_t *smem_out, int *grid_out,
                                 void *stream)
 {
+    VG_RANGE("vg_batch_prepare");
     vg_clear_error();
     if (njobs < 1) return vg_fail(VG_ERR_VALUE, "no integrals");
     if (kind != VG_F_LORENTZ && kind != VG_F_LATTICE)
         return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: Lorentzian products and the lattice action only");
     for (int b = 0; b < NBUCKET; b++)
-        if (cfg[b] < 0 || cfg[b] >= NCONFIG) return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
+        if ((cfg[b] < 0 || cfg[b] >= NCONFIG) && cfg[b] != VG_BATCH_CFG_F64)
+            return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
     if (nitn < 1) return vg_fail(VG_ERR_VALUE, "nitn < 1");
     if (table_bytes < vg_batch_table_bytes(njobs)) return vg_fail(VG_ERR_VALUE, "job table too small");
     int rc = ensure_aux();
@@ -118,17 +146,23 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
     int present[NBUCKET] = {0, 0, 0};
     for (int j = 0; j < njobs; j++) {
         const vg_integrator *it = &its[j];
-        if (it->precision != VG_F32) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch computes in FP32");
+        const int dim = it->dim;
+        if (dim < 1 || dim > 16) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: dim %d outside 1..16", dim);
+        const int b = bucket_of(dim);
+        const int f64 = it->precision == VG_F64;
+        if (f64 != (cfg[b] == VG_BATCH_CFG_F64))
+            return vg_fail(VG_ERR_VALUE, "batched launch: FP64 integrals need configuration VG_BATCH_CFG_F64 "
+                                         "and FP32 integrals one of the FP32 configurations");
+        if (f64 && (kind != VG_F_LORENTZ || dim > F64_DIMB))
+            return vg_fail(VG_ERR_UNSUPPORTED, "batched FP64 configuration: Lorentzian products of dim <= %d",
+                           F64_DIMB);
         BatchJob &J = jobs[(size_t)j];
         memset(&J, 0, sizeof(J));
         if ((rc = vg::fill_iter_args(J.a, it, 0, nullptr))) return rc;
         int tab_len = 0;
         if ((rc = vg_build_params(kind, it->dim, params + (size_t)j * ldp, nparams[j], &prm[(size_t)j], &tab_len)))
             return rc;
-        const int dim = it->dim;
-        if (dim > 16) return vg_fail(VG_ERR_UNSUPPORTED, "batched launch: dim %d above 16", dim);
-        const int b = bucket_of(dim);
-        const BucketConfig C = BUCKET_CONFIGS[b][cfg[b]];
+        const BucketConfig C = f64 ? F64_CONFIG : BUCKET_CONFIGS[b][cfg[b]];
         J.bucket = b;
         present[b] = 1;
         IterArgs &a = J.a;
@@ -142,14 +176,18 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
         // training histogram (global atomics)
         a.table_smem = 1;
         a.hist_smem = bins;
-        vg::SmemPlan p = vg::smem_plan<float>(dim, a.maxK, TT, 1, a.hist_smem, tab_len, bins, 1);
+        auto plan = [&](int table, int hist) {
+            return f64 ? vg::smem_plan<double>(dim, a.maxK, TT, table, hist, tab_len, bins, 1)
+                       : vg::smem_plan<float>(dim, a.maxK, TT, table, hist, tab_len, bins, 1);
+        };
+        vg::SmemPlan p = plan(1, a.hist_smem);
         if (p.total > budget) {
             a.table_smem = 0;
-            p = vg::smem_plan<float>(dim, a.maxK, TT, 0, a.hist_smem, tab_len, bins, 1);
+            p = plan(0, a.hist_smem);
         }
         if (p.total > budget && a.hist_smem) {
             a.hist_smem = 0;
-            p = vg::smem_plan<float>(dim, a.maxK, TT, 0, 0, tab_len, bins, 1);
+            p = plan(0, 0);
         }
         if (p.total > 220 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "shared memory plan too large");
         size_t need = p.total;
@@ -175,7 +213,7 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
             ad.ldi_new = it->ldi;
             ad.max_old = max_old;
             ad.sequential = 1;
-            ad.fast = 1;
+            ad.fast = f64 ? 0 : 1;
             const size_t an = sizeof(double) * (2 * (size_t)max_old + vg::NT);
             need = an > need ? an : need;
         }
@@ -211,11 +249,11 @@ extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn,
                                const int *group, int *status, const size_t *smem, const int *grid, const int *cfg,
                                void *stream)
 {
+    VG_RANGE("vg_batch_launch");
     vg_clear_error();
     if (nwarm < 0 || nwarm >= nitn) return vg_fail(VG_ERR_VALUE, "need 0 <= nwarm < nitn");
-    int dev = 0;
-    VG_CUDA_CHECK(cudaGetDevice(&dev));
-    if (g_aux.dev != dev) return vg_fail(VG_ERR_VALUE, "vg_batch_prepare was not called on this device");
+    AuxStreams *aux = aux_of_current();
+    if (aux == nullptr) return vg_fail(VG_ERR_VALUE, "vg_batch_prepare was not called on this device");
     cudaStream_t st = (cudaStream_t)stream;
     const BatchJob *jobs = (const BatchJob *)table;
     const VgParams *prm = (const VgParams *)((const char *)table + table_jobs_bytes(njobs));
@@ -223,7 +261,8 @@ extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn,
     for (int b = 0; b < NBUCKET; b++) {
         if (seg[2 * b + 1] <= 0) continue;
         npresent++;
-        if (cfg[b] < 0 || cfg[b] >= NCONFIG) return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
+        if ((cfg[b] < 0 || cfg[b] >= NCONFIG) && cfg[b] != VG_BATCH_CFG_F64)
+            return vg_fail(VG_ERR_VALUE, "bucket %d: configuration %d", b, cfg[b]);
         if (seg[2 * b] < 0 || seg[2 * b] + seg[2 * b + 1] > njobs) return vg_fail(VG_ERR_VALUE, "bucket segment");
         if (grid[b] < 1) return vg_fail(VG_ERR_VALUE, "bucket %d was not prepared", b);
         if (group[b] > 1) {
@@ -242,7 +281,7 @@ extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn,
     VG_CUDA_CHECK(cudaMemsetAsync(queue, 0, sizeof(unsigned int) * NBUCKET, st));
     // fork: the first bucket (largest dimension first) runs on the caller's
     // stream, the others on their own streams after it was enqueued
-    if (npresent > 1) VG_CUDA_CHECK(cudaEventRecord(g_aux.fork, st));
+    if (npresent > 1) VG_CUDA_CHECK(cudaEventRecord(aux->fork, st));
     int first = 1;
     int joined[NBUCKET] = {0, 0, 0};
     for (int b = NBUCKET - 1; b >= 0; b--) {
@@ -250,20 +289,20 @@ extern "C" int vg_batch_launch(const void *table, int njobs, int kind, int nitn,
         if (n <= 0) continue;
         cudaStream_t sb = st;
         if (!first) {
-            sb = g_aux.s[b];
-            VG_CUDA_CHECK(cudaStreamWaitEvent(sb, g_aux.fork, 0));
+            sb = aux->s[b];
+            VG_CUDA_CHECK(cudaStreamWaitEvent(sb, aux->fork, 0));
         }
         const int g = group[b] > 1 ? n * group[b] : (grid[b] < n ? grid[b] : n);
         int rc = launch_dispatch(b, kind, cfg[b], jobs, prm, order + seg[2 * b], n, nitn, nwarm, itn0, queue + b,
                                  smem[b], g, group[b] > 1 ? group[b] : 1, status, sb);
         if (rc) return rc;
         if (!first) {
-            VG_CUDA_CHECK(cudaEventRecord(g_aux.join[b], sb));
+            VG_CUDA_CHECK(cudaEventRecord(aux->join[b], sb));
             joined[b] = 1;
         }
         first = 0;
     }
     for (int b = 0; b < NBUCKET; b++)
-        if (joined[b]) VG_CUDA_CHECK(cudaStreamWaitEvent(st, g_aux.join[b], 0));
+        if (joined[b]) VG_CUDA_CHECK(cudaStreamWaitEvent(st, aux->join[b], 0));
     return VG_OK;
 }

@@ -30,9 +30,10 @@ struct BatchJob {
 
 // Barrier of the G CTAs working on one integral (group mode; the launch is
 // cooperative, so they are co-resident).  Thread 0 releases this CTA's
-// writes, arrives, and waits (bounded) until all G arrived `round` times.
+// writes, arrives, and waits (at most 4 wait_iters polls) until all G
+// arrived `round` times.
 // Returns false when the wait gave up.
-__device__ __forceinline__ bool group_barrier(unsigned int *ctr, unsigned int target)
+__device__ __forceinline__ bool group_barrier(unsigned int *ctr, unsigned int target, uint32_t wait_iters)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -40,7 +41,8 @@ __device__ __forceinline__ bool group_barrier(unsigned int *ctr, unsigned int ta
         __threadfence();
         atomicAdd(ctr, 1u);
         int ok = 0;
-        for (uint32_t i = 0; i < (1u << 26); i++) {
+        const uint64_t budget = 4ull * wait_iters;
+        for (uint64_t i = 0; i < budget; i++) {
             unsigned int v;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
             if (v >= target) {
@@ -188,6 +190,81 @@ static __device__ __noinline__ void cta_finalize(const IterArgs &a, int ngroup, 
     __syncthreads();
 }
 
+// FP64 mode: the hypercube whose first piece is the tail record of tile t,
+// merged in FP64 with its pieces in the following tiles (Chan et al.'s
+// parallel-variance update, the FP64 finalize's formulas); adds its mean,
+// variance and sigf to the compensated sums and stores its sigf.
+static __device__ __noinline__ void merge_cut_f64(const IterArgs &a, int64_t t, int64_t ntiles, VgKSum &cm,
+                                                  VgKSum &cv, VgKSum &cs)
+{
+    const TileRec r = a.recs[2 * t + 1];
+    if (r.h < 0) return;
+    double n = r.n, Sx = r.S, Q = r.Q, D = r.D;
+    for (int64_t t2 = t + 1; t2 < ntiles; t2++) {
+        const TileRec q = a.recs[2 * t2];
+        if (q.h != r.h) break;
+        const double n2 = n + q.n;
+        const double delta = q.S / q.n - Sx / n;
+        Q = Q + q.Q + delta * delta * (n * q.n / n2);
+        Sx += q.S;
+        D += q.D;
+        n = n2;
+        if (!q.spans) break;
+    }
+    const double num = __dsub_rn(__dmul_rn(n, Q), __dmul_rn(D, D));
+    const double vh = __ddiv_rn(num, __dsub_rn(n, 1.));
+    cm.add(__dadd_rn(Sx, D));
+    cv.add(vh);
+    if (a.adaptive) {
+        const double sg = pow(fabs(vh), a.beta_half);
+        a.sigf[r.h] = sg;
+        cs.add(sg);
+    }
+}
+
+// FP64 mode (the parity configuration of the batched launch): the group
+// CTAs' FP64 partials plus the merged cut hypercubes, compensated FP64 sums
+// in a fixed order; sum_sigf and the constant-integrand reset as
+// cta_finalize.
+static __device__ __noinline__ void cta_finalize_f64(const IterArgs &a, int ngroup, VgKSum *red, int *flag)
+{
+    const int tid = threadIdx.x;
+    vg_stats *st = a.stats;
+    const int64_t N = st->neval;
+    const int64_t ntiles = st->ntiles ? (N + a.T - 1) / a.T : 0;
+    VgKSum cm = {0.0, 0.0}, cv = {0.0, 0.0}, cs = {0.0, 0.0};
+    if (tid < ngroup && ntiles > 0) {
+        const TilePart p = a.parts[tid];
+        cm = p.mean;
+        cv = p.var;
+        cs = p.sigf;
+    }
+    for (int64_t t = tid; t < ntiles; t += NT) merge_cut_f64(a, t, ntiles, cm, cv, cs);
+    const VgKSum M = vg_block_ksum<NT>(cm, red);
+    const VgKSum V = vg_block_ksum<NT>(cv, red);
+    const VgKSum Sg = vg_block_ksum<NT>(cs, red);
+    if (tid == 0) {
+        st->mean = M.value();
+        st->var = V.value();
+        st->sigf_reset = 0;
+        *flag = 0;
+        if (a.adaptive) {
+            const double ss = Sg.value();
+            if (ss > 0) {
+                st->sum_sigf = ss;
+            } else {
+                st->sum_sigf = (double)a.H;
+                st->sigf_reset = 1;
+                *flag = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (*flag)
+        for (int64_t h = tid; h < a.H; h += NT) a.sigf[h] = 1.0;
+    __syncthreads();
+}
+
 // End of iteration: adapt the map (one axis after another), copy the new
 // grid back, clear the training histogram (vg_end_iteration's work).
 static __device__ __noinline__ void cta_adapt(const BatchJob &J, const IterArgs &a, unsigned char *smem)
@@ -243,7 +320,8 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
 }
 
 // The persistent kernel of one dimension bucket (every integral it takes has
-// dim <= DIMB): S samples per thread and MINB CTAs per SM it is compiled for
+// dim <= DIMB): sampling, map and evaluation in T (float; double in the
+// FP64 parity configuration), S samples per thread and MINB CTAs per SM it is compiled for
 // (the tile shape and occupancy the autotuner picks per bucket; one kernel
 // per bucket lets the small-dimension integrals run at the occupancy their
 // registers and shared memory allow).
@@ -253,7 +331,7 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
 // order[c / G] as rank c % G; rank 0 allocates, finalizes and adapts, all G
 // ranks share the tiles (rank r takes tiles r, r + G, ...), with two group
 // barriers per iteration.
-template <int KIND, int DIMB, int S, int MINB>
+template <typename T, int KIND, int DIMB, int S, int MINB>
 __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restrict__ jobs,
                                                    const VgParams *__restrict__ params,
                                                    const int *__restrict__ order, int njobs, int nitn,
@@ -297,12 +375,13 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
             if (tid == 0) sa.itn = itn0 + (uint32_t)it;
             __syncthreads();
             if (rank == 0) cta_alloc(sa, scan);
-            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
-            if (sa.stats->ntiles > 0) tile_body<float, MODE_FUSED, KIND, DIMB, S>(sa, params[j], smem, rank, G, rank);
+            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds, sa.wait_iters))) break;
+            if (sa.stats->ntiles > 0) tile_body<T, MODE_FUSED, KIND, DIMB, S>(sa, params[j], smem, rank, G, rank);
             __syncthreads();
-            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds))) break;
+            if (G > 1 && !(ok = group_barrier(J.sync, (unsigned)G * ++rounds, sa.wait_iters))) break;
             if (rank == 0) {
-                cta_finalize(sa, G, red, &s_flag);
+                if constexpr (sizeof(T) == 8) cta_finalize_f64(sa, G, red, &s_flag);
+                else cta_finalize(sa, G, red, &s_flag);
                 if (tid == 0) {
                     J.out[2 * it] = sa.stats->mean;
                     J.out[2 * it + 1] = sa.stats->var;
@@ -322,11 +401,11 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
 
 // Launch (queue mode, or cooperative for co-resident groups) and occupancy
 // of one instantiation; the bucket files dispatch to these.
-template <int KIND, int DIMB, int S, int MINB>
+template <typename T, int KIND, int DIMB, int S, int MINB>
 int launch_one(const BatchJob *jobs, const VgParams *prm, const int *order, int njobs, int nitn, int nwarm,
                uint32_t itn0, unsigned int *queue, size_t smem, int grid, int group, int *status, cudaStream_t st)
 {
-    auto k = batch_kernel<KIND, DIMB, S, MINB>;
+    auto k = batch_kernel<T, KIND, DIMB, S, MINB>;
     if (group > 1) {
         void *args[] = {(void *)&jobs, (void *)&prm, (void *)&order, (void *)&njobs, (void *)&nitn, (void *)&nwarm,
                         (void *)&itn0, (void *)&queue, (void *)&group, (void *)&status};
@@ -339,10 +418,10 @@ int launch_one(const BatchJob *jobs, const VgParams *prm, const int *order, int 
 }
 
 // sets the kernel's shared-memory attribute (outside any stream capture)
-template <int KIND, int DIMB, int S, int MINB>
+template <typename T, int KIND, int DIMB, int S, int MINB>
 int occupancy_one(size_t smem, int *per_sm)
 {
-    auto k = batch_kernel<KIND, DIMB, S, MINB>;
+    auto k = batch_kernel<T, KIND, DIMB, S, MINB>;
     VG_CUDA_CHECK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     VG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, NT, smem));
     return VG_OK;
@@ -355,6 +434,11 @@ struct BucketConfig {
 constexpr int NCONFIG = 3;
 constexpr int NBUCKET = 3;
 constexpr int BUCKET_DIM[NBUCKET] = {4, 8, 16};
+// FP64 parity configuration (cfg VG_BATCH_CFG_F64): Lorentzian products of
+// dim <= 8 (buckets 0 and 1 share the one instantiation), 2 samples per
+// thread, one CTA per SM -- the single-integral FP64 kernel's tile shape.
+constexpr BucketConfig F64_CONFIG = {2, 1};
+constexpr int F64_DIMB = 8;
 constexpr BucketConfig BUCKET_CONFIGS[NBUCKET][NCONFIG] = {
     {{2, 4}, {4, 2}, {2, 2}},   // dim <= 4
     {{2, 2}, {4, 1}, {2, 3}},   // dim <= 8
@@ -372,13 +456,13 @@ int bucket_launch(int cfg, const BatchJob *jobs, const VgParams *prm, const int 
     constexpr BucketConfig c0 = BUCKET_CONFIGS[b][0], c1 = BUCKET_CONFIGS[b][1], c2 = BUCKET_CONFIGS[b][2];
     switch (cfg) {
     case 0:
-        return launch_one<KIND, DIMB, c0.S, c0.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+        return launch_one<float, KIND, DIMB, c0.S, c0.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
                                                      group, status, st);
     case 1:
-        return launch_one<KIND, DIMB, c1.S, c1.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+        return launch_one<float, KIND, DIMB, c1.S, c1.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
                                                      group, status, st);
     default:
-        return launch_one<KIND, DIMB, c2.S, c2.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
+        return launch_one<float, KIND, DIMB, c2.S, c2.minb>(jobs, prm, order, njobs, nitn, nwarm, itn0, queue, smem, grid,
                                                      group, status, st);
     }
 }
@@ -389,9 +473,9 @@ int bucket_occupancy(int cfg, size_t smem, int *per_sm)
     constexpr int b = DIMB == 4 ? 0 : (DIMB == 8 ? 1 : 2);
     constexpr BucketConfig c0 = BUCKET_CONFIGS[b][0], c1 = BUCKET_CONFIGS[b][1], c2 = BUCKET_CONFIGS[b][2];
     switch (cfg) {
-    case 0: return occupancy_one<KIND, DIMB, c0.S, c0.minb>(smem, per_sm);
-    case 1: return occupancy_one<KIND, DIMB, c1.S, c1.minb>(smem, per_sm);
-    default: return occupancy_one<KIND, DIMB, c2.S, c2.minb>(smem, per_sm);
+    case 0: return occupancy_one<float, KIND, DIMB, c0.S, c0.minb>(smem, per_sm);
+    case 1: return occupancy_one<float, KIND, DIMB, c1.S, c1.minb>(smem, per_sm);
+    default: return occupancy_one<float, KIND, DIMB, c2.S, c2.minb>(smem, per_sm);
     }
 }
 

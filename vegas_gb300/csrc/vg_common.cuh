@@ -1,9 +1,23 @@
 // vg_common.cuh -- device helpers shared by the vegas+ kernels (sm_103a).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "vg_internal.h"
+
+// NVTX range around an entry point's enqueue work (host side), so that a
+// profiler's timeline groups each call's kernels under the ABI name.  The
+// NVTX3 calls are no-ops unless a profiling tool is attached.
+struct VgRange {
+    explicit VgRange(const char *name) { nvtxRangePushA(name); }
+    ~VgRange() { nvtxRangePop(); }
+    VgRange(const VgRange &) = delete;
+    VgRange &operator=(const VgRange &) = delete;
+};
+#define VG_RANGE_CAT2(a, b) a##b
+#define VG_RANGE_CAT(a, b) VG_RANGE_CAT2(a, b)
+#define VG_RANGE(name) VgRange VG_RANGE_CAT(vg_range_, __LINE__)(name)
 
 #define VG_TINY 1e-257                       // _vegas.pyx:34
 #define VG_EPSILON (2.220446049250313e-16 * 1e4)  // _vegas.pyx:36

@@ -1364,6 +1364,7 @@ extern "C" int64_t vg_flow_train_bytes(const vg_flow *fl, int64_t nrows)
 
 extern "C" int vg_flow_refresh(const vg_flow *fl, void *stream)
 {
+    VG_RANGE("vg_flow_refresh");
     vg_clear_error();
     FlowGeom g;
     int rc = geom_of(g, fl);
@@ -1448,6 +1449,7 @@ static int flow_pass(const vg_flow *fl, int dir, int64_t n, const float *zin, fl
 extern "C" int vg_flow_sample(const vg_flow *fl, int64_t n, const float *zhat, float *z,
                               float *logdet, void *stream)
 {
+    VG_RANGE("vg_flow_sample");
     vg_clear_error();
     return flow_pass(fl, 1, n, zhat, z, logdet, nullptr, (cudaStream_t)stream);
 }
@@ -1455,6 +1457,7 @@ extern "C" int vg_flow_sample(const vg_flow *fl, int64_t n, const float *zhat, f
 extern "C" int vg_flow_density(const vg_flow *fl, int64_t n, const float *z, float *zhat,
                                float *logdet, void *stream)
 {
+    VG_RANGE("vg_flow_density");
     vg_clear_error();
     return flow_pass(fl, 0, n, z, zhat, logdet, nullptr, (cudaStream_t)stream);
 }
@@ -1462,6 +1465,7 @@ extern "C" int vg_flow_density(const vg_flow *fl, int64_t n, const float *z, flo
 extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const float *w,
                             void *work, size_t work_bytes, void *stream)
 {
+    VG_RANGE("vg_flow_grad");
     vg_clear_error();
     FlowGeom g;
     int rc = geom_of(g, fl);
@@ -1530,6 +1534,7 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
 extern "C" int vg_flow_adam(const vg_flow *fl, float scale, float lr, float beta1, float beta2,
                             float eps, int step, float clip, void *stream)
 {
+    VG_RANGE("vg_flow_adam");
     vg_clear_error();
     FlowGeom g;
     int rc = geom_of(g, fl);
@@ -1565,6 +1570,7 @@ extern "C" int vg_flow_train_batch(int64_t n, int64_t m, uint64_t seed, uint32_t
                                    const float *f, const double *wgt, const int64_t *hc, const int32_t *neval_h,
                                    int chi2, float *zs, float *ws, double *scratch, void *stream)
 {
+    VG_RANGE("vg_flow_train_batch");
     vg_clear_error();
     if (n < 1 || m < 1 || n >= ((int64_t)1 << 32)) return vg_fail(VG_ERR_VALUE, "training batch sizes");
     if (dim < 1 || dim > FMAXD) return vg_fail(VG_ERR_UNSUPPORTED, "flow dim %d", dim);

@@ -3,6 +3,10 @@
 #define VG_INTERNAL_H
 #include "../../include/vegas_gb300.h"
 
+/* Per-device host caches (forked streams, the no-alloc scratch address) are
+ * indexed by device ordinal below this bound. */
+#define VG_MAX_DEVICES 64
+
 #ifdef __cplusplus
 extern "C" {
 #endif

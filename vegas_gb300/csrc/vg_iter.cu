@@ -26,6 +26,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "vg_adapt.cuh"
 #include "vg_tile.cuh"
 
@@ -194,12 +196,13 @@ __global__ void __launch_bounds__(ALLOC_NT) alloc_kernel(IterArgs a, int64_t nbl
             if (p >= 0) {
                 unsigned long long w = 0;
                 uint32_t i = 0;
-                for (; i < (1u << 24); i++) {
+                const uint32_t budget = a.wait_iters;
+                for (; i < budget; i++) {
                     w = ld_acquire_u64(&flags[p]);
                     if ((unsigned int)(w >> 42) == (epoch & 0x3fffffu) && ((w >> 40) & 3u) != 0) break;
                     if (i >= 64) __nanosleep(64);
                 }
-                if (i == (1u << 24)) ok = 0;   // gave up: reported below, the walk goes on
+                if (i == budget) ok = 0;   // gave up: reported below, the walk goes on
                 v = (int64_t)(w & ((1ull << 40) - 1));
                 inc = ((w >> 40) & 3u) == (unsigned)FLAG_INC;
             }
@@ -571,6 +574,7 @@ int fill_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *
     a.u = u;
     a.dv_y = 1.0 / (double)it->nhcube;
     a.beta_half = it->beta / 2.0;
+    a.wait_iters = g_wait_iters;
     return VG_OK;
 }
 
@@ -612,12 +616,17 @@ extern "C" int64_t vg_neval_cap(const vg_integrator *it) { return neval_cap(it);
 
 extern "C" size_t vg_workspace_bytes(const vg_integrator *it, int64_t ncap)
 {
+    if (it == nullptr || it->dim < 1 || it->dim > VG_MAX_DIM) {   // layout() reads ninc[0 .. dim)
+        vg_fail(VG_ERR_VALUE, "vg_workspace_bytes: dim outside 1..%d", VG_MAX_DIM);
+        return 0;
+    }
     if (ncap <= 0) ncap = neval_cap(it);
     return layout(it, ncap).total;
 }
 
 extern "C" int vg_allocate(const vg_integrator *it, void *stream)
 {
+    VG_RANGE("vg_allocate");
     vg_clear_error();
     IterArgs a;
     int rc = fill_args(a, it, 0, nullptr);
@@ -659,6 +668,7 @@ static int reset_counter(IterArgs &a, cudaStream_t st)
 extern "C" int vg_sample(const vg_integrator *it, uint32_t itn, const double *u, void *x, void *y,
                          double *wgt, int64_t *hcube, int64_t n_cap, void *stream)
 {
+    VG_RANGE("vg_sample");
     vg_clear_error();
     IterArgs a;
     int rc = fill_args(a, it, itn, u);
@@ -680,6 +690,7 @@ extern "C" int vg_sample(const vg_integrator *it, uint32_t itn, const double *u,
 extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u, const void *f,
                          int f_dtype, void *stream)
 {
+    VG_RANGE("vg_reduce");
     vg_clear_error();
     IterArgs a;
     int rc = fill_args(a, it, itn, u);
@@ -693,6 +704,7 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
 
 static unsigned long long *g_term_count = nullptr;
 namespace vg {
+uint32_t g_wait_iters = VG_WAIT_ITERS_DEFAULT;
 int g_eval_split = 0;
 int g_tile_s4 = 0, g_tile_table = -1, g_tile_hist = -1;
 }
@@ -709,6 +721,18 @@ extern "C" int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem)
     vg::g_tile_s4 = s_dim4;
     vg::g_tile_table = table_smem;
     vg::g_tile_hist = hist_smem;
+    return VG_OK;
+}
+
+// Polls of the bounded device-side waits (allocation look-back; four times
+// as many for the batched launch's group barriers) before they give up and
+// report VG_ERR_TIMEOUT; a negative value restores the default.  Read when
+// an iteration's arguments are filled (vg_allocate, vg_iterate, ...,
+// vg_batch_prepare).
+extern "C" int vg_set_wait_budget(int64_t iters)
+{
+    vg::g_wait_iters = iters < 0 ? VG_WAIT_ITERS_DEFAULT
+                                 : (iters > 0xffffffffll ? 0xffffffffu : (uint32_t)iters);
     return VG_OK;
 }
 
@@ -768,11 +792,12 @@ int vg_build_params(int kind, int dim, const double *params, int nparams, VgPara
 extern "C" int vg_fused_iteration(const vg_integrator *it, uint32_t itn, const double *u, int kind,
                                   const double *params, int nparams, void *stream)
 {
+    VG_RANGE("vg_fused_iteration");
     vg_clear_error();
     IterArgs a;
     int rc = fill_args(a, it, itn, u);
     if (rc) return rc;
-    static VgParams P;
+    VgParams P;   // copied into the kernel arguments at launch
     int tab_len = 0;
     if ((rc = vg_build_params(kind, it->dim, params, nparams, &P, &tab_len))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
@@ -791,6 +816,7 @@ int vg_adapt_in_place_ok(int max_old);
 
 extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
 {
+    VG_RANGE("vg_end_iteration");
     vg_clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     if (!(it->adapt && it->alpha > 0)) return VG_OK;
@@ -830,22 +856,42 @@ extern "C" int vg_end_iteration(const vg_integrator *it, void *stream)
 // on the first call on a device (outside any stream capture).
 namespace {
 struct IterAux {
-    int dev = -1;
     cudaStream_t s;
     cudaEvent_t fork, join;
 };
-IterAux g_iter_aux;
+std::mutex g_iter_aux_mutex;
+IterAux *g_iter_aux[VG_MAX_DEVICES];   // per device ordinal; created once, never replaced
+
+// The forked stream and events of the current device, created on the first
+// call on that device.
+int iter_aux(IterAux **out)
+{
+    int dev = 0;
+    VG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= VG_MAX_DEVICES) return vg_fail(VG_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lock(g_iter_aux_mutex);
+    if (g_iter_aux[dev] == nullptr) {
+        IterAux a;
+        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&a.fork, cudaEventDisableTiming));
+        VG_CUDA_CHECK(cudaEventCreateWithFlags(&a.join, cudaEventDisableTiming));
+        g_iter_aux[dev] = new IterAux(a);
+    }
+    *out = g_iter_aux[dev];
+    return VG_OK;
+}
 }  // namespace
 
 extern "C" int vg_iterate(const vg_integrator *it, uint32_t itn, int kind, const double *params, int nparams,
                           void *stream)
 {
+    VG_RANGE("vg_iterate");
     int rc = vg_allocate(it, stream);
     if (rc) return rc;
     vg_clear_error();
     IterArgs a;
     if ((rc = fill_args(a, it, itn, nullptr))) return rc;
-    static VgParams P;
+    VgParams P;   // copied into the kernel arguments at launch
     int tab_len = 0;
     if ((rc = vg_build_params(kind, it->dim, params, nparams, &P, &tab_len))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
@@ -857,19 +903,13 @@ extern "C" int vg_iterate(const vg_integrator *it, uint32_t itn, int kind, const
         if ((rc = vg::finalize_launch(a, st, it->precision == VG_F32))) return rc;
         return vg_end_iteration(it, stream);
     }
-    int dev = 0;
-    VG_CUDA_CHECK(cudaGetDevice(&dev));
-    if (g_iter_aux.dev != dev) {
-        VG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_iter_aux.s, cudaStreamNonBlocking));
-        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_iter_aux.fork, cudaEventDisableTiming));
-        VG_CUDA_CHECK(cudaEventCreateWithFlags(&g_iter_aux.join, cudaEventDisableTiming));
-        g_iter_aux.dev = dev;
-    }
-    VG_CUDA_CHECK(cudaEventRecord(g_iter_aux.fork, st));
-    VG_CUDA_CHECK(cudaStreamWaitEvent(g_iter_aux.s, g_iter_aux.fork, 0));
-    rc = vg_end_iteration(it, g_iter_aux.s);
-    VG_CUDA_CHECK(cudaEventRecord(g_iter_aux.join, g_iter_aux.s));
+    IterAux *aux = nullptr;
+    if ((rc = iter_aux(&aux))) return rc;
+    VG_CUDA_CHECK(cudaEventRecord(aux->fork, st));
+    VG_CUDA_CHECK(cudaStreamWaitEvent(aux->s, aux->fork, 0));
+    rc = vg_end_iteration(it, aux->s);
+    VG_CUDA_CHECK(cudaEventRecord(aux->join, aux->s));
     if (rc == VG_OK) rc = vg::finalize_launch(a, st, it->precision == VG_F32);
-    VG_CUDA_CHECK(cudaStreamWaitEvent(st, g_iter_aux.join, 0));
+    VG_CUDA_CHECK(cudaStreamWaitEvent(st, aux->join, 0));
     return rc;
 }

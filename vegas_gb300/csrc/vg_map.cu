@@ -158,6 +158,7 @@ int fill_geom(MapGeom &g, int dim, const int64_t *ninc)
 extern "C" int vg_make_uniform(int dim, const int64_t *ninc, const double *xl, const double *xu,
                                double *grid, int64_t ldg, double *inc, int64_t ldi, void *stream)
 {
+    VG_RANGE("vg_make_uniform");
     vg_clear_error();
     MapGeom g;
     int rc = fill_geom(g, dim, ninc);
@@ -197,6 +198,7 @@ __global__ void jac1d_kernel(MapGeom g, const double *__restrict__ inc, int64_t 
 extern "C" int vg_jac1d(int dim, const int64_t *ninc, const double *inc, int64_t ldi, int64_t n,
                         const void *y, void *out, int dtype, void *stream)
 {
+    VG_RANGE("vg_jac1d");
     vg_clear_error();
     MapGeom g;
     int rc = fill_geom(g, dim, ninc);
@@ -217,6 +219,7 @@ extern "C" int vg_map(int dim, const int64_t *ninc, const double *grid, const do
                       int64_t ldg, int64_t ldi, int64_t n, const void *y, void *x, void *jac,
                       int dtype, void *stream)
 {
+    VG_RANGE("vg_map");
     vg_clear_error();
     MapGeom g;
     int rc = fill_geom(g, dim, ninc);
@@ -280,6 +283,7 @@ extern "C" int vg_invmap(int dim, const int64_t *ninc, const double *grid, const
                          int64_t ldg, int64_t ldi, int64_t n, const void *x, void *y, void *jac,
                          int dtype, void *stream)
 {
+    VG_RANGE("vg_invmap");
     vg_clear_error();
     MapGeom g;
     int rc = fill_geom(g, dim, ninc);
@@ -301,6 +305,7 @@ extern "C" int vg_add_training_data(int dim, const int64_t *ninc, int64_t ldi, i
                                     const void *y, const void *f, int dtype, double *sum_f,
                                     uint64_t *n_f, void *stream)
 {
+    VG_RANGE("vg_add_training_data");
     vg_clear_error();
     MapGeom g;
     int rc = fill_geom(g, dim, ninc);
@@ -401,6 +406,7 @@ extern "C" int vg_adapt(int dim, const int64_t *old_ninc, const int64_t *new_nin
                         const double *sum_f, const uint64_t *n_f, double alpha, double *new_grid,
                         double *new_inc, int64_t ldg_new, int64_t ldi_new, void *stream)
 {
+    VG_RANGE("vg_adapt");
     vg_clear_error();
     if (new_grid == grid) return vg_fail(VG_ERR_VALUE, "vg_adapt writes a separate grid");
     return vg_adapt_launch(dim, old_ninc, new_ninc, grid, inc, ldg, ldi, sum_f, n_f, alpha,

@@ -23,17 +23,19 @@ int vg_alloc_sync_reset(const vg_integrator *it, void *stream);   // vg_iter.cu
 
 namespace {
 std::mutex g_mutex;
-void *g_scratch[VG_MAX_DIM];   // device address of the array, per device ordinal
+void *g_scratch[VG_MAX_DEVICES];   // device address of the array, per device ordinal
 }  // namespace
 
 // Device address of the scratch array for the current device.  The first
 // call on a device looks it up with cudaGetSymbolAddress (the host-side name
-// of the array is only a stand-in, never a device address).
+// of the array is only a stand-in, never a device address).  The cached
+// address assumes the device's primary context stays alive: after a
+// cudaDeviceReset the module is loaded again and the address may change.
 static int scratch_address(void **out)
 {
     int dev = 0;
     VG_CUDA_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= VG_MAX_DIM) return vg_fail(VG_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    if (dev < 0 || dev >= VG_MAX_DEVICES) return vg_fail(VG_ERR_UNSUPPORTED, "device ordinal %d", dev);
     std::lock_guard<std::mutex> lock(g_mutex);
     if (g_scratch[dev] == nullptr) {
         void *p = nullptr;
@@ -49,7 +51,11 @@ static int scratch_address(void **out)
 extern "C" int vg_iteration_noalloc(const vg_integrator *it, uint32_t itn, const double *u, int kind,
                                     const double *params, int nparams, void *stream)
 {
+    VG_RANGE("vg_iteration_noalloc");
     vg_clear_error();
+    if (it == nullptr) return vg_fail(VG_ERR_VALUE, "vg_iteration_noalloc: no integrator");
+    if (it->dim < 1 || it->dim > VG_MAX_DIM)   // before anything reads ninc[0 .. dim)
+        return vg_fail(VG_ERR_VALUE, "vg_iteration_noalloc: dim %d outside 1..%d", it->dim, VG_MAX_DIM);
     void *scratch = nullptr;
     int rc = scratch_address(&scratch);
     if (rc) return rc;

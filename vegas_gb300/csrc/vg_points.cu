@@ -84,6 +84,7 @@ __global__ void weight_kernel(int64_t n, const float *__restrict__ f, const floa
 extern "C" int vg_weight_points(int64_t n, const float *f, const float *jac, const float *logdet, float *out,
                                 void *stream)
 {
+    VG_RANGE("vg_weight_points");
     vg_clear_error();
     if (n <= 0) return VG_OK;
     int64_t nb = (n + 255) / 256;
@@ -98,10 +99,11 @@ extern "C" int vg_eval_points(int kind, const double *params, int nparams, int d
                               const float *z, const double *lo, const double *width,
                               const float *logdet, const float *jac, float *f, void *stream)
 {
+    VG_RANGE("vg_eval_points");
     vg_clear_error();
     if (dim < 1 || dim > VG_MAX_DIM) return vg_fail(VG_ERR_VALUE, "dim %d out of range", dim);
     if (n < 0) return vg_fail(VG_ERR_VALUE, "negative point count");
-    static VgParams P;
+    VgParams P;   // copied into the kernel arguments at launch
     int tab_len = 0, rc;
     if ((rc = vg_build_params(kind, dim, params, nparams, &P, &tab_len))) return rc;
     if (sizeof(float) * (tab_len + 4) > 48 * 1024) return vg_fail(VG_ERR_UNSUPPORTED, "integrand table too large");

@@ -25,6 +25,8 @@ namespace vg {
 
 constexpr int NT = 256;          // threads per tile CTA
 constexpr int BASE_TILE = 256;   // granularity of the tile schedule tile_h0[]
+#define VG_WAIT_ITERS_DEFAULT (1u << 24)   // polls of a bounded wait (vg_set_wait_budget)
+extern uint32_t g_wait_iters;
 constexpr int ALLOC_NT = 256;    // allocation count / offsets blocks
 constexpr int ALLOC_PER = 4;     // hypercubes per thread there
 constexpr int FIN_NT = 1024;
@@ -100,6 +102,8 @@ struct IterArgs {
     int ncta;                 // CTAs of the launched reduction kernel (one partial each)
     double dv_y;              // 1 / nhcube (pyx:1639)
     double beta_half;         // beta / 2 (pyx:2185)
+    uint32_t wait_iters;      // polls of a bounded wait before it gives up (vg_set_wait_budget)
+    uint32_t pad_wait;
 };
 
 template <typename T>

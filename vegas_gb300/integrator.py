@@ -593,6 +593,9 @@ class Integrator(object):
         of its neval, neval range and sum_sigf."""
         if st.status == N.VG_ERR_MEMORY:
             raise MemoryError('iteration exceeded its evaluation capacity')
+        elif st.status == N.VG_ERR_TIMEOUT:
+            raise N.VegasTimeout('a bounded device-side wait gave up (allocation look-back); '
+                                 'the iteration scheduled no work')
         elif st.status != 0:
             raise N.VegasError('device status %d' % st.status)
         if st.nan_seen:
