@@ -46,8 +46,8 @@ RIDGE_M, RIDGE_S = 1000, 0.01
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
-    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--steps', type=int, default=3000)
+    ap.add_argument('--warmup', type=int, default=10)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-tta', action='store_true')
@@ -59,6 +59,8 @@ def parse():
                          '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals, '
                          'dropin = the drop-in path (torch integrand, sampling and reduction kernels)')
     ap.add_argument('--no-batch', action='store_true', help='skip the batched many-integral line')
+    ap.add_argument('--no-reference-runs', action='store_true',
+                    help='skip the normal-mode comparisons with oracle runs of the same workloads')
     return ap.parse_args()
 
 
@@ -160,13 +162,14 @@ def batch_workload(njobs=4096, seed=2024):
 def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
     """The drop-in path: a torch lbatch integrand (the dim-4 Gaussian
     (100/pi)^2 exp(-100 sum (x-1/2)^2) written in torch ops) through
-    Integrator.__call__ -- sampling + map kernel (vg_sample), the integrand's
-    own torch kernels, reduction + training histogram kernel (vg_reduce),
-    adapt.  Evaluations/s through the API, and the HBM roofline of the
-    sampling and reduction kernels: algorithmic bytes per evaluation (x
-    written 4 dim + weight 8 by the sampler; f read 4 by the reduction, which
-    regenerates y from Philox instead of reading it) over their CUDA-event
-    times, against the measured copy bandwidth."""
+    Integrator.__call__ -- sampling + map kernel (vg_sample_keep), the
+    integrand's own torch kernels, reduction + training histogram kernel
+    (vg_reduce_kept), adapt.  Evaluations/s through the API, and the HBM
+    roofline of the sampling and reduction kernels: algorithmic bytes per
+    evaluation (x (4 dim), the Jacobian (4) and the training bins (2 dim)
+    written by the sampler; f, the Jacobian and the bins read by the
+    reduction) over their CUDA-event times, against the measured copy
+    bandwidth."""
     import math
     import numpy as np
     import torch
@@ -192,20 +195,22 @@ def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
     integ._allocate(it)
     n = int(integ._read_stats().neval)
     x = torch.empty((ncap, dim), dtype=torch.float32, device=dev)
-    w = torch.empty(ncap, dtype=torch.float64, device=dev)
+    keep = integ._keep_buffer(it, ncap)
     cur = torch.cuda.current_stream(dev)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
 
-    def sample():
-        N.check(L.vg_sample(ctypes.byref(it), 7, None, N.ptr(x), None, N.ptr(w), None, ncap, stream))
+    def sample():   # x, and each sample's Jacobian and training bins kept for the reduction
+        N.check(L.vg_sample_keep(ctypes.byref(it), 7, None, N.ptr(x), None, None, None, ncap, N.ptr(keep),
+                                 keep.numel(), stream))
 
     sample()
     f = gauss(x[:n])
     fb = torch.zeros(ncap, dtype=torch.float32, device=dev)
     fb[:n] = f
 
-    def reduce():
-        N.check(L.vg_reduce(ctypes.byref(it), 7, None, N.ptr(fb), N.VG_F32, stream))
+    def reduce():   # reads f, the kept Jacobians and bins
+        N.check(L.vg_reduce_kept(ctypes.byref(it), 7, None, N.ptr(fb), N.VG_F32, N.ptr(keep), keep.numel(),
+                                 stream))
 
     reduce()
     torch.cuda.synchronize()
@@ -230,8 +235,15 @@ def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
     except (OSError, ValueError):
         pass
     hbm = float(peaks.get('hbm_gbs', 6800.0))
-    b_s, b_r = 4 * dim + 8, 4
+    # algorithmic bytes per evaluation: the sampler writes x (4 dim), the
+    # Jacobian (4) and the training bins (2 dim); the reduction reads f (4),
+    # the Jacobian and the bins
+    b_s, b_r = 6 * dim + 4, 4 + 4 + 2 * dim
+    ex1 = math.erf(math.sqrt(100.0) * 0.5)   # (100/pi)^2 exp(-100 sum (x-1/2)^2) over [0,1]^4
+    exact = ex1 ** 4
     return {
+        'fp32_vs_fp64_oracle': {'oracle': 'exact value erf(5)^4 in FP64', 'exact': exact,
+                                'rel_dev': r.mean / exact - 1.0, 'pull': (r.mean - exact) / r.sdev},
         'workload': 'drop-in path: torch lbatch integrand (dim-4 Gaussian, torch ops) through '
                     'Integrator.__call__, neval %.0e/itn, FP32 sampling, FP64 sums' % neval,
         'value': r.sum_neval / api_s, 'unit': 'evals/s', 'neval_per_iteration': n,
@@ -242,14 +254,14 @@ def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
             'bound': 'hbm', 'unit': 'GB/s', 'peak': hbm,
             'peak_source': 'MEASURED_PEAKS.json hbm_gbs' if 'hbm_gbs' in peaks else 'fallback',
             'traffic_source': 'dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu, '
-                              'bench.py --device-loop-only --case dropin, 9.33e6 evaluations)',
+                              'bench.py --device-loop-only --case dropin)',
             'sample_kernel': {'bytes_per_eval': b_s, 'achieved': b_s * n / t_s / 1e9,
-                              'frac': b_s * n / t_s / 1e9 / hbm, 'traffic': 181.6e6},
+                              'frac': b_s * n / t_s / 1e9 / hbm, 'traffic': None,
+                              'writes': 'x (FP32, 4 dim B), Jacobian (4 B), training bins (2 dim B)'},
             'reduce_kernel': {'bytes_per_eval': b_r, 'achieved': b_r * n / t_r / 1e9,
-                              'frac': b_r * n / t_r / 1e9 / hbm, 'traffic': 54.0e6,
-                              'note': 'regenerates each sample (Philox, map) and forms the two-pass '
-                                      'hypercube sums and the training histogram: bound by that '
-                                      'work, not by its 4 bytes per evaluation'}},
+                              'frac': b_r * n / t_r / 1e9 / hbm, 'traffic': None,
+                              'reads': 'f (4 B), Jacobian (4 B), training bins (2 dim B); forms the '
+                                       'two-pass hypercube sums and the training histogram'}},
     }
 
 
@@ -287,8 +299,14 @@ def batched_line(dev, reps=2):
         'setup_seconds': t_setup, 'integrals': len(fs),
         'pull_rms': float(np.sqrt(np.mean(pulls ** 2))), 'pull_max_abs': float(np.max(np.abs(pulls))),
         'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
+        'fp32_vs_fp64_oracle': {
+            'oracle': 'closed-form Lorentzian integrals in FP64 (LorentzianProduct.exact)',
+            'max_rel_dev': float(np.max(np.abs(res[:, 0] / exact - 1))),
+            'median_rel_dev': float(np.median(np.abs(res[:, 0] / exact - 1))),
+            'pull_rms': float(np.sqrt(np.mean(pulls ** 2)))},
         # Lorentz factor per axis: subtract, FMA, reciprocal, multiply
-        'roofline': issue_roofline(dims, [n * 16 for n in nevals], secs, lambda d: 4 * d, 2070.0),
+        'nominal_evals_per_launch': B.nominal_evaluations(),
+        'roofline': issue_roofline(dims, B.iterations()[:, :, 2].sum(axis=1), secs, lambda d: 4 * d, 2070.0),
     }
 
 
@@ -351,9 +369,21 @@ def lattice_line(dev, reps=2):
         'rel_err_median': float(np.median(res[:, 1] / np.abs(res[:, 0]))),
         'oracle': 'transfer matrix, 400-node Gauss-Legendre, FP64 (LatticeAction.exact)',
         # action per axis: difference, square, x^2, x^4 and the FMAs (6), plus one exp
-        'roofline': issue_roofline([16] * 64, [10 ** 7 * 16] * 64, secs, lambda d: 6 * d + 2, 2070.0),
+        'nominal_evals_per_launch': B.nominal_evaluations(),
+        'roofline': issue_roofline([16] * 64, B.iterations()[:, :, 2].sum(axis=1), secs, lambda d: 6 * d + 2,
+                                   2070.0),
         'fp32_vs_fp64_oracle_max_rel_dev': float(np.max(np.abs(res[:, 0] / exact - 1))),
     }
+
+
+def _jsonable(o):
+    """JSON encoder fallback for numpy scalars and arrays."""
+    import numpy as np
+    if isinstance(o, np.generic):
+        return o.item()
+    if isinstance(o, np.ndarray):
+        return o.tolist()
+    raise TypeError(type(o).__name__)
 
 
 def max_over_ranks(value, world, device=None):
@@ -372,6 +402,37 @@ def replica_seed(base, rank):
     """Seed of a replica: replicas are independent vegas+ runs (own Philox
     key, stream = rank); nothing is exchanged on the data path."""
     return (int(base) + 7919 * int(rank)) & ((1 << 63) - 1)
+
+
+def ridge_fp64_line(dev, nitn=20, warm=5):
+    """The ridge workload with sampling, map and evaluation in FP64 (all
+    1000 Gaussian terms per evaluation, as the reference computes them):
+    evaluations/s of the device loop (vg_iterate, CUDA events), the
+    same-precision companion of the FP64 CPU baseline."""
+    import torch
+    import vegas_gb300 as vg
+    from vegas_gb300 import _native as N
+    L = N.load()
+    f = vg.Ridge(M=RIDGE_M, s=RIDGE_S)
+    I = vg.Integrator(DIM * [[0, 1]], neval=NEVAL, precision='fp64', seed=64, device=dev)
+    it, ncap = I._struct()
+    I._put_sum_sigf()
+    params = N.dbl_array(f.params(DIM))
+    stream = N.stream_ptr(dev)
+    for k in range(warm):
+        N.check(L.vg_iterate(ctypes.byref(it), k + 1, f.kind, params, 2, stream))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(nitn):
+        N.check(L.vg_iterate(ctypes.byref(it), warm + k + 1, f.kind, params, 2, stream))
+    e1.record()
+    torch.cuda.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3 / nitn
+    n = int(I._read_stats().neval)
+    return {'workload': 'vegas+ ridge as the headline line, sampling / map / evaluation in FP64 (1000 '
+                        'terms per evaluation)', 'value': n / secs, 'unit': 'evals/s',
+            'seconds_per_iteration': secs, 'iterations': nitn, 'neval_per_iteration': n}
 
 
 def config1_line(dev, nitn=20):
@@ -523,6 +584,10 @@ def gpu_arm(args):
     executed = int(cnt.item())
     achieved = executed / kern_s / 1e9
     peak = measure_ex2_peak(L, dev)
+    model = ridge_issue_model(executed / neval_step)
+    clk_max = float(clk.get('sm_max_mhz') or 2070.0)
+    issue_peak = 152 * 128 * clk_max * 1e6
+    model_rate = model['total'] * neval_step / kern_s
     # -------- e2e through the public API: one call of K iterations (each
     # iteration's record read back to pinned host memory), and K calls of one
     # iteration each
@@ -551,17 +616,22 @@ def gpu_arm(args):
         t0 = time.perf_counter()
         r3 = integ3(f, nitn=5000, rtol=1e-4)
         torch.cuda.synchronize()
+        pull3 = (r3.mean - exact) / r3.sdev
         tta = {'ridge_plain': {
             'seconds': time.perf_counter() - t0, 'iterations': r3.nitn,
             'result': str(r3), 'rel_err': r3.sdev / abs(r3.mean),
-            'exact': exact, 'pull': (r3.mean - exact) / r3.sdev,
+            'exact': exact, 'pull': pull3,
+            'reached': bool(r3.sdev / abs(r3.mean) <= 1e-4 and abs(pull3) <= 3.0),
             'chi2_dof': (r3.chi2 / r3.dof if r3.dof > 0 else 0.0)}}
         if rank == 0:
             tta['mixture_flow_vs_plain'] = tta_flow_vs_plain(dev)
-    batched = lattice = small = dropin = None
+    batched = lattice = small = dropin = ridge64 = refruns = None
     if rank == 0:
         small = config1_line(dev)
         dropin = dropin_line(dev)
+        ridge64 = ridge_fp64_line(dev)
+        if not args.no_reference_runs:
+            refruns = reference_runs(dev)
     if not args.no_batch and rank == 0:
         batched = batched_line(dev)
         lattice = lattice_line(dev)
@@ -587,33 +657,38 @@ def gpu_arm(args):
                                      % args.steps}},
         # per timed step: allocation, fused tile kernel, finalize, adapt
         'gpu_launches': 4 * args.steps,
-        'roofline': {'bound': 'sfu', 'achieved': ex2_per_launch / kern_s / 1e9, 'peak': peak,
-                     'unit': 'Gex2/s', 'frac': ex2_per_launch / kern_s / 1e9 / peak,
+        'roofline': {'bound': 'issue (model)', 'achieved': model_rate / 1e12, 'peak': issue_peak / 1e12,
+                     'unit': 'T thread-instr/s', 'frac': model_rate / issue_peak,
                      'traffic': 1.70e6,
                      'traffic_source': 'dram__bytes_read.sum + dram__bytes_write.sum of one fused '
                                        'tile_kernel launch (ncu, bench.py --device-loop-only)',
                      'kernel': 'ridge iteration: fused tile_kernel (evaluate + reduce) + finalize '
-                               '(CUDA events)',
-                     'algorithmic': 'the integrand\'s M=1000 exponentials per evaluation: %d ex2 '
-                                    'per launch' % ex2_per_launch,
-                     # the kernel evaluates only the terms that can be nonzero in FP32 (the
-                     # others are exactly zero, so f is identical): above 1 against the
-                     # algorithmic count, and this fraction of the peak for what it executes
-                     'executed': executed, 'executed_frac': achieved / peak,
-                     'note': 'frac above 1: the kernel skips the Gaussian terms that are exactly '
-                             'zero in FP32 (identical results); executed_frac is the MUFU '
-                             'utilisation of the terms it does evaluate',
-                     'peak_source': 'MUFU ex2 probe kernel on this GPU (vg_probe_mufu_ex2)'},
+                               '(CUDA events on the launching stream, median over the timed steps)',
+                     'algorithmic': 'thread instructions per evaluation from op counts (ridge_issue_model) '
+                                    'x %d evaluations per launch' % neval_step,
+                     'model_per_eval': model,
+                     'peak_source': '152 SMs x 4 schedulers x 32 lanes x %.0f MHz (maximum SM clock)'
+                                    % clk_max,
+                     'sfu': {'executed_ex2_per_launch': executed,
+                             'achieved': achieved, 'peak': peak, 'unit': 'Gex2/s',
+                             'frac_executed': achieved / peak,
+                             'reference_terms_equivalent': ex2_per_launch / kern_s / 1e9,
+                             'note': 'the reference evaluates all M=1000 terms (%d ex2 per launch); the '
+                                     'kernel evaluates only those that can be nonzero in FP32 (identical '
+                                     'f), so the reference-terms rate is not a utilisation' % ex2_per_launch,
+                             'peak_source': 'MUFU ex2 probe kernel on this GPU (vg_probe_mufu_ex2)'}},
         'clocks': clk,
         'time_to_1e-4': tta,
         'batched': batched,
         'lattice_scan': lattice,
         'small_fp64': small,
         'dropin': dropin,
+        'ridge_fp64': ridge64,
+        'reference_runs': refruns,
     }
     if not args.no_cpu_baseline and world == 1:
         out['cpu_baseline'] = cpu_baseline(iters=2)
-    print(json.dumps(out))
+    print(json.dumps(out, default=_jsonable))
 
 
 MIX_DIM, MIX_NEVAL = 8, 1 << 20
@@ -630,11 +705,14 @@ def mixture_integrand():
     return vg.GaussianMixture(rng.uniform(0.15, 0.85, (4, MIX_DIM)), sigma=0.03)
 
 
-def _tta_run(step, warm_itn, cap_s, target=1e-4):
+def _tta_run(step, warm_itn, cap_s, target=1e-4, exact=None):
     """Wall-clock time until the running result (iterations after the first
     warm_itn) reaches target relative error.  step() runs one iteration and
     returns (mean, var, neval).  Past cap_s the time is extrapolated with the
-    1/n error law from the accumulated precision."""
+    1/n error law from the accumulated precision.  With the exact value
+    given, the target counts as reached only when the result also lies
+    within 3 standard deviations of it (a biased result reaches nothing):
+    "reached" says so, and "pull" is (mean - exact) / sdev."""
     import torch
     from vegas_gb300 import RAvg, gvar
     torch.cuda.synchronize()
@@ -645,9 +723,11 @@ def _tta_run(step, warm_itn, cap_s, target=1e-4):
     t_warm = time.perf_counter() - t0
     r = RAvg()
     neval = 0
+    means = []
     while True:
         m, v, ne = step()
         r.add(gvar(m, max(v, 0.0) ** 0.5))
+        means.append(m)
         neval += ne
         rel = r.sdev / abs(r.mean) if r.mean != 0 else float('inf')
         t = time.perf_counter() - t0
@@ -657,11 +737,30 @@ def _tta_run(step, warm_itn, cap_s, target=1e-4):
     t = time.perf_counter() - t0
     t_acc = t - t_warm
     est = t if rel <= target else t_warm + t_acc * (rel / target) ** 2
-    return {'seconds': est, 'measured_seconds': t, 'extrapolated': rel > target,
-            'warmup_seconds': t_warm, 'warmup_iterations': warm_itn, 'iterations': r.nitn,
-            'evaluations': neval, 'result': str(r), 'mean': r.mean, 'sdev': r.sdev, 'rel_err': rel,
-            'var_per_eval': (r.sdev ** 2) * neval,
-            'chi2_dof': (r.chi2 / r.dof if r.dof > 0 else 0.0)}
+    out = {'seconds': est, 'measured_seconds': t, 'extrapolated': rel > target,
+           'warmup_seconds': t_warm, 'warmup_iterations': warm_itn, 'iterations': r.nitn,
+           'evaluations': neval, 'result': str(r), 'mean': r.mean, 'sdev': r.sdev, 'rel_err': rel,
+           'var_per_eval': (r.sdev ** 2) * neval,
+           'chi2_dof': (r.chi2 / r.dof if r.dof > 0 else 0.0)}
+    if exact is not None:
+        out['exact'] = exact
+        out['pull'] = (r.mean - exact) / r.sdev if r.sdev > 0 else None
+        out['reached'] = bool(rel <= target and out['pull'] is not None and abs(out['pull']) <= 3.0)
+    if len(means) > 2:
+        # the plain (unweighted) mean of the iterations: unbiased where the
+        # inverse-variance weighting is not, with the error from the spread
+        # of the iterations; its time to the target by the 1/n law
+        import numpy as np
+        mu = float(np.mean(means))
+        su = float(np.std(means, ddof=1) / len(means) ** 0.5)
+        relu = su / abs(mu) if mu != 0 else float('inf')
+        u = {'mean': mu, 'sdev': su, 'rel_err': relu,
+             'seconds': t if relu <= target else t_warm + t_acc * (relu / target) ** 2,
+             'extrapolated': bool(relu > target)}
+        if exact is not None and su > 0:
+            u['pull'] = (mu - exact) / su
+        out['unweighted_average'] = u
+    return out
 
 
 def tta_flow_vs_plain(dev, cap_s=30.0):
@@ -683,7 +782,7 @@ def tta_flow_vs_plain(dev, cap_s=30.0):
         return v.mean, v.sdev ** 2, plain.last_neval
 
     out = {'workload': MIX_WORKLOAD, 'exact': exact}
-    out['plain'] = _tta_run(pstep, 10, cap_s)
+    out['plain'] = _tta_run(pstep, 10, cap_s, exact=exact)
     fi = FlowIntegrator(lim, neval=MIX_NEVAL, seed=777, device=dev, plain_itn=10, kl_itn=10,
                         train_itn=40, grace=10, patience=3, train_steps=4, train_batch=1 << 15,
                         lr=1e-3)
@@ -693,13 +792,157 @@ def tta_flow_vs_plain(dev, cap_s=30.0):
         h = fi.history[-1]
         return h['mean'], h['sdev'] ** 2, h['neval']
 
-    out['flow'] = _tta_run(fstep, 50, cap_s)
+    out['flow'] = _tta_run(fstep, 50, cap_s, exact=exact)
     out['flow']['flow_active_at_end'] = bool(fi.flow_on)
-    for k in ('plain', 'flow'):
-        r = out[k]
-        r['pull'] = (r['mean'] - exact) / r['sdev'] if r['sdev'] > 0 else None
+    # time-to-accuracy counts only a run that reached 1e-4 within 3 sigma
+    # of the exact value; plain vegas+ on this multimodal integrand
+    # converges to a biased value (see reference_runs.config4_mixture)
     out['speedup'] = out['plain']['seconds'] / out['flow']['seconds']
+    out['speedup_note'] = ('ratio of times to 1e-4 relative error; plain reached=%s, flow reached=%s'
+                           % (out['plain']['reached'], out['flow']['reached']))
     return out
+
+
+# ------------------------------------------------- normal-mode comparisons
+def _combined(a_mean, a_sdev, b_mean, b_sdev):
+    d = (a_sdev ** 2 + b_sdev ** 2) ** 0.5
+    return (a_mean - b_mean) / d if d > 0 else None
+
+
+def _oracle_run(st, kind, params, nwarm, nitn, seed, nthreads):
+    """The oracle (the reference algorithm in FP64 on the host) for nwarm
+    adapting iterations then nitn more: per-iteration (mean, var), the
+    weighted average (RAvg.add, pyx:2392-2410) and the wall time."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    t0 = time.perf_counter()
+    ms, vs = [], []
+    neval = 0
+    for k in range(nwarm + nitn):
+        out = st.iterate(kind, params, seed=seed, stream=0, itn=k + 1, nthreads=nthreads)
+        if k >= nwarm:
+            ms.append(out['mean'])
+            vs.append(out['var'])
+            neval += out['neval']
+    dt = time.perf_counter() - t0
+    mean, sdev, chi2, dof, Q = O.weighted_average(ms, vs)
+    ms = np.asarray(ms)
+    return {'mean': mean, 'sdev': sdev, 'chi2_dof': chi2 / dof if dof else 0.0, 'Q': Q,
+            'unweighted_mean': float(ms.mean()),
+            'unweighted_sdev': float(ms.std(ddof=1) / len(ms) ** 0.5) if len(ms) > 1 else 0.0,
+            'seconds': dt, 'evaluations': neval, 'iterations': nitn, 'warmup_iterations': nwarm,
+            'threads': nthreads}
+
+
+def _gpu_run(I, f, nwarm, nitn):
+    """The same on the GPU through the public API: per-iteration results
+    after nwarm adapting iterations, weighted and unweighted averages."""
+    import numpy as np
+    import torch
+    if nwarm:
+        I(f, nitn=nwarm)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = I(f, nitn=nitn)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ms = np.array([x.mean for x in r.itn_results])
+    return {'mean': r.mean, 'sdev': r.sdev, 'chi2_dof': r.chi2 / r.dof if r.dof else 0.0, 'Q': r.Q,
+            'unweighted_mean': float(ms.mean()),
+            'unweighted_sdev': float(ms.std(ddof=1) / len(ms) ** 0.5) if len(ms) > 1 else 0.0,
+            'seconds': dt, 'evaluations': int(r.sum_neval), 'iterations': nitn, 'warmup_iterations': nwarm,
+            'precision': I.precision}
+
+
+def _pulls(runs, exact):
+    """Each run's pull against the exact value (weighted and unweighted
+    averages) and the combined-sigma pull of every GPU run against the
+    oracle run."""
+    for k, r in runs.items():
+        if not isinstance(r, dict) or 'mean' not in r:
+            continue
+        r['pull_vs_exact'] = (r['mean'] - exact) / r['sdev'] if r['sdev'] > 0 else None
+        r['rel_dev_vs_exact'] = r['mean'] / exact - 1.0
+        if r.get('unweighted_sdev'):
+            r['unweighted_pull_vs_exact'] = (r['unweighted_mean'] - exact) / r['unweighted_sdev']
+    o = runs['oracle']
+    for k, r in runs.items():
+        if k != 'oracle' and isinstance(r, dict) and 'mean' in r:
+            r['combined_pull_vs_oracle'] = _combined(r['mean'], r['sdev'], o['mean'], o['sdev'])
+    runs['exact'] = exact
+    return runs
+
+
+def reference_runs(dev):
+    """Normal-mode results on the GPU against oracle runs of the same
+    workload (independent draws: the oracle is the reference algorithm in
+    FP64 on the host cores), combined-sigma pulls, and each against the
+    exact value.  Config 1: dim-4 Gaussian, 1e4/itn, 10+10, FP64.  Config 2:
+    the ridge, 1e6/itn, 10+10, FP32 on the GPU (and FP64).  Config 4: plain
+    vegas+ on the 8-d Gaussian mixture, 2^20/itn, 10 + 150 iterations in
+    FP32 and FP64 on the GPU and in the oracle -- the weighted average
+    (RAvg) and the plain mean of the iterations, to attribute the bias of
+    plain vegas+ on this multimodal integrand."""
+    import vegas_gb300 as vg
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    cores = os.cpu_count() or 1
+    out = {}
+    # config 1
+    f = vg.Gaussian(a=100.0, c=0.5, dim=4)
+    runs = {'gpu_fp64': _gpu_run(vg.Integrator(4 * [[0, 1]], neval=10000, precision='fp64', seed=101,
+                                               device=dev), f, 10, 10),
+            'gpu_fp32': _gpu_run(vg.Integrator(4 * [[0, 1]], neval=10000, seed=102, device=dev), f, 10, 10),
+            'oracle': _oracle_run(O.State(4 * [[0, 1]], 10000), O.F_GAUSS, f.params(4), 10, 10, 103, 1)}
+    out['config1_gauss4'] = _pulls(runs, f.exact(4))
+    # config 2
+    f = vg.Ridge(M=RIDGE_M, s=RIDGE_S)
+    runs = {'gpu_fp32': _gpu_run(vg.Integrator(DIM * [[0, 1]], neval=NEVAL, seed=201, device=dev), f, 10, 10),
+            'gpu_fp64': _gpu_run(vg.Integrator(DIM * [[0, 1]], neval=NEVAL, precision='fp64', seed=202,
+                                               device=dev), f, 10, 10),
+            'oracle': _oracle_run(O.State(DIM * [[0, 1]], NEVAL), O.F_RIDGE, [RIDGE_M, RIDGE_S], 10, 10, 203,
+                                  cores)}
+    out['config2_ridge'] = _pulls(runs, f.exact(DIM))
+    # config 4, plain vegas+
+    f = mixture_integrand()
+    lim = MIX_DIM * [[0.0, 1.0]]
+    n4 = 150
+    runs = {'gpu_fp32': _gpu_run(vg.Integrator(lim, neval=MIX_NEVAL, seed=401, device=dev), f, 10, n4),
+            'gpu_fp64': _gpu_run(vg.Integrator(lim, neval=MIX_NEVAL, precision='fp64', seed=402, device=dev),
+                                 f, 10, n4),
+            'oracle': _oracle_run(O.State(lim, MIX_NEVAL), O.F_MIXTURE, f.params(MIX_DIM), 10, n4, 403, cores)}
+    out['config4_mixture_plain'] = _pulls(runs, f.exact(MIX_DIM))
+    out['note'] = ('gpu_* and oracle are independent runs (own Philox streams); combined_pull_vs_oracle = '
+                   '(I_gpu - I_oracle) / sqrt(sdev_gpu^2 + sdev_oracle^2); the oracle is the reference '
+                   'algorithm restated in C, FP64, on %d host threads' % cores)
+    return out
+
+
+def ridge_issue_model(terms_per_eval, dim=DIM):
+    """Issue-rate model of the fused FP32 ridge iteration: thread
+    instructions per evaluation from the algorithm's op counts.
+
+      Philox4x32-10 for the sample's uniforms: 80 per 4 uniforms (10 rounds
+        of 2 wide multiplies, 2 three-input XORs, 2 key adds; 4 conversions)
+      map, per axis: stratum coordinate, bin index, table load, node + inc
+        x fraction, Jacobian factor, training bin -- 12
+      ridge: mean and spread of x (3 dim + 1), exponent offset and centre
+        (2), window of the Gaussian terms that can be nonzero in FP32 (15),
+        final scale (3); per evaluated term: subtract, FMA, ex2, add and a
+        quarter of a vector shared load -- 4.25
+      per-sample reduction: weight and fdv2 (4), training histogram (3 per
+        axis), float-float two-pass hypercube sums (30)
+
+    The terms are the ones the kernel evaluates (those that can be nonzero
+    in FP32; the others are exactly zero), counted per iteration.  Peak: 152
+    SMs x 4 schedulers x 32 lanes per cycle at the maximum SM clock."""
+    philox = 80 * ((dim + 3) // 4)
+    mapping = 12 * dim
+    integrand = (3 * dim + 1) + 2 + 15 + 3 + 4.25 * terms_per_eval
+    reduction = 4 + 3 * dim + 30
+    return {'philox': philox, 'map': mapping, 'integrand': integrand, 'reduction': reduction,
+            'total': philox + mapping + integrand + reduction, 'terms_per_eval': terms_per_eval}
 
 
 def measure_ex2_peak(L, dev):
@@ -721,10 +964,56 @@ def measure_ex2_peak(L, dev):
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_baseline(iters=2, kind='port'):
-    """Oracle restatement of the reference on all host cores, same workload."""
+def _cpu_tta(st, kind, params, nwarm, seed, nthreads, cap_s, target=1e-4, exact=None):
+    """The oracle's time to `target` relative error on one workload: nwarm
+    adapting iterations, then iterations until the weighted average reaches
+    the target or cap_s passes (then extrapolated with the 1/n law)."""
     sys.path.insert(0, os.path.join(ROOT, 'oracle'))
     import oracle as O
+    t0 = time.perf_counter()
+    k = 0
+    for _ in range(nwarm):
+        k += 1
+        st.iterate(kind, params, seed=seed, itn=k, nthreads=nthreads)
+    t_warm = time.perf_counter() - t0
+    ms, vs = [], []
+    ne = 0
+    rel = float('inf')
+    while True:
+        k += 1
+        out = st.iterate(kind, params, seed=seed, itn=k, nthreads=nthreads)
+        ms.append(out['mean'])
+        vs.append(out['var'])
+        ne += out['neval']
+        mean, sdev, chi2, dof, Q = O.weighted_average(ms, vs)
+        rel = sdev / abs(mean) if mean != 0 else float('inf')
+        t = time.perf_counter() - t0
+        if rel <= target or t > cap_s:
+            break
+    t_acc = t - t_warm
+    r = {'seconds': t if rel <= target else t_warm + t_acc * (rel / target) ** 2,
+         'measured_seconds': t, 'extrapolated': rel > target, 'iterations': len(ms),
+         'warmup_iterations': nwarm, 'evaluations': ne, 'rel_err': rel, 'mean': mean, 'sdev': sdev,
+         'evals_per_s': ne / t_acc if t_acc > 0 else None, 'threads': nthreads}
+    if exact is not None:
+        r['pull'] = (mean - exact) / sdev if sdev > 0 else None
+    return r
+
+
+def cpu_baseline(iters=2, kind='port'):
+    """The reference algorithm on the host cores (the C restatement in
+    oracle/, FP64): the ridge workload at all cores (the reported value)
+    and at one core; the oracle's time to 1e-4 relative error on the dim-4
+    Gaussian (1e4/itn, one core) and the ridge (all cores); and per-
+    evaluation rates on bounded subsets of the batched Lorentzian workload
+    (32 of its 4096 integrals, 2 iterations each), the 8-d mixture (2
+    iterations of 2^20) and the lattice scan (1 of its 64 couplings, 2
+    iterations of 1e7), from which the full workloads' CPU times are
+    extrapolated."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+    import oracle as O
+    import vegas_gb300 as vg
     cores = os.cpu_count() or 1
     st = O.State(DIM * [[0, 1]], NEVAL)
     t0 = time.perf_counter()
@@ -733,18 +1022,66 @@ def cpu_baseline(iters=2, kind='port'):
         out = st.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=5, itn=k + 1, nthreads=cores)
         ne += out['neval']
     dt = time.perf_counter() - t0
+    # one core, one iteration of the same workload
+    st1 = O.State(DIM * [[0, 1]], NEVAL)
+    t1 = time.perf_counter()
+    ne1 = st1.iterate(O.F_RIDGE, [RIDGE_M, RIDGE_S], seed=6, itn=1, nthreads=1)['neval']
+    t1 = time.perf_counter() - t1
     # the CPU-sized workload (dim 4 Gaussian, neval 1e4, FP64): seconds per
     # iteration of the reference algorithm on one core
-    st1 = O.State(4 * [[0, 1]], 10000)
-    p1 = [100.0, 0.5, (100.0 / 3.141592653589793) ** 2]
-    t1 = time.perf_counter()
+    f1 = vg.Gaussian(a=100.0, c=0.5, dim=4)
+    stg = O.State(4 * [[0, 1]], 10000)
+    tg = time.perf_counter()
     for k in range(20):
-        st1.iterate(O.F_GAUSS, p1, seed=5, itn=k + 1, nthreads=1)
-    t1 = (time.perf_counter() - t1) / 20
+        stg.iterate(O.F_GAUSS, f1.params(4), seed=5, itn=k + 1, nthreads=1)
+    tg = (time.perf_counter() - tg) / 20
+    tta = {'config1_gauss4_1core': _cpu_tta(O.State(4 * [[0, 1]], 10000), O.F_GAUSS, f1.params(4), 10, 7, 1,
+                                            10.0, exact=f1.exact(4)),
+           'config2_ridge_all_cores': _cpu_tta(O.State(DIM * [[0, 1]], NEVAL), O.F_RIDGE, [RIDGE_M, RIDGE_S], 5,
+                                               8, cores, 15.0, exact=vg.Ridge(M=RIDGE_M, s=RIDGE_S).exact(DIM))}
+    # bounded subsets of the larger workloads
+    subsets = {}
+    fs, nevals, dims = batch_workload()
+    rng = np.random.default_rng(1)
+    idx = rng.choice(len(fs), 32, replace=False)
+    t3, n3 = time.perf_counter(), 0
+    for i in idx:
+        s3 = O.State(int(dims[i]) * [[0, 1]], int(nevals[i]))
+        for k in range(2):
+            n3 += s3.iterate(O.F_LORENTZ, fs[i].params(int(dims[i])), seed=9, itn=k + 1, nthreads=cores)['neval']
+    t3 = time.perf_counter() - t3
+    # the full launch's evaluations: nominal neval x 16 iterations, scaled by
+    # the subset's actual / nominal ratio (the allocation rounds down)
+    total3 = float(np.sum(nevals)) * 16 * n3 / (2.0 * float(np.sum(nevals[idx])))
+    subsets['config3_batched_lorentz'] = {
+        'sample': '32 of the 4096 integrals, 2 iterations each', 'evaluations': n3, 'seconds': t3,
+        'evals_per_s': n3 / t3, 'extrapolated_seconds_full_launch': total3 / (n3 / t3),
+        'full_launch_evaluations': total3}
+    fm = mixture_integrand()
+    s4 = O.State(MIX_DIM * [[0.0, 1.0]], MIX_NEVAL)
+    t4, n4 = time.perf_counter(), 0
+    for k in range(2):
+        n4 += s4.iterate(O.F_MIXTURE, fm.params(MIX_DIM), seed=9, itn=k + 1, nthreads=cores)['neval']
+    t4 = time.perf_counter() - t4
+    subsets['config4_mixture_plain'] = {'sample': '2 iterations of 2^20', 'evaluations': n4, 'seconds': t4,
+                                        'evals_per_s': n4 / t4}
+    s5 = O.State(16 * [[-5.0, 5.0]], 10 ** 7)
+    t5, n5 = time.perf_counter(), 0
+    for k in range(2):
+        n5 += s5.iterate(O.F_LATTICE, [0.5, 0.1], seed=9, itn=k + 1, nthreads=cores)['neval']
+    t5 = time.perf_counter() - t5
+    total5 = 64.0 * 16 * n5 / 2.0   # per-lambda actual evaluations of this sample
+    subsets['config5_lattice_scan'] = {
+        'sample': '1 of the 64 couplings (lambda 0.1), 2 iterations of 1e7', 'evaluations': n5, 'seconds': t5,
+        'evals_per_s': n5 / t5, 'extrapolated_seconds_full_launch': total5 / (n5 / t5),
+        'full_launch_evaluations': total5}
     return {'value': ne / dt, 'unit': 'evals/s', 'cores': cores, 'kind': kind,
-            'sample': '%d full iterations of the workload (neval=1e6 each), FP64, %d threads'
+            'sample': '%d full iterations of the ridge workload (neval=1e6 each), FP64, %d threads'
                       % (iters, cores),
-            'small_fp64_seconds_per_iteration_1core': t1}
+            'one_core': {'value': ne1 / t1, 'unit': 'evals/s', 'sample': '1 iteration of 1e6, 1 thread'},
+            'small_fp64_seconds_per_iteration_1core': tg,
+            'time_to_1e-4': tta, 'subsets': subsets,
+            'host': {'nproc': cores, 'machine': os.uname().machine}}
 
 
 def reference_arm(args):

@@ -189,6 +189,24 @@ int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u, const void
               void *stream);
 
 /*
+ * The same pair with the samples kept between them, so that the reduction
+ * streams what the sampler stored instead of regenerating every sample
+ * (Philox draws, hypercube walk, map): vg_sample_keep writes what vg_sample
+ * writes and, into `keep` (device, vg_keep_bytes(it, n_cap) bytes), each
+ * sample's Jacobian (FP32 / FP64 by precision) and its training bins (16-bit
+ * per axis); vg_reduce_kept then reads f, the Jacobians and the bins and
+ * gives the same results as vg_reduce, bit for bit (itn and u as given to
+ * the sampler).  Together they replace
+ * the batch loop of Integrator.__call__ for a user integrand (pyx:2096-2197).
+ */
+size_t vg_keep_bytes(const vg_integrator *it, int64_t n_cap);
+int vg_sample_keep(const vg_integrator *it, uint32_t itn, const double *u, void *x, void *y,
+                   double *wgt, int64_t *hcube, int64_t n_cap, void *keep, size_t keep_bytes,
+                   void *stream);
+int vg_reduce_kept(const vg_integrator *it, uint32_t itn, const double *u, const void *f, int f_dtype,
+                   const void *keep, size_t keep_bytes, void *stream);
+
+/*
  * Fused iteration for a built-in integrand: sampling, map, evaluation,
  * reduction and training histogram in one persistent kernel (the whole
  * body of Integrator.__call__'s batch loop, pyx:2096-2197).  params are host
@@ -353,8 +371,8 @@ int vg_weight_points(int64_t n, const float *f, const float *jac, const float *l
  * its integrals * G <= grid[b]): a cooperative launch in which G CTAs share
  * each integral's tiles (sync: device uint[njobs] barrier counters).  Each
  * iteration is the same allocation / fused evaluation + reduction / adapt
- * as vg_fused_iteration; out (device double[njobs][nitn][2]) receives every
- * iteration's mean and variance, res (device double[njobs][4]) the weighted
+ * as vg_fused_iteration; out (device double[njobs][nitn][3]) receives every
+ * iteration's mean, variance and number of evaluations, res (device double[njobs][4]) the weighted
  * average over the iterations after the first nwarm (mean, sdev, chi2, dof).
  * stats->sum_sigf of each integral must hold its starting value (nhcube for
  * a fresh one).  cfg[b] = VG_BATCH_CFG_F64 selects the FP64 parity
@@ -403,6 +421,11 @@ int vg_set_eval_split(int policy);
  * training histogram in shared memory (-1 automatic, 0 off, 1 on where it
  * fits). */
 int vg_set_tile_tuning(int s_dim4, int table_smem, int hist_smem);
+
+/* Tuning of the drop-in path's FP32 kernels at dim <= 4: samples per thread
+ * of vg_sample / vg_sample_keep (0 automatic, or 2, 4, 8) and of
+ * vg_reduce_kept (0 automatic, or 2, 4). */
+int vg_set_dropin_tuning(int s_points, int s_reduce);
 
 /* ------------------------------------------------------------- probes */
 /* Throughput probes used for roofline denominators (see bench.py). */

@@ -50,6 +50,8 @@ def test_batch_matches_single_integral_path(variant):
             # Later iterations start from maps adapted on FP32 shared-memory
             # histograms whose atomic-add order differs from run to run.
             tol = 1e-6 if k == 0 else 1e-4
+            if k == 0:   # same allocation (uniform sigf): same evaluation count
+                assert int(out[j, k, 2]) == I.last_neval
             assert abs(out[j, k, 0] - m) <= tol * abs(m), (j, k, out[j, k, 0], m)
             assert abs(out[j, k, 1] - s * s) <= tol * 10 * s * s, (j, k)
 

@@ -278,3 +278,44 @@ def test_constant_integrand_epsilon_guard():
     np.testing.assert_almost_equal(res.mean, 7.0, 7)
     res = I(vg.Constant(0.0), nitn=4)
     assert res.mean == 0.0
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+def test_reduce_kept_matches_reduce(precision):
+    """vg_sample_keep + vg_reduce_kept (the reduction streams the kept
+    Jacobians and training bins) == vg_sample + vg_reduce (the reduction
+    regenerates every sample) on the same allocation and integrand values:
+    mean, variance, sum_sigf and sigf bit for bit (same arithmetic, static
+    tile partials in a fixed order); the training histogram bit for bit in
+    FP64 and at 1e-6 relative in FP32 (FP32 atomic adds in arrival order)."""
+    L = N.load()
+    f = vg.Gaussian(a=30.0, c=0.45, dim=4)
+    A = vg.Integrator(4 * [[0, 1]], neval=200000, precision=precision, seed=21)
+    A(f, nitn=2)                               # a non-uniform map and sigf
+    B = vg.Integrator(4 * [[0, 1]], neval=200000, precision=precision, seed=21)
+    set_state(B, A.map.grid, A.sigf, A.sum_sigf)
+    stream = N.stream_ptr(A.device)
+    res = []
+    for I, kept in ((A, False), (B, True)):
+        it, ncap = I._struct()
+        I._allocate(it)
+        n = int(I._read_stats().neval)
+        keep = I._keep_buffer(it, ncap) if kept else None
+        x, _, _, _ = I._points(it, ncap, 9, None, want_w=False, keep=keep)
+        fx = torch.zeros(ncap, dtype=x.dtype, device=x.device)
+        fx[:n] = f(x[:n])
+        fdt = N.VG_F64 if precision == 'fp64' else N.VG_F32
+        if kept:
+            N.check(L.vg_reduce_kept(ctypes.byref(it), 9, None, N.ptr(fx), fdt, N.ptr(keep), keep.numel(),
+                                     stream))
+        else:
+            N.check(L.vg_reduce(ctypes.byref(it), 9, None, N.ptr(fx), fdt, stream))
+        st = I._read_stats()
+        res.append((st, I.sigf.copy(), I.map.sum_f.cpu().numpy().copy(), I.map.n_f.cpu().numpy().copy(), n))
+    (sa, ga, ha, ca, na), (sb, gb, hb, cb, nb) = res
+    assert na == nb
+    assert sa.mean == sb.mean and sa.var == sb.var and sa.sum_sigf == sb.sum_sigf
+    assert np.array_equal(ga, gb)
+    assert np.array_equal(ca, cb) and 0 < ca.sum() <= na * 4
+    tol = 1e-12 if precision == 'fp64' else 1e-6
+    assert np.max(np.abs(ha - hb)) <= tol * np.max(np.abs(ha))

@@ -124,7 +124,7 @@ def test_batch_fp64_matches_oracle():
             rec = B.read_stats(j)
             v = B.state(j)
             assert rec.status == 0
-            assert rec.neval == o['neval'] == tot_want, (j, itn)
+            assert rec.neval == o['neval'] == tot_want == int(out[j, 0, 2]), (j, itn)
             assert (rec.range_lo, rec.range_hi) == tuple(o['range']) == tuple(rng_want)
             nh = v['neval_h'].cpu().numpy().astype(np.int64)
             assert np.array_equal(nh, nh_want), (j, itn, int(np.sum(nh != nh_want)))

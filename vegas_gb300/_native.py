@@ -146,6 +146,9 @@ SIGNATURES = {
     'vg_allocate': (I32, [P, P]),
     'vg_sample': (I32, [P, U32, P, P, P, P, P, I64, P]),
     'vg_reduce': (I32, [P, U32, P, P, I32, P]),
+    'vg_keep_bytes': (SZ, [P, I64]),
+    'vg_sample_keep': (I32, [P, U32, P, P, P, P, P, I64, P, SZ, P]),
+    'vg_reduce_kept': (I32, [P, U32, P, P, I32, P, SZ, P]),
     'vg_fused_iteration': (I32, [P, U32, P, I32, P, I32, P]),
     'vg_end_iteration': (I32, [P, P]),
     'vg_iterate': (I32, [P, U32, I32, P, I32, P]),
@@ -174,6 +177,7 @@ SIGNATURES = {
     'vg_set_term_counter': (I32, [P]),
     'vg_set_eval_split': (I32, [I32]),
     'vg_set_wait_budget': (I32, [I64]),
+    'vg_set_dropin_tuning': (I32, [I32, I32]),
     'vg_set_tile_tuning': (I32, [I32, I32, I32]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),

@@ -173,7 +173,7 @@ class BatchIntegrator(object):
             p = f.params(int(self.dims[j]))
             self.params[j, :len(p)] = p
             self.nparams[j] = len(p)
-        self.out = torch.zeros((nj, self.nitn, 2), dtype=torch.float64, device=self.device)
+        self.out = torch.zeros((nj, self.nitn, 3), dtype=torch.float64, device=self.device)
         self.res = torch.zeros((nj, 4), dtype=torch.float64, device=self.device)
         self.table = torch.empty(int(L.vg_batch_table_bytes(nj)), dtype=torch.uint8, device=self.device)
         # queue order: grouped by dimension bucket, largest first in each
@@ -267,7 +267,7 @@ class BatchIntegrator(object):
         return self.res.cpu().numpy()
 
     def iterations(self):
-        """Every iteration's (mean, variance) (numpy [njobs, nitn, 2])."""
+        """Every iteration's (mean, variance, evaluations) (numpy [njobs, nitn, 3])."""
         return self.out.cpu().numpy()
 
     def integrator_struct(self, j):
@@ -309,7 +309,14 @@ class BatchIntegrator(object):
         self.state(j)['stats'].copy_(torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8))
 
     def evaluations(self):
-        """Evaluations of the last launch summed over integrals and iterations."""
+        """Evaluations of the last launch summed over integrals and iterations
+        (the allocations' actual counts, read back from the device)."""
+        return int(round(float(self.out[:, :, 2].sum().item())))
+
+    def nominal_evaluations(self):
+        """The requested neval of every integral times nitn (the allocation
+        gives each iteration about this many; rounding down per hypercube
+        usually gives fewer)."""
         return int(sum(self.neval)) * self.nitn
 
     # ------------------------------------------------------------ autotune

@@ -217,7 +217,7 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
             const size_t an = sizeof(double) * (2 * (size_t)max_old + vg::NT);
             need = an > need ? an : need;
         }
-        J.out = out + (size_t)j * 2 * nitn;
+        J.out = out + (size_t)j * 3 * nitn;
         J.res = res + (size_t)j * 4;
         J.sync = sync != nullptr ? sync + j : nullptr;
         smem_max[b] = need > smem_max[b] ? need : smem_max[b];

@@ -21,7 +21,7 @@ using namespace vg;
 struct BatchJob {
     IterArgs a;                  // per-integral arguments (its own workspace)
     vgadapt::AdaptArgs ad;       // adapt: grid -> scratch grid of the workspace
-    double *out;                 // [nitn][2] iteration mean, variance
+    double *out;                 // [nitn][3] iteration mean, variance, evaluations
     double *res;                 // [4] weighted mean, sdev, chi2, dof
     unsigned int *sync;          // group barrier counter (group mode)
     int bucket;                  // dimension bucket: 0 (dim <= 4), 1 (<= 8), 2 (<= 16)
@@ -300,7 +300,7 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
     double sw = 0.0, swm = 0.0;
     int cnt = 0;
     for (int i = nwarm; i < nitn; i++) {
-        const double m = J.out[2 * i], v = J.out[2 * i + 1];
+        const double m = J.out[3 * i], v = J.out[3 * i + 1];
         if (v > 0) {
             sw += 1.0 / v;
             swm += m / v;
@@ -310,7 +310,7 @@ static __device__ __noinline__ void cta_ravg(const BatchJob &J, int nitn, int nw
     const double mean = sw > 0 ? swm / sw : 0.0;
     double chi2 = 0.0;
     for (int i = nwarm; i < nitn; i++) {
-        const double m = J.out[2 * i], v = J.out[2 * i + 1];
+        const double m = J.out[3 * i], v = J.out[3 * i + 1];
         if (v > 0) chi2 += (m - mean) * (m - mean) / v;
     }
     J.res[0] = mean;
@@ -383,8 +383,9 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
                 if constexpr (sizeof(T) == 8) cta_finalize_f64(sa, G, red, &s_flag);
                 else cta_finalize(sa, G, red, &s_flag);
                 if (tid == 0) {
-                    J.out[2 * it] = sa.stats->mean;
-                    J.out[2 * it + 1] = sa.stats->var;
+                    J.out[3 * it] = sa.stats->mean;
+                    J.out[3 * it + 1] = sa.stats->var;
+                    J.out[3 * it + 2] = (double)sa.stats->neval;
                 }
                 if (J.adapt) cta_adapt(J, sa, smem);
             }

@@ -702,6 +702,81 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
+// The kept-sample buffer of vg_sample_keep / vg_reduce_kept: per sample its
+// Jacobian (the precision's float type), then its training bins (16-bit per
+// axis, rows padded to a multiple of 4 axes so that each 4 bins move as one
+// 8-byte word).
+static int keep_bstride(const vg_integrator *it) { return (it->dim + 3) & ~3; }
+
+static size_t keep_jac_bytes(const vg_integrator *it, int64_t ncap)
+{
+    const size_t t = it->precision == VG_F64 ? sizeof(double) : sizeof(float);
+    return (t * (size_t)ncap + 255) & ~(size_t)255;
+}
+
+extern "C" size_t vg_keep_bytes(const vg_integrator *it, int64_t n_cap)
+{
+    if (it == nullptr || it->dim < 1 || it->dim > VG_MAX_DIM) {
+        vg_fail(VG_ERR_VALUE, "vg_keep_bytes: dim outside 1..%d", VG_MAX_DIM);
+        return 0;
+    }
+    if (n_cap <= 0) n_cap = neval_cap(it);
+    return keep_jac_bytes(it, n_cap) + sizeof(unsigned short) * (size_t)keep_bstride(it) * (size_t)n_cap;
+}
+
+static int keep_args(IterArgs &a, const vg_integrator *it, void *keep, size_t keep_bytes)
+{
+    if (keep == nullptr) return vg_fail(VG_ERR_VALUE, "kept-sample buffer missing");
+    if (keep_bytes < vg_keep_bytes(it, a.ncap))
+        return vg_fail(VG_ERR_VALUE, "kept-sample buffer too small: %zu < %zu", keep_bytes,
+                       vg_keep_bytes(it, a.ncap));
+    a.keep_jac = keep;
+    a.keep_bins = (unsigned short *)((char *)keep + keep_jac_bytes(it, a.ncap));
+    a.keep_bstride = keep_bstride(it);
+    return VG_OK;
+}
+
+extern "C" int vg_sample_keep(const vg_integrator *it, uint32_t itn, const double *u, void *x, void *y,
+                              double *wgt, int64_t *hcube, int64_t n_cap, void *keep, size_t keep_bytes,
+                              void *stream)
+{
+    VG_RANGE("vg_sample_keep");
+    vg_clear_error();
+    IterArgs a;
+    int rc = fill_args(a, it, itn, u);
+    if (rc) return rc;
+    if (n_cap < a.ncap) return vg_fail(VG_ERR_VALUE, "output capacity %lld < %lld",
+                                       (long long)n_cap, (long long)a.ncap);
+    if ((rc = keep_args(a, it, keep, keep_bytes))) return rc;
+    a.x_out = x;
+    a.y_out = y;
+    a.wgt_out = wgt;
+    a.hc_out = hcube;
+    a.train = 0;
+    a.train_hc = 0;
+    a.adaptive = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = reset_counter(a, st))) return rc;
+    return vg::launch_points(a, it->precision == VG_F64, st);
+}
+
+extern "C" int vg_reduce_kept(const vg_integrator *it, uint32_t itn, const double *u, const void *f, int f_dtype,
+                              const void *keep, size_t keep_bytes, void *stream)
+{
+    VG_RANGE("vg_reduce_kept");
+    vg_clear_error();
+    IterArgs a;
+    int rc = fill_args(a, it, itn, u);   // itn, u: the finalize regenerates a cut hypercube's last sample
+                                         // under adapt_to_errors
+    if (rc) return rc;
+    if ((rc = keep_args(a, it, const_cast<void *>(keep), keep_bytes))) return rc;
+    a.f_in = f;
+    a.f_f64 = (f_dtype == VG_F64);
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = vg::launch_reduce_kept(a, it->precision == VG_F64, st))) return rc;   // static tiles
+    return vg::finalize_launch(a, st, it->precision == VG_F32);
+}
+
 static unsigned long long *g_term_count = nullptr;
 namespace vg {
 uint32_t g_wait_iters = VG_WAIT_ITERS_DEFAULT;

@@ -31,11 +31,14 @@ constexpr int ALLOC_NT = 256;    // allocation count / offsets blocks
 constexpr int ALLOC_PER = 4;     // hypercubes per thread there
 constexpr int FIN_NT = 1024;
 
-// POINTS: write points for a torch integrand; REDUCE: read f and reduce;
-// FUSED: evaluate a built-in integrand and reduce in one kernel; EVAL:
-// evaluate a built-in integrand and write f (first half of the split path
-// used for expensive integrands, followed by a REDUCE launch).
-enum { MODE_POINTS = 0, MODE_REDUCE = 1, MODE_FUSED = 2, MODE_EVAL = 3 };
+// POINTS: write points for a torch integrand (optionally also keep each
+// sample's Jacobian and training bins); REDUCE: read f and reduce,
+// regenerating each sample; REDUCE_KEPT: read f and the kept Jacobians and
+// bins and reduce (no Philox, no map: a stream over HBM); FUSED: evaluate a
+// built-in integrand and reduce in one kernel; EVAL: evaluate a built-in
+// integrand and write f (first half of the split path used for expensive
+// integrands, followed by a REDUCE launch).
+enum { MODE_POINTS = 0, MODE_REDUCE = 1, MODE_FUSED = 2, MODE_EVAL = 3, MODE_REDUCE_KEPT = 4 };
 
 // Partial statistics of a hypercube cut by a tile boundary.
 struct TileRec {
@@ -86,7 +89,10 @@ struct IterArgs {
     uint32_t stream;
     uint32_t itn;
     const double *u;          // injected uniforms [n, dim] or nullptr
-    const void *f_in;         // MODE_REDUCE
+    const void *f_in;         // MODE_REDUCE, MODE_REDUCE_KEPT
+    void *keep_jac;           // per-sample Jacobian (T): written by MODE_POINTS when set, read by REDUCE_KEPT
+    unsigned short *keep_bins;   // per-sample training bins [n, keep_bstride] (0xffff: none), likewise
+    int keep_bstride;            // bins per kept sample: dim rounded up to 4 (8-byte aligned rows)
     int f_f64;
     void *x_out, *y_out;      // MODE_POINTS
     float *f_eval;            // MODE_EVAL output / MODE_REDUCE input of the split path
@@ -667,7 +673,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
     constexpr int KSUB = TT / BASE_TILE;   // base tiles per tile
     const int dim = a.dim;
     const int tid = threadIdx.x;
-    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
+    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED || MODE == MODE_REDUCE_KEPT);
     const int use_bins = NEED_RED && (a.train || a.train_hc);   // per-sample bins in shared memory
     const SmemPlan sp = smem_plan<T>(dim, a.maxK, TT, a.table_smem, a.hist_smem, a.tab_len,
                                      use_bins, NEED_RED);
@@ -879,8 +885,9 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
         // the uniforms of all the thread's samples first (into xs): the
         // draws do not depend on the hypercube walk below, so the S samples'
         // Philox rounds interleave instead of waiting on one another
+        // (REDUCE_KEPT reads the kept Jacobians instead)
 #pragma unroll
-        for (int k = 0; k < S; k++) {
+        for (int k = 0; k < S && MODE != MODE_REDUCE_KEPT; k++) {
 #pragma unroll
             for (int d = 0; d < DIMB; d++) xs[k][d] = (T)0.5;
             if (k < nmine) {
@@ -924,9 +931,22 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                 const int nh = win_n[cur];
                 T jac = (T)1;
                 T yv[DIMB];
+                unsigned short kbin[DIMB];   // MODE_POINTS: the bins to keep
+                if constexpr (MODE == MODE_REDUCE_KEPT) {
+                    jac = ((const T *)a.keep_jac)[ig];
+                    if (use_bins) {   // rows of 4 bins, one 8-byte load each
+                        const uint2 *src = reinterpret_cast<const uint2 *>(a.keep_bins + ig * a.keep_bstride);
+                        for (int q = 0; q < dim; q += 4) {
+                            const uint2 v = src[q >> 2];
+                            const unsigned short b4[4] = {(unsigned short)(v.x & 0xffffu), (unsigned short)(v.x >> 16),
+                                                          (unsigned short)(v.y & 0xffffu), (unsigned short)(v.y >> 16)};
+                            for (int r = 0; r < 4 && q + r < dim; r++) sbins[(li0 + k) * dim + q + r] = b4[r];
+                        }
+                    }
+                }
 #pragma unroll
                 for (int d = 0; d < DIMB; d++) {
-                    if (d >= dim) continue;
+                    if (d >= dim || MODE == MODE_REDUCE_KEPT) continue;
                     const int K = a.ninc[d];
                     T yd, yn, yfl;
                     const int iy = sample_y<T>(y0[d], y0f[d], xs[k][d], a.nstrat[d], rstrat[d], K, Kf[d], yd, yn, yfl);
@@ -957,6 +977,18 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                         jac = (T)((float)jac * ((float)e.y * Kf[d]));
                     }
                     if (use_bins) sbins[(li0 + k) * dim + d] = sample_bin<T>(yd, iy, K);
+                    if (MODE == MODE_POINTS) kbin[d] = sample_bin<T>(yd, iy, K);
+                }
+                if (MODE == MODE_POINTS && a.keep_bins) {   // rows of 4 bins, one 8-byte store each
+                    uint2 *dst = reinterpret_cast<uint2 *>(a.keep_bins + ig * a.keep_bstride);
+#pragma unroll
+                    for (int q = 0; q < DIMB; q += 4) {
+                        if (q >= dim) break;
+                        unsigned int w4[4];
+#pragma unroll
+                        for (int r = 0; r < 4; r++) w4[r] = (q + r < dim && q + r < DIMB) ? kbin[q + r] : 0xffffu;
+                        dst[q >> 2] = make_uint2(w4[0] | (w4[1] << 16), w4[2] | (w4[3] << 16));
+                    }
                 }
                 // weight, pyx:1748-1749: jac *= dv_y / neval_hcube
                 if (sizeof(T) == 8) wg[k] = (T)__dmul_rn((double)jac, __ddiv_rn(dv_y, (double)nh));
@@ -977,6 +1009,7 @@ __device__ __forceinline__ void tile_body(const IterArgs &a, const VgParams &prm
                     }
                     if (a.wgt_out) a.wgt_out[ig] = (double)wg[k];
                     if (a.hc_out) a.hc_out[ig] = h0 + cur;
+                    if (a.keep_jac) ((T *)a.keep_jac)[ig] = jac;
                 }
             }
         }
@@ -1381,8 +1414,9 @@ template <typename T, int MODE, int KIND, int DIMB, int S>
 constexpr int tile_min_blocks()
 {
     return (sizeof(T) == 4 && DIMB <= 4 &&
-            ((MODE == MODE_FUSED && KIND == VG_F_RIDGE) || MODE == MODE_REDUCE || MODE == MODE_POINTS))
-               ? (S == 2 ? 4 : 2)
+            ((MODE == MODE_FUSED && KIND == VG_F_RIDGE) || MODE == MODE_REDUCE || MODE == MODE_POINTS ||
+             MODE == MODE_REDUCE_KEPT))
+               ? ((S == 2 || (MODE == MODE_POINTS && S == 4)) ? 4 : 2)
                : 1;
 }
 
@@ -1406,7 +1440,7 @@ int launch_tile(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st)
     const int dim = a.dim;
     a.tab_len = tab_len;
     a.T = TT;
-    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED);
+    constexpr int NEED_RED = (MODE == MODE_REDUCE || MODE == MODE_FUSED || MODE == MODE_REDUCE_KEPT);
     const int bins = NEED_RED && (a.train || a.train_hc);
     const size_t budget = 200 * 1024;
     // the 4-CTA-per-SM configuration reads the FP32 grid table through L1
@@ -1452,6 +1486,7 @@ int launch_dim(IterArgs &a, const VgParams *prm, int tab_len, cudaStream_t st);
 
 int finalize_launch(IterArgs &a, cudaStream_t st, int fast);
 int launch_reduce(IterArgs &a, int f64, cudaStream_t st);
+int launch_reduce_kept(IterArgs &a, int f64, cudaStream_t st);
 // IterArgs of one integral (pointers into its workspace) and its adapt scratch grid
 int fill_iter_args(IterArgs &a, const vg_integrator *it, uint32_t itn, const double *u);
 void scratch_grid(const vg_integrator *it, double **new_grid, double **new_inc);

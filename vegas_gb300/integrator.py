@@ -296,16 +296,32 @@ class Integrator(object):
         N.check(L.vg_allocate(ctypes.byref(it), N.stream_ptr(self.device)))
 
     # ------------------------------------------------------------- sampling
-    def _points(self, it, ncap, itn, u, want_y=False, want_hc=False):
+    def _points(self, it, ncap, itn, u, want_y=False, want_hc=False, want_w=True, keep=None):
+        """x (and y, weights, hypercubes) of the current allocation; with
+        ``keep`` (a device buffer of vg_keep_bytes) the sampler also keeps
+        each sample's Jacobian and training bins for vg_reduce_kept."""
         L = N.load()
         dt = torch.float64 if self.precision == 'fp64' else torch.float32
         x = torch.empty((ncap, self.dim), dtype=dt, device=self.device)
         y = torch.empty((ncap, self.dim), dtype=dt, device=self.device) if want_y else None
-        w = torch.empty(ncap, dtype=torch.float64, device=self.device)
+        w = torch.empty(ncap, dtype=torch.float64, device=self.device) if want_w else None
         hc = torch.empty(ncap, dtype=torch.int64, device=self.device) if want_hc else None
-        N.check(L.vg_sample(ctypes.byref(it), itn, N.ptr(u), N.ptr(x), N.ptr(y), N.ptr(w),
-                            N.ptr(hc), ncap, N.stream_ptr(self.device)))
+        if keep is None:
+            N.check(L.vg_sample(ctypes.byref(it), itn, N.ptr(u), N.ptr(x), N.ptr(y), N.ptr(w),
+                                N.ptr(hc), ncap, N.stream_ptr(self.device)))
+        else:
+            N.check(L.vg_sample_keep(ctypes.byref(it), itn, N.ptr(u), N.ptr(x), N.ptr(y), N.ptr(w),
+                                     N.ptr(hc), ncap, N.ptr(keep), keep.numel(), N.stream_ptr(self.device)))
         return x, y, w, hc
+
+    def _keep_buffer(self, it, ncap):
+        """Device buffer for the kept Jacobians and training bins of one
+        iteration's samples (reused across iterations)."""
+        L = N.load()
+        need = int(L.vg_keep_bytes(ctypes.byref(it), ncap))
+        if getattr(self, '_keep', None) is None or self._keep.numel() < need:
+            self._keep = torch.empty(need, dtype=torch.uint8, device=self.device)
+        return self._keep
 
     def _draw_u(self, n):
         """Injected uniforms [n, dim] (FP64, device) from ran_array_generator,
@@ -523,7 +539,14 @@ class Integrator(object):
                     N.check(L.vg_fused_iteration(ctypes.byref(it), itn_word, N.ptr(u),
                                                  int(fcn.kind), N.dbl_array(p), len(p), stream))
                 else:
-                    x, yv, w, _ = self._points(it, ncap, itn_word, u, want_y=self.uses_jac)
+                    # the sampler keeps each sample's Jacobian and training
+                    # bins, so the reduction streams them instead of
+                    # regenerating the samples; the weights are written only
+                    # while an array-valued integrand may need them
+                    keep = self._keep_buffer(it, ncap)
+                    want_w = fshape is None or bool(fshape)
+                    x, yv, w, _ = self._points(it, ncap, itn_word, u, want_y=self.uses_jac, want_w=want_w,
+                                               keep=keep)
                     jac = self.map.jac1d(yv[:n]) if self.uses_jac else None
                     f = None
                     nb = self._eval_batch_size()
@@ -551,7 +574,8 @@ class Integrator(object):
                         raise ValueError('integrand evaluates to nan')
                     fdt = N.VG_F64 if dt == torch.float64 else N.VG_F32
                     f0 = f if f.dim() == 1 else f[:, 0].contiguous()
-                    N.check(L.vg_reduce(ctypes.byref(it), itn_word, N.ptr(u), N.ptr(f0), fdt, stream))
+                    N.check(L.vg_reduce_kept(ctypes.byref(it), itn_word, N.ptr(u), N.ptr(f0), fdt, N.ptr(keep),
+                                             keep.numel(), stream))
                     if f.dim() > 1:
                         arr = self._reduce_array(it, f, fdt, w)
             # adapt the map on the device before reading the iteration record
