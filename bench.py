@@ -254,12 +254,12 @@ def dropin_line(dev, neval=10 ** 7, nitn=5, reps=5):
             'bound': 'hbm', 'unit': 'GB/s', 'peak': hbm,
             'peak_source': 'MEASURED_PEAKS.json hbm_gbs' if 'hbm_gbs' in peaks else 'fallback',
             'traffic_source': 'dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu, '
-                              'bench.py --device-loop-only --case dropin)',
+                              'bench.py --device-loop-only --case dropin, about 9.3e6 evaluations)',
             'sample_kernel': {'bytes_per_eval': b_s, 'achieved': b_s * n / t_s / 1e9,
-                              'frac': b_s * n / t_s / 1e9 / hbm, 'traffic': None,
+                              'frac': b_s * n / t_s / 1e9 / hbm, 'traffic': 227.2e6,
                               'writes': 'x (FP32, 4 dim B), Jacobian (4 B), training bins (2 dim B)'},
             'reduce_kernel': {'bytes_per_eval': b_r, 'achieved': b_r * n / t_r / 1e9,
-                              'frac': b_r * n / t_r / 1e9 / hbm, 'traffic': None,
+                              'frac': b_r * n / t_r / 1e9 / hbm, 'traffic': 179.3e6,
                               'reads': 'f (4 B), Jacobian (4 B), training bins (2 dim B); forms the '
                                        'two-pass hypercube sums and the training histogram'}},
     }
@@ -289,7 +289,20 @@ def batched_line(dev, reps=2):
     res = B.results()
     exact = np.array([f.exact(int(d)) for f, d in zip(fs, dims)])
     pulls = (res[:, 0] - exact) / res[:, 1]
+    # where the launch's time goes: every integral's start and end (device
+    # globaltimer) in one more, instrumented launch
+    t_s, t_e, _ = B.timeline()
+    span = float(t_e.max()) / 1e9
+    dur = (t_e - t_s) / 1e9
+    bucket = np.where(dims <= 4, 0, np.where(dims <= 8, 1, 2))
+    timeline = {'launch_span_s': span, 'longest_integral_s': float(dur.max()),
+                'longest_integral_dim': int(dims[int(np.argmax(dur))]),
+                'longest_integral_neval': int(nevals[int(np.argmax(dur))]),
+                'last_start_s': float(t_s.max()),
+                'per_bucket_end_s': {str(b): float(t_e[bucket == b].max()) for b in range(3) if np.any(bucket == b)},
+                'note': 'one instrumented launch; the tail is span - last_start_s (no integral left to start)'}
     return {
+        'timeline': timeline,
         'workload': '4096 Lorentzian-product integrals, dim U{3..9}, centres U[0.2,0.8]^d, widths '
                     'log-U[0.01,0.1], neval log-U[1e4,1e6] per integral, nitn 8+8, one persistent '
                     'kernel per 16 iterations replayed from a CUDA graph, FP32 eval + FP64 sums',
@@ -384,6 +397,52 @@ def _jsonable(o):
     if isinstance(o, np.ndarray):
         return o.tolist()
     raise TypeError(type(o).__name__)
+
+
+def lattice_flow_line(dev, lams=(0.01, 0.1, 1.0), neval=1 << 20):
+    """The flow on the lattice couplings: for a subset of the 64 lambda of
+    the scan, flow-augmented vegas+ (FlowIntegrator: 6 coupling layers,
+    32-bin splines, 2x128 conditioners, as on the mixture) against plain
+    vegas+ at the same evaluations per iteration; variance per evaluation,
+    seconds per iteration, pulls against the FP64 transfer-matrix value and
+    the gate's decision (plain vegas+ judges by variance per evaluation)."""
+    import numpy as np
+    import torch
+    import vegas_gb300 as vg
+    from vegas_gb300.flow_vegas import FlowIntegrator
+    out = {'workload': 'dim-16 periodic lattice action, a=0.5, x in [-5,5]^16, lambda in %s, %d evaluations '
+                       'per iteration; plain vegas+ 50 + 20 iterations; flow-augmented vegas+ 30 plain + 40 '
+                       'flow (trained) + 20 measured' % (list(lams), neval), 'per_lambda': {}}
+    lim = 16 * [[-5.0, 5.0]]
+    for lam in lams:
+        f = vg.LatticeAction(0.5, float(lam))
+        ex = f.exact(16)
+        I = vg.Integrator(lim, neval=neval, seed=3, device=dev)
+        I(f, nitn=50)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = I(f, nitn=20)
+        torch.cuda.synchronize()
+        tp = (time.perf_counter() - t0) / 20
+        fi = FlowIntegrator(lim, neval=neval, seed=3, device=dev, plain_itn=30, kl_itn=10, train_itn=40,
+                            grace=10, patience=3, train_steps=4, train_batch=1 << 15, lr=1e-3)
+        fi(f, nitn=70)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rf = fi(f, nitn=20)
+        torch.cuda.synchronize()
+        tf = (time.perf_counter() - t0) / 20
+        vp = r.sdev ** 2 * r.sum_neval / ex ** 2
+        vf = rf.sdev ** 2 * rf.sum_neval / ex ** 2
+        out['per_lambda'][str(lam)] = {
+            'exact': ex, 'plain': str(r), 'plain_pull': (r.mean - ex) / r.sdev if r.sdev > 0 else None,
+            'plain_rel_var_per_eval': vp, 'plain_seconds_per_iteration': tp,
+            'flow': str(rf), 'flow_pull': (rf.mean - ex) / rf.sdev if rf.sdev > 0 else None,
+            'flow_rel_var_per_eval': vf, 'flow_seconds_per_iteration': tf,
+            'flow_active_at_end': bool(fi.flow_on),
+            'variance_per_eval_ratio_flow_over_plain': vf / vp if vp > 0 else None,
+            'variance_x_time_ratio_flow_over_plain': (vf * tf) / (vp * tp) if vp > 0 and tp > 0 else None}
+    return out
 
 
 def max_over_ranks(value, world, device=None):
@@ -632,9 +691,11 @@ def gpu_arm(args):
         ridge64 = ridge_fp64_line(dev)
         if not args.no_reference_runs:
             refruns = reference_runs(dev)
+    lattice_flow = None
     if not args.no_batch and rank == 0:
         batched = batched_line(dev)
         lattice = lattice_line(dev)
+        lattice_flow = lattice_flow_line(dev)
     if world > 1:
         dist.destroy_process_group()
     if rank != 0:
@@ -681,6 +742,7 @@ def gpu_arm(args):
         'time_to_1e-4': tta,
         'batched': batched,
         'lattice_scan': lattice,
+        'lattice_flow': lattice_flow,
         'small_fp64': small,
         'dropin': dropin,
         'ridge_fp64': ridge64,

@@ -394,6 +394,12 @@ int vg_batch_launch(const void *table, int njobs, int kind, int nitn, int nwarm,
                     const int *seg, unsigned int *queue, unsigned int *sync, const int *group, int *status,
                     const size_t *smem, const int *grid, const int *cfg, void *stream);
 
+/* Instrumentation of the batched launch: while set (device
+ * uint64[3 * njobs], NULL = off), vg_batch_prepare makes each integral j
+ * record the start and end of its iterations (globaltimer, ns) and its SM in
+ * stamps[3j .. 3j+2]. */
+int vg_batch_set_stamps(unsigned long long *stamps);
+
 /* Instrumentation: while set (device counter, NULL = off), the FP32 ridge
  * adds the number of Gaussian terms it evaluates -- the ones that can be
  * nonzero in FP32; the rest are exactly zero and skipped. */

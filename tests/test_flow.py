@@ -7,10 +7,15 @@ rounding of activations and weights:
   sampling / density outputs z:      |dz| <= 2e-3 absolute
   logdet:                            |d logdet| <= 2e-2 absolute (6 layers)
   round trip density(sample(zhat)):  |d zhat| <= 2e-3
-  gradient of the training loss:     relative L2 error <= 3e-2 and
-                                     cosine similarity >= 0.999
-(the backward rounds dL/dout, dL/dh2 and dL/dh1 to BF16 for the tensor-core
-weight-gradient GEMMs).
+  gradient of the training loss:     relative L2 error <= 2u overall and
+                                     <= 4u in every parameter block (W1,
+                                     b1, W2, b2, W3, b3 of each layer),
+                                     u = 2^-9 the BF16 unit roundoff
+(the backward rounds dL/dout, dL/dh2', dL/dh1' and the transposed
+activations to BF16 for the tensor-core weight-gradient GEMMs -- one BF16
+rounding of each operand, which the oracle does not emulate -- so each
+block carries a relative error of order u; measured: at most 3u per block
+and 1.3u overall on these cases).
 """
 import ctypes
 
@@ -190,10 +195,17 @@ def test_gpu_flow_gradient_vs_oracle(dim):
     loss = float(fl.loss.item()) / w.astype(np.float64).sum()
     lo, go = _oracle_bf16(F.loss_and_grad, theta, x.astype(np.float64), w.astype(np.float64), dim)
     assert abs(loss - lo) <= 1e-3 * max(1.0, abs(lo))
+    u = 2.0 ** -9                      # BF16 unit roundoff
     err = np.linalg.norm(g - go) / np.linalg.norm(go)
-    cos = float(g @ go / (np.linalg.norm(g) * np.linalg.norm(go)))
-    assert err <= 3e-2, err
-    assert cos >= 0.999, cos
+    assert err <= 2 * u, err
+    o = 0
+    for li, sz in enumerate(F.layer_sizes(dim, 6, 32, 128)):
+        for name in ('W1', 'b1', 'W2', 'b2', 'W3', 'b3'):
+            a, b = g[o:o + sz[name]], go[o:o + sz[name]]
+            o += sz[name]
+            eb = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            assert eb <= 4 * u, (li, name, eb)
+    assert o == len(go)
 
 
 @pytest.mark.gpu

@@ -62,3 +62,24 @@ def test_flow_switched_off_when_plain_vegas_wins():
     assert F.flow_dead and not F.flow_on
     assert abs(r.mean - 2.0) < 1e-6
     assert not F.history[-1]['flow']
+
+
+@pytest.mark.gpu
+def test_flow_on_lattice_is_unbiased():
+    """The flow in vegas's y-space on the dim-16 lattice action (one coupling
+    of the lambda scan): every flow iteration carries the flow's exact
+    log-determinant, so the average of the flow iterations agrees with the
+    FP64 transfer-matrix value (within 5 sigma), trained or not."""
+    from vegas_gb300.flow_vegas import FlowIntegrator
+    f = vg.LatticeAction(0.5, 0.05)
+    ex = f.exact(16)
+    fi = FlowIntegrator(16 * [[-5.0, 5.0]], neval=1 << 18, seed=21, plain_itn=20, kl_itn=5, train_itn=15,
+                        grace=100, patience=3, train_steps=2, train_batch=1 << 13)
+    fi(f, nitn=50)
+    flows = [h for h in fi.history if h['flow']]
+    assert len(flows) == 30
+    w = np.array([1.0 / h['sdev'] ** 2 for h in flows[-15:]])
+    m = np.array([h['mean'] for h in flows[-15:]])
+    mean = float(np.sum(w * m) / np.sum(w))
+    sdev = float(np.sum(w) ** -0.5)
+    assert abs(mean - ex) < 5 * sdev, (mean, sdev, ex)

@@ -178,6 +178,7 @@ SIGNATURES = {
     'vg_set_eval_split': (I32, [I32]),
     'vg_set_wait_budget': (I32, [I64]),
     'vg_set_dropin_tuning': (I32, [I32, I32]),
+    'vg_batch_set_stamps': (I32, [P]),
     'vg_set_tile_tuning': (I32, [I32, I32, I32]),
     'vg_probe_mufu_ex2': (I32, [P, I64, I32, P]),
     'vg_probe_fp64_fma': (I32, [P, I64, I32, P]),

@@ -270,6 +270,26 @@ class BatchIntegrator(object):
         """Every iteration's (mean, variance, evaluations) (numpy [njobs, nitn, 3])."""
         return self.out.cpu().numpy()
 
+    def timeline(self):
+        """One launch with every integral's start and end recorded on the
+        device (globaltimer): returns (start_ns, end_ns, sm) arrays
+        [njobs], times relative to the earliest start.  The job table is
+        rebuilt with the instrumentation for this launch and without it
+        afterwards."""
+        L = N.load()
+        stamps = torch.zeros(3 * self.njobs, dtype=torch.int64, device=self.device)
+        N.check(L.vg_batch_set_stamps(N.ptr(stamps)))
+        try:
+            self.set_variant(self.variant)
+        finally:
+            N.check(L.vg_batch_set_stamps(None))
+        self.launch()
+        torch.cuda.synchronize(self.device)
+        self.set_variant(self.variant)
+        s = stamps.view(self.njobs, 3).cpu().numpy()
+        t0 = s[:, 0].min()
+        return s[:, 0] - t0, s[:, 1] - t0, s[:, 2]
+
     def integrator_struct(self, j):
         """The C-ABI record of integral j (device pointers into the arena:
         grid, inc, sigf, training histogram, stats, workspace)."""

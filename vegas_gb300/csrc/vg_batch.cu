@@ -116,6 +116,16 @@ AuxStreams *aux_of_current()
 
 }  // namespace
 
+// Instrumentation: while set, vg_batch_prepare points integral j's job at
+// stamps[3j .. 3j+2] (start and end of its iterations, globaltimer ns; SM).
+static unsigned long long *g_batch_stamps = nullptr;
+
+extern "C" int vg_batch_set_stamps(unsigned long long *stamps)
+{
+    g_batch_stamps = stamps;
+    return VG_OK;
+}
+
 extern "C" int vg_batch_variants(void) { return NCONFIG; }
 
 extern "C" size_t vg_batch_table_bytes(int njobs)
@@ -220,6 +230,7 @@ extern "C" int vg_batch_prepare(const vg_integrator *its, int njobs, int kind, c
         J.out = out + (size_t)j * 3 * nitn;
         J.res = res + (size_t)j * 4;
         J.sync = sync != nullptr ? sync + j : nullptr;
+        J.stamp = g_batch_stamps != nullptr ? g_batch_stamps + 3 * (size_t)j : nullptr;
         smem_max[b] = need > smem_max[b] ? need : smem_max[b];
     }
     cudaStream_t st = (cudaStream_t)stream;

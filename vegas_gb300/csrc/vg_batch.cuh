@@ -26,7 +26,22 @@ struct BatchJob {
     unsigned int *sync;          // group barrier counter (group mode)
     int bucket;                  // dimension bucket: 0 (dim <= 4), 1 (<= 8), 2 (<= 16)
     int adapt;                   // adapt the map after each iteration
+    unsigned long long *stamp;   // instrumentation (or nullptr): [0] start, [1] end (globaltimer ns), [2] SM
 };
+
+__device__ __forceinline__ unsigned long long vg_globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned int vg_smid()
+{
+    unsigned int r;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+    return r;
+}
 
 // Barrier of the G CTAs working on one integral (group mode; the launch is
 // cooperative, so they are co-resident).  Thread 0 releases this CTA's
@@ -362,6 +377,10 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
         if (q >= njobs) break;
         const int j = order[q];
         const BatchJob &J = jobs[j];
+        if (J.stamp != nullptr && tid == 0 && rank == 0) {
+            J.stamp[0] = vg_globaltimer();
+            J.stamp[2] = vg_smid();
+        }
         {
             const int nw = (int)(sizeof(IterArgs) / 4);
             const uint32_t *src = reinterpret_cast<const uint32_t *>(&J.a);
@@ -397,6 +416,7 @@ __global__ void __launch_bounds__(NT, MINB) batch_kernel(const BatchJob *__restr
         }
         if (rank == 0) cta_ravg(J, nitn, nwarm);
         __syncthreads();
+        if (J.stamp != nullptr && tid == 0 && rank == 0) J.stamp[1] = vg_globaltimer();
     }
 }
 
