@@ -1016,7 +1016,7 @@ __host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
     p.oW1 = o; o += sizeof(float) * FH * 8;
     p.ob1 = o; o += sizeof(float) * FH;
     p.ob2 = o; o += sizeof(float) * FH;
-    p.ob3 = o; o += sizeof(float) * 8 * (2 * FMAXK + 1);
+    p.ob3 = o; o += sizeof(float) * 8 * (2 * g.K + 1);   // dB <= 8 coordinates of 2K + 1 outputs
     p.oZ = o;  o += sizeof(float) * (size_t)ST * FROWS * p.zst;
     p.oLD = o; o += sizeof(float) * UNH * (size_t)ST * FROWS;
     p.total = o + 1024;          // + alignment slack of the dynamic base
@@ -1382,10 +1382,16 @@ template <int K>
 static int flow_pass_umma_k(const FlowGeom &g, const vg_flow *fl, int dir, int64_t n, const float *zin,
                             float *zout, float *logdet, float *zl, cudaStream_t st, int *rc)
 {
-    const size_t limit = VG_FLOW_SMEM_MAX;
+    const void *k = dir == 0 ? (const void *)flow_pass_umma_kernel<K, 0> : (const void *)flow_pass_umma_kernel<K, 1>;
+    // the dynamic shared memory left beside the kernel's static shared memory
+    size_t stat = 0;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k) == cudaSuccess) stat = fa.sharedSizeBytes;
+    else (void)cudaGetLastError();
+    const size_t limit = VG_FLOW_SMEM_MAX > stat ? VG_FLOW_SMEM_MAX - stat : 0;
     int STmax = UST_MAX;
     while (STmax > 1 && umma_plan(g, STmax).total > limit) STmax--;
-    if (umma_plan(g, STmax).total > limit) return 0;
+    if (umma_plan(g, STmax).total > limit) return 0;   // the mma.sync pass instead
     // super-tile size: as large as shared memory allows (weights are fetched
     // once per layer and super-tile), but small enough that the static
     // round-robin over CTAs ends within one super-tile of balance
@@ -1397,8 +1403,10 @@ static int flow_pass_umma_k(const FlowGeom &g, const vg_flow *fl, int dir, int64
     if (ST > STmax) ST = STmax;
     const UmmaPlan pl = umma_plan(g, ST);
     size_t smem = pl.total < 120 * 1024 ? 120 * 1024 : pl.total;   // one CTA per SM (TMEM: 512 columns)
-    const void *k = dir == 0 ? (const void *)flow_pass_umma_kernel<K, 0> : (const void *)flow_pass_umma_kernel<K, 1>;
-    if ((*rc = set_smem(k, smem))) return 1;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        (void)cudaGetLastError();   // not enough shared memory on this part: the mma.sync pass instead
+        return 0;
+    }
     const int64_t rows_per = (int64_t)ST * FROWS;
     const int64_t nsuper = (n + rows_per - 1) / rows_per;
     int64_t grid = (int64_t)vg_num_sms();
