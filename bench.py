@@ -298,8 +298,9 @@ def batched_line(dev, reps=2):
     timeline = {'launch_span_s': span, 'longest_integral_s': float(dur.max()),
                 'longest_integral_dim': int(dims[int(np.argmax(dur))]),
                 'longest_integral_neval': int(nevals[int(np.argmax(dur))]),
-                'last_start_s': float(t_s.max()),
-                'per_bucket_end_s': {str(b): float(t_e[bucket == b].max()) for b in range(3) if np.any(bucket == b)},
+                'last_start_s': float(t_s.max()) / 1e9,
+                'per_bucket_end_s': {str(b): float(t_e[bucket == b].max()) / 1e9 for b in range(3)
+                                     if np.any(bucket == b)},
                 'note': 'one instrumented launch; the tail is span - last_start_s (no integral left to start)'}
     return {
         'timeline': timeline,
