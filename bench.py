@@ -53,11 +53,12 @@ def parse():
     ap.add_argument('--no-tta', action='store_true')
     ap.add_argument('--device-loop-only', action='store_true',
                     help='run only the device-resident iteration loop (for profilers)')
-    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch', 'dropin'],
+    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch', 'dropin', 'lattice'],
                     help='with --device-loop-only: which kernel family to run (for profilers): '
                          'ridge = the fused vegas+ iteration, flow = the flow sampling pass '
                          '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals, '
-                         'dropin = the drop-in path (torch integrand, sampling and reduction kernels)')
+                         'dropin = the drop-in path (torch integrand, sampling and reduction kernels), '
+                         'lattice = the lambda-scan launch on 16 couplings x 2e6 evaluations')
     ap.add_argument('--no-batch', action='store_true', help='skip the batched many-integral line')
     ap.add_argument('--no-reference-runs', action='store_true',
                     help='skip the normal-mode comparisons with oracle runs of the same workloads')
@@ -138,6 +139,16 @@ def profile_case(args, dev):
         from vegas_gb300.batch import BatchIntegrator
         fs, nevals, _ = batch_workload(256)
         B = BatchIntegrator(fs, nevals, nitn=2, nwarm=1, seed=99, device=dev, variant=(1, 1, 0))
+        for _ in range(args.warmup + args.steps):
+            B.launch()
+    elif args.case == 'lattice':
+        import numpy as np
+        import vegas_gb300 as vg
+        from vegas_gb300.batch import BatchIntegrator
+        lams = np.exp(np.linspace(np.log(0.01), np.log(1.0), 16))
+        fs = [vg.LatticeAction(0.5, float(l)) for l in lams]
+        B = BatchIntegrator(fs, [2 * 10 ** 6] * 16, nitn=2, nwarm=1, seed=7, dims=[16] * 16,
+                            limits=(-5.0, 5.0), device=dev, variant=(0, 0, 2))
         for _ in range(args.warmup + args.steps):
             B.launch()
     torch.cuda.synchronize()
