@@ -411,7 +411,7 @@ def _jsonable(o):
     raise TypeError(type(o).__name__)
 
 
-def lattice_flow_line(dev, lams=(0.01, 0.1, 1.0), neval=1 << 20):
+def lattice_flow_line(dev, nlam=8, neval=1 << 20):
     """The flow on the lattice couplings: for a subset of the 64 lambda of
     the scan, flow-augmented vegas+ (FlowIntegrator: 6 coupling layers,
     32-bin splines, 2x128 conditioners, as on the mixture) against plain
@@ -422,9 +422,12 @@ def lattice_flow_line(dev, lams=(0.01, 0.1, 1.0), neval=1 << 20):
     import torch
     import vegas_gb300 as vg
     from vegas_gb300.flow_vegas import FlowIntegrator
+    # every 9th coupling of the 64-coupling scan (log-spaced in [0.01, 1]) and the last
+    scan = np.exp(np.linspace(np.log(0.01), np.log(1.0), 64))
+    lams = [float(v) for v in scan[np.linspace(0, 63, nlam).round().astype(int)]]
     out = {'workload': 'dim-16 periodic lattice action, a=0.5, x in [-5,5]^16, lambda in %s, %d evaluations '
                        'per iteration; plain vegas+ 50 + 20 iterations; flow-augmented vegas+ 30 plain + 40 '
-                       'flow (trained) + 20 measured' % (list(lams), neval), 'per_lambda': {}}
+                       'flow (trained) + 20 measured' % ([round(v, 4) for v in lams], neval), 'per_lambda': {}}
     lim = 16 * [[-5.0, 5.0]]
     for lam in lams:
         f = vg.LatticeAction(0.5, float(lam))
@@ -454,6 +457,16 @@ def lattice_flow_line(dev, lams=(0.01, 0.1, 1.0), neval=1 << 20):
             'flow_active_at_end': bool(fi.flow_on),
             'variance_per_eval_ratio_flow_over_plain': vf / vp if vp > 0 else None,
             'variance_x_time_ratio_flow_over_plain': (vf * tf) / (vp * tp) if vp > 0 and tp > 0 else None}
+    rv = [v['variance_per_eval_ratio_flow_over_plain'] for v in out['per_lambda'].values()]
+    rt = [v['variance_x_time_ratio_flow_over_plain'] for v in out['per_lambda'].values()]
+    out['summary'] = {
+        'couplings': len(rv),
+        'geo_mean_variance_per_eval_ratio': float(np.exp(np.mean(np.log(rv)))),
+        'geo_mean_variance_x_time_ratio': float(np.exp(np.mean(np.log(rt)))),
+        'flow_wins_variance_x_time': int(sum(1 for x in rt if x < 1.0)),
+        'max_abs_flow_pull': float(max(abs(v['flow_pull']) for v in out['per_lambda'].values())),
+        'note': 'ratios below 1: the flow is better; per coupling the better of the two is what a gate on '
+                'variance x time would keep'}
     return out
 
 
