@@ -121,6 +121,11 @@ int vg_set_strata(int dim, int mode, int64_t *neval, int neval_given, const int6
                   double max_mem, int minimize_mem, int64_t maxinc_axis, int64_t *nstrat_out,
                   int64_t *ninc_out, int64_t *min_neval_hcube_out);
 
+/* Set a device record to zero but for sum_sigf, the vegas+ normaliser the
+ * next allocation uses (the value Integrator carries between iterations,
+ * pyx:2209-2215); enqueued on `stream`. */
+int vg_stats_reset(vg_stats *stats, double sum_sigf, void *stream);
+
 /* Upper bound on the evaluations of one iteration (capacity of x / f buffers). */
 int64_t vg_neval_cap(const vg_integrator *it);
 

@@ -319,3 +319,40 @@ def test_reduce_kept_matches_reduce(precision):
     assert np.array_equal(ca, cb) and 0 < ca.sum() <= na * 4
     tol = 1e-12 if precision == 'fp64' else 1e-6
     assert np.max(np.abs(ha - hb)) <= tol * np.max(np.abs(ha))
+
+
+def test_stepwise_builtin_path_matches_pipelined(tmp_path):
+    """A built-in integrand with a host decision per iteration (rtol stop,
+    analyzer, save) runs the same kernels as the pipelined call: identical
+    iteration results on the same draws; rtol stops the loop; the analyzer
+    sees every iteration; save writes the running result.  FP64, compared
+    at the FP64 parity tolerance: the training histogram's FP64 atomics add
+    in arrival order, so the adapted maps of two runs differ at the 1e-16
+    level."""
+    import pickle
+    f = vg.Gaussian(a=60.0, c=0.45, dim=3)
+    A = vg.Integrator(3 * [[0, 1]], neval=20000, seed=17, precision='fp64')
+    B = vg.Integrator(3 * [[0, 1]], neval=20000, seed=17, precision='fp64')
+    ra = A(f, nitn=6)
+    seen = []
+
+    class Watch(object):
+        def begin(self, itn, integrator):
+            seen.append(('begin', itn))
+
+        def end(self, itn_result, result):
+            seen.append(('end', itn_result.mean))
+
+    out = str(tmp_path / 'r.pkl')
+    rb = B(f, nitn=6, rtol=1e-15, analyzer=Watch(), save=out)
+    assert len(ra.itn_results) == len(rb.itn_results) == 6
+    assert rel([x.mean for x in rb.itn_results], [x.mean for x in ra.itn_results]) <= RTOL
+    assert rel([x.sdev for x in rb.itn_results], [x.sdev for x in ra.itn_results]) <= RTOL
+    ga, gb = np.nan_to_num(A.map.grid), np.nan_to_num(B.map.grid)
+    assert np.max(np.abs(ga - gb)) <= RTOL and rel(B.sigf, A.sigf) <= 1e-10
+    assert len(seen) == 12 and seen[0] == ('begin', 0)
+    with open(out, 'rb') as fh:
+        assert abs(pickle.load(fh).mean - rb.mean) <= 1e-15 * abs(rb.mean)
+    C = vg.Integrator(3 * [[0, 1]], neval=20000, seed=17, precision='fp64')
+    rc = C(f, nitn=6, rtol=0.5)
+    assert rc.nitn == 1

@@ -144,6 +144,7 @@ SIGNATURES = {
     'vg_jac1d': (I32, [I32, P, P, I64, I64, P, P, I32, P]),
     'vg_add_training_data': (I32, [I32, P, I64, I64, P, P, I32, P, P, P]),
     'vg_allocate': (I32, [P, P]),
+    'vg_stats_reset': (I32, [P, DBL, P]),
     'vg_sample': (I32, [P, U32, P, P, P, P, P, I64, P]),
     'vg_reduce': (I32, [P, U32, P, P, I32, P]),
     'vg_keep_bytes': (SZ, [P, I64]),

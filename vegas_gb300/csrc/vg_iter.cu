@@ -702,6 +702,26 @@ extern "C" int vg_reduce(const vg_integrator *it, uint32_t itn, const double *u,
     return vg::finalize_launch(a, st, it->precision == VG_F32);
 }
 
+// An iteration record set to zero but for the carried sum_sigf.
+__global__ void stats_reset_kernel(vg_stats *st, double sum_sigf)
+{
+    if (threadIdx.x == 0) {
+        vg_stats z;
+        memset(&z, 0, sizeof(z));
+        z.sum_sigf = sum_sigf;
+        *st = z;
+    }
+}
+
+extern "C" int vg_stats_reset(vg_stats *stats, double sum_sigf, void *stream)
+{
+    vg_clear_error();
+    if (stats == nullptr) return vg_fail(VG_ERR_VALUE, "vg_stats_reset: no record");
+    stats_reset_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(stats, sum_sigf);
+    VG_LAUNCH_CHECK();
+    return VG_OK;
+}
+
 // The kept-sample buffer of vg_sample_keep / vg_reduce_kept: per sample its
 // Jacobian (the precision's float type), then its training bins (16-bit per
 // axis, rows padded to a multiple of 4 axes so that each 4 bins move as one

@@ -235,7 +235,14 @@ class Integrator(object):
         if (3 * dim + 3) * workspace + (0 if self.minimize_mem else self.nhcube) > self.max_mem:
             raise MemoryError('work arrays larger than max_mem; reduce min_neval_batch or '
                               'max_neval_hcube (or increase max_mem)')
-        self._work = None   # re-derive device workspace lazily
+        geometry = (tuple(int(v) for v in np.asarray(self.nstrat).reshape(-1)), self.nhcube,
+                    tuple(int(v) for v in np.asarray(self.map.ninc).reshape(-1)), self.neval,
+                    self.neval_frac, self.min_neval_hcube, self.max_neval_hcube, self.precision)
+        if geometry != getattr(self, '_geometry', None):
+            # a new workspace (zeroed: the allocation keeps its ticket and
+            # epoch words there) for the new strata / capacity
+            self._work = None
+            self._geometry = geometry
         return old_val
 
     # ----------------------------------------------------- device plumbing
@@ -282,9 +289,10 @@ class Integrator(object):
         return it, int(ncap)
 
     def _put_sum_sigf(self):
-        st = N.VgStats()
-        st.sum_sigf = self.sum_sigf
-        self._stats.copy_(torch.frombuffer(bytearray(bytes(st)), dtype=torch.uint8))
+        """The device record reset with the carried sum_sigf (the rest is
+        written by the iteration), enqueued on the current stream without a
+        host wait."""
+        N.check(N.load().vg_stats_reset(N.ptr(self._stats), float(self.sum_sigf), N.stream_ptr(self.device)))
 
     def _read_stats(self):
         b = self._stats.cpu().numpy().tobytes()
@@ -506,10 +514,11 @@ class Integrator(object):
             raise ValueError('integrand given is a class, not an object -- need to initialize?')
         kind = self._classify(fcn)
         result = RAvg(weighted=self.adapt)
-        if (kind == 'builtin' and self.ran_array_generator is None and not self.uses_jac
-                and self.analyzer is None and save is None and saveall is None
-                and self.rtol == 0 and self.atol == 0):
-            return self._call_pipelined(fcn, result)
+        if kind == 'builtin' and self.ran_array_generator is None and not self.uses_jac:
+            if (self.analyzer is None and save is None and saveall is None
+                    and self.rtol == 0 and self.atol == 0):
+                return self._call_pipelined(fcn, result)
+            return self._call_stepwise(fcn, result, save, saveall)
         L = N.load()
         stream = N.stream_ptr(self.device)
         dt = torch.float64 if self.precision == 'fp64' else torch.float32
@@ -669,6 +678,45 @@ class Integrator(object):
             gs.append(gv.gvar(st.mean, st.var ** 0.5))
             result.sum_neval += self.last_neval
         result.add_many(gs)
+        return result
+
+    def _call_stepwise(self, fcn, result, save, saveall):
+        """__call__ for a built-in integrand when iterations need a host
+        decision (rtol/atol stop, analyzer, save): one ``vg_iterate`` call
+        per iteration (the kernels of the pipelined path), its record copied
+        to pinned host memory and waited for on an event; sum_sigf stays on
+        the device between iterations.  The analyzer, save and stopping rule
+        run after each iteration as in the reference (pyx:2086-2226)."""
+        L = N.load()
+        stream = N.stream_ptr(self.device)
+        it, ncap = self._struct()
+        self._put_sum_sigf()
+        p = fcn.params(self.dim)
+        params = N.dbl_array(p)
+        host = self._records_host(1)
+        sz = ctypes.sizeof(N.VgStats)
+        done = torch.cuda.Event()
+        for itn in range(int(self.nitn)):
+            if self.analyzer is not None:
+                self.analyzer.begin(itn, self)
+            self._itn += 1
+            N.check(L.vg_iterate(ctypes.byref(it), self._itn & 0xffffffff, int(fcn.kind), params, len(p),
+                                 stream))
+            host[0].copy_(self._stats, non_blocking=True)
+            done.record(torch.cuda.current_stream(self.device))
+            done.synchronize()
+            st = N.VgStats.from_buffer_copy(host[0].numpy().tobytes()[:sz])
+            self._take_record(st)
+            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            result.sum_neval += self.last_neval
+            if self.analyzer is not None:
+                self.analyzer.end(result.itn_results[-1], result)
+            if save is not None:
+                _save(save, result)
+            if saveall is not None:
+                _save(saveall, (result, self))
+            if result.converged(self.rtol, self.atol):
+                break
         return result
 
     # --------------------------------------------------------------- report

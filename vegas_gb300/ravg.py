@@ -23,7 +23,7 @@ class RAvg(GVar):
     """Running average of scalar Monte Carlo estimates (pyx:2276)."""
 
     __slots__ = ('weighted', '_wlist', '_mlist', '_msum', '_varsum', '_n', 'itn_results',
-                 'sum_neval', 'rescale')
+                 'sum_neval', 'rescale', '_wbuf', '_mbuf')
 
     def __init__(self, weighted=True, itn_results=None, sum_neval=0, _rescale=True):
         super(RAvg, self).__init__(0.0, {})
@@ -31,6 +31,8 @@ class RAvg(GVar):
         self.weighted = bool(weighted)
         self._wlist = []
         self._mlist = []
+        self._wbuf = np.empty(16)   # the weights and means as arrays (same values as the lists)
+        self._mbuf = np.empty(16)
         self._msum = 0.0
         self._varsum = 0.0
         self._n = 0
@@ -59,12 +61,21 @@ class RAvg(GVar):
         """Add several estimates in order.  The weighted average after the
         last one depends only on the full lists (the reference recomputes it
         from them at every ``add``), so it is formed once, with the same
-        numpy sums; the unweighted running sums are accumulated in order."""
+        numpy sums -- over arrays holding the lists' values, which numpy sums
+        exactly as it sums the lists, at array rather than Python-loop cost
+        per iteration; the unweighted running sums are accumulated in order."""
         for g in gs:
             self.itn_results.append(g)
             self._mlist.append(g.mean)
             if self.weighted:
-                self._wlist.append(1 / (g.var if g.var > TINY else TINY))
+                k = len(self._wlist)
+                w = 1 / (g.var if g.var > TINY else TINY)
+                self._wlist.append(w)
+                if k == self._wbuf.shape[0]:
+                    self._wbuf = np.concatenate([self._wbuf, np.empty(k)])
+                    self._mbuf = np.concatenate([self._mbuf, np.empty(k)])
+                self._wbuf[k] = w
+                self._mbuf[k] = g.mean
             else:
                 self._msum += g.mean
                 self._varsum += g.var
@@ -72,9 +83,10 @@ class RAvg(GVar):
         if not self._mlist:
             return
         if self.weighted:
-            var = 1. / np.sum(self._wlist)
+            k = len(self._wlist)
+            var = 1. / np.sum(self._wbuf[:k])
             sdev = np.sqrt(var)
-            mean = np.sum([w * m for w, m in zip(self._wlist, self._mlist)]) * var
+            mean = np.sum(self._wbuf[:k] * self._mbuf[:k]) * var
         else:
             mean = self._msum / self._n
             sdev = np.sqrt(self._varsum / self._n ** 2)
