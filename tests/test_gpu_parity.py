@@ -356,3 +356,33 @@ def test_stepwise_builtin_path_matches_pipelined(tmp_path):
     C = vg.Integrator(3 * [[0, 1]], neval=20000, seed=17, precision='fp64')
     rc = C(f, nitn=6, rtol=0.5)
     assert rc.nitn == 1
+
+
+def test_speculative_rtol_path_leaves_the_state_of_the_stop():
+    """An rtol stop without other host hooks runs one iteration ahead of the
+    host and undoes it at the stop: the same iterations, results and final
+    state (map, sigf, sum_sigf, iteration counter) as the iteration-by-
+    iteration loop (here: the same call with an analyzer), and the next call
+    continues identically (FP64, parity tolerance)."""
+    f = vg.Gaussian(a=60.0, c=0.45, dim=3)
+
+    class Quiet(object):
+        def begin(self, itn, integrator):
+            pass
+
+        def end(self, itn_result, result):
+            pass
+
+    A = vg.Integrator(3 * [[0, 1]], neval=20000, seed=29, precision='fp64')
+    B = vg.Integrator(3 * [[0, 1]], neval=20000, seed=29, precision='fp64')
+    ra = A(f, nitn=40, rtol=2e-3)
+    rb = B(f, nitn=40, rtol=2e-3, analyzer=Quiet())
+    assert 1 < ra.nitn < 40 and ra.nitn == rb.nitn
+    assert rel([x.mean for x in ra.itn_results], [x.mean for x in rb.itn_results]) <= RTOL
+    assert A._itn == B._itn == ra.nitn
+    assert rel(A.sum_sigf, B.sum_sigf) <= RTOL and rel(A.sigf, B.sigf) <= 1e-10
+    ga, gb = np.nan_to_num(A.map.grid), np.nan_to_num(B.map.grid)
+    assert np.max(np.abs(ga - gb)) <= RTOL
+    B.set(analyzer=None)
+    ra2, rb2 = A(f, nitn=2), B(f, nitn=2)
+    assert rel([x.mean for x in ra2.itn_results], [x.mean for x in rb2.itn_results]) <= RTOL

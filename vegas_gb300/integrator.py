@@ -515,9 +515,10 @@ class Integrator(object):
         kind = self._classify(fcn)
         result = RAvg(weighted=self.adapt)
         if kind == 'builtin' and self.ran_array_generator is None and not self.uses_jac:
-            if (self.analyzer is None and save is None and saveall is None
-                    and self.rtol == 0 and self.atol == 0):
-                return self._call_pipelined(fcn, result)
+            if self.analyzer is None and save is None and saveall is None:
+                if self.rtol == 0 and self.atol == 0:
+                    return self._call_pipelined(fcn, result)
+                return self._call_speculative(fcn, result)
             return self._call_stepwise(fcn, result, save, saveall)
         L = N.load()
         stream = N.stream_ptr(self.device)
@@ -716,6 +717,70 @@ class Integrator(object):
             if saveall is not None:
                 _save(saveall, (result, self))
             if result.converged(self.rtol, self.atol):
+                break
+        return result
+
+    def _call_speculative(self, fcn, result):
+        """__call__ for a built-in integrand with an rtol/atol stop and no
+        other host hook: iteration k + 1 is enqueued before iteration k's
+        record is read, so the GPU never waits for the host.  After each
+        iteration the map and sigf are copied to one of two backup slots on
+        the device; when the stopping rule (pyx:2226) or an error ends the
+        loop at iteration k, the iteration already enqueued after it is
+        undone from slot k -- the integrator is left exactly as the
+        iteration-by-iteration loop leaves it, and the next call draws the
+        same random numbers."""
+        L = N.load()
+        stream = N.stream_ptr(self.device)
+        cur = torch.cuda.current_stream(self.device)
+        it, ncap = self._struct()
+        self._put_sum_sigf()
+        p = fcn.params(self.dim)
+        params = N.dbl_array(p)
+        nitn = int(self.nitn)
+        grid, inc, sigf = self.map.grid_tensor, self.map.inc_tensor, self._sigf
+        bk = [(torch.empty_like(grid), torch.empty_like(inc), torch.empty_like(sigf)) for _ in range(2)]
+        host = self._records_host(2)
+        sz = ctypes.sizeof(N.VgStats)
+        done = [torch.cuda.Event(), torch.cuda.Event()]
+        itn0 = self._itn
+
+        def enqueue(k):
+            N.check(L.vg_iterate(ctypes.byref(it), (itn0 + k + 1) & 0xffffffff, int(fcn.kind), params, len(p),
+                                 stream))
+            host[k % 2].copy_(self._stats, non_blocking=True)
+            done[k % 2].record(cur)
+            g, i, s_ = bk[k % 2]
+            g.copy_(grid, non_blocking=True)
+            i.copy_(inc, non_blocking=True)
+            s_.copy_(sigf, non_blocking=True)
+
+        def undo(k):   # back to the state after iteration k
+            g, i, s_ = bk[k % 2]
+            grid.copy_(g, non_blocking=True)
+            inc.copy_(i, non_blocking=True)
+            sigf.copy_(s_, non_blocking=True)
+            cur.synchronize()
+
+        enqueue(0)
+        for k in range(nitn):
+            ahead = k + 1 < nitn
+            if ahead:
+                enqueue(k + 1)
+            done[k % 2].synchronize()
+            st = N.VgStats.from_buffer_copy(host[k % 2].numpy().tobytes()[:sz])
+            self._itn = itn0 + k + 1
+            try:
+                self._take_record(st)
+            except Exception:
+                if ahead:
+                    undo(k)
+                raise
+            result.add(gv.gvar(st.mean, st.var ** 0.5))
+            result.sum_neval += self.last_neval
+            if result.converged(self.rtol, self.atol):
+                if ahead:
+                    undo(k)
                 break
         return result
 
