@@ -22,8 +22,16 @@
 //                       GEMMs (K = batch rows) + flow_wgrad_reduce_kernel
 //   flow_adam_kernel    Adam update of the FP32 parameters
 //   flow_mirror_kernel  BF16 copies of W2, W3 (and transposes) for the MMAs
-// The 128x128 hidden layer and the output layer run on the tensor cores as
-// BF16 mma.sync.m16n8k16 with FP32 accumulation.
+// These run the 128x128 hidden layer and the output layer as BF16
+// mma.sync.m16n8k16 with FP32 accumulation; they serve the configurations
+// the tcgen05 kernels do not fit (more than 4 transformed coordinates per
+// layer, K outside {16, 32}).  The 5th-generation tensor-core kernels:
+//   flow_pass_umma_kernel   inference / training forward through all layers
+//   flow_bwd_umma_kernel    training backward of one layer: forward
+//                           recomputation, spline backward in registers,
+//                           dH2, dH1 and dW1 with TMEM accumulators
+//   flow_wgrad_img_kernel   dW2, dW3 (and db2, db3) over the backward's
+//                           tile images + flow_wgrad_img_reduce_kernel
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
@@ -1277,6 +1285,729 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
     if (warp == 0) umma::tmem_dealloc(tmem, 512);
 }
 
+// ------------------------------------------------ tcgen05 training backward
+// Makes the compiler treat the values of o[] as redefined here (no
+// instruction is emitted), so that sums of them are recomputed in the next
+// pass instead of being kept live from the previous one: the backward's
+// passes then fit in the register budget of a 512-thread CTA.
+template <int NRV>
+__device__ __forceinline__ void regs_opaque(float (&o)[NRV])
+{
+#pragma unroll
+    for (int q = 0; q < NRV; q++) asm volatile("" : "+f"(o[q]));
+}
+
+// Spline of one coordinate in registers (compile-time K): CDF at x (density
+// direction), lp = its log pdf, and the backward of (C, log pdf) with the
+// upstream gradients gC = dL/dC and gL = dL/dlp.  On exit o[] holds
+// dL/dlogits; returns dL/dx.  The formulas are those of spline_prepare,
+// spline_cdf and spline_backward above.
+template <int K>
+__device__ __forceinline__ float spline_grad_reg(float (&o)[2 * K + 1], float x, float gC, float gL, float &lp)
+{
+    constexpr float c1 = 1.f - K * EPS_W;
+    float m4[4], v4[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        m4[q] = o[q];
+        v4[q] = o[K + q];
+    }
+#pragma unroll
+    for (int k = 4; k < K; k++) m4[k & 3] = fmaxf(m4[k & 3], o[k]);
+#pragma unroll
+    for (int k = 4; k <= K; k++) v4[k & 3] = fmaxf(v4[k & 3], o[K + k]);
+    const float mx = fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3]));
+    const float mv = fmaxf(fmaxf(v4[0], v4[1]), fmaxf(v4[2], v4[3]));
+    float s4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        o[k] = __expf(o[k] - mx);
+        s4[k & 3] += o[k];
+    }
+    const float rse = 1.f / ((s4[0] + s4[1]) + (s4[2] + s4[3]));
+#pragma unroll
+    for (int k = 0; k < K; k++) o[k] *= rse;                               // softmax s_k
+#pragma unroll
+    for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);          // vertex heights u_k
+    // bin of x with the prefix sums at it, in the CDF's sequential order
+    float E = 0.f, P = 0.f, Eb = 0.f, Pb = 0.f, Wb = 1.f, ub = 0.f, ub1 = 0.f;
+    int b = K - 1;
+    bool f = false;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float W = EPS_W + c1 * o[k];
+        const bool here = !f && (k == K - 1 || x < E + W);
+        b = here ? k : b;
+        Eb = here ? E : Eb;
+        Pb = here ? P : Pb;
+        Wb = here ? W : Wb;
+        ub = here ? o[K + k] : ub;
+        ub1 = here ? o[K + k + 1] : ub1;
+        f = f || here;
+        E += W;
+        P += 0.5f * (o[K + k] + o[K + k + 1]) * W;
+    }
+    const float Z = P;
+    regs_opaque(o);
+    float al = (x - Eb) / Wb;
+    al = fminf(fmaxf(al, 0.f), 1.f);
+    const float du = ub1 - ub;
+    const float num = Pb + Wb * (al * ub + 0.5f * al * al * du);
+    const float pdfu = (1.f - al) * ub + al * ub1;
+    lp = __logf(pdfu) - __logf(Z);
+    const float g_num = gC / Z;
+    const float g_Z = -gC * num / (Z * Z) - gL / Z;
+    const float g_pdfu = gL / pdfu;
+    const float g_al = g_pdfu * du + g_num * Wb * (ub + al * du);
+    const float g_ub = g_pdfu * (1.f - al) + g_num * Wb * (al - 0.5f * al * al);
+    const float g_ub1 = g_pdfu * al + g_num * Wb * 0.5f * al * al;
+    const float g_Wb = g_num * (al * ub + 0.5f * al * al * du) - g_al * al / Wb;
+    const float g_x = g_al / Wb;
+    const float g_E = -g_al / Wb;
+    const float hz = 0.5f * g_Z, hn = 0.5f * g_num;
+    // dot = sum_k s_k c1 dL/dW_k (the softmax Jacobian)
+    float d4[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const float us = o[K + k] + o[K + k + 1];
+        float gW = hz * us;
+        gW += k < b ? g_E + hn * us : 0.f;
+        gW += k == b ? g_Wb : 0.f;
+        d4[k & 3] += o[k] * c1 * gW;
+    }
+    const float dot = (d4[0] + d4[1]) + (d4[2] + d4[3]);
+    regs_opaque(o);
+    float Wprev = 0.f;
+#pragma unroll
+    for (int k = 0; k <= K; k++) {
+        const float Wk = k < K ? EPS_W + c1 * o[k] : 0.f;
+        float gu = hz * (Wprev + Wk);
+        gu += (k >= 1 && k <= b) ? hn * Wprev : 0.f;
+        gu += k < b ? hn * Wk : 0.f;
+        gu += k == b ? g_ub : 0.f;
+        gu += k == b + 1 ? g_ub1 : 0.f;
+        if (k < K) {
+            const float us = o[K + k] + o[K + k + 1];
+            float gW = hz * us;
+            gW += k < b ? g_E + hn * us : 0.f;
+            gW += k == b ? g_Wb : 0.f;
+            o[k] = o[k] * (c1 * gW - dot);
+        }
+        o[K + k] = gu * o[K + k];
+        Wprev = Wk;
+    }
+    return g_x;
+}
+
+// One (row, coordinate) of the backward's spline phase: logits from TMEM
+// (taddr: this warp's lanes, the coordinate's first column) plus the bias
+// bb, spline forward and backward, dL/dout as bf16 into row r, columns
+// [c0, c0 + CH) of the K-major A-operand tile sD.  Returns (dL/dx, log pdf).
+// Out of line so that its ~90 live values get the whole register budget
+// of the 512-thread kernel (inlined, they spill to local memory).
+template <int K>
+__device__ __noinline__ float2 spline_grad_row(uint32_t taddr, const float *bb, float x, float gC, float gL,
+                                               uint8_t *sD, int r, int c0)
+{
+    constexpr int NR = 2 * K + 1;
+    constexpr int CHT = (NR + 7) / 8 * 8;
+    float o[NR];
+    {
+        float v[32];
+        umma::tmem_ld32(taddr, v);
+#pragma unroll
+        for (int q = 0; q < 32; q++) o[q] = v[q];
+        if (NR > 32) {
+            umma::tmem_ld32(taddr + 32u, v);
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (32 + q < NR) o[32 + q] = v[q];
+        }
+        if (NR > 64) o[64] = umma::tmem_ld1(taddr + 64u);
+    }
+#pragma unroll
+    for (int q = 0; q < NR; q++) o[q] += bb[q];
+    float lp;
+    const float gx = spline_grad_reg<K>(o, x, gC, gL, lp);
+#pragma unroll
+    for (int c8 = 0; c8 < CHT; c8 += 8) {
+        float a[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) a[i] = (c8 + i < NR) ? o[c8 + i] : 0.f;
+        uint4 pk;
+        pk.x = pack_bf16(a[0], a[1]);
+        pk.y = pack_bf16(a[2], a[3]);
+        pk.z = pack_bf16(a[4], a[5]);
+        pk.w = pack_bf16(a[6], a[7]);
+        *reinterpret_cast<uint4 *>(sD + umma::sw128_offset(FROWS, r, c0 + c8)) = pk;
+    }
+    return make_float2(gx, lp);
+}
+
+constexpr int BNT = 512;                 // threads of the tcgen05 backward: 16 warps
+constexpr uint32_t BLK = FROWS * 128;    // bytes of one 64-column block of a 128-row tile (16 KB)
+constexpr uint32_t TW1_COL = 448;        // TMEM columns [448, 480): dW1 | db1 accumulator
+
+// Shared-memory plan of the tcgen05 backward (offsets from the 1024-aligned
+// dynamic base).  RA holds, in turn: H1 | H2 (A operands of the forward
+// recomputation), dL/dout (A operand of dH2, NB3 blocks), dH2' | dH1'.
+struct BwdPlan {
+    int NB3;                             // 64-column blocks of the dL/dout tile (widest layer)
+    size_t oW2, oW3, oRA, oBz, oW1, ob1, ob2, ob3, oZ, oG, oLW, oRED, total;
+};
+
+__host__ __device__ inline BwdPlan bwd_plan(const FlowGeom &g)
+{
+    BwdPlan p;
+    p.NB3 = (g.NPmax + 63) / 64;
+    const int zst = g.dim | 1;
+    size_t o = 0;
+    p.oW2 = o; o += (size_t)FH * FH * 2;
+    p.oW3 = o; o += ((size_t)g.NPmax * FH * 2 + 1023) / 1024 * 1024;
+    p.oRA = o;
+    {
+        const size_t a = (size_t)4 * BLK, d = (size_t)p.NB3 * BLK;
+        o += a > d ? a : d;
+    }
+    p.oBz = o; o += (size_t)32 * FROWS * 2;    // [z_A hi (8) | z_A lo (8) | 1 | 0...] x 128 rows, K-major
+    p.oW1 = o; o += sizeof(float) * FH * 8;
+    p.ob1 = o; o += sizeof(float) * FH;
+    p.ob2 = o; o += sizeof(float) * FH;
+    p.ob3 = o; o += sizeof(float) * 4 * (2 * g.K + 1);
+    p.oZ = o;  o += sizeof(float) * FROWS * zst;
+    p.oG = o;  o += sizeof(float) * FROWS * zst;
+    p.oLW = o; o += sizeof(float) * FROWS;
+    p.oRED = o; o += sizeof(float) * 3 * FROWS * 8;
+    p.total = o + 1024;
+    return p;
+}
+
+// Training backward of layer l on the 5th-generation tensor cores (layers
+// with at most 4 transformed and 8 conditioning coordinates).  One CTA (16
+// warps) per SM, persistent over 128-row tiles; the layer's W2 and W3
+// operand images are fetched once per CTA.  Per tile:
+//   H1 = relu(W1 z_A + b1)                    FP32 FMA -> bf16 A operand
+//   TMEM[0,128)   = H1 W2^T                   tcgen05, K-major A and B
+//   H2 = relu(. + b2)                         epilogue -> bf16 A operand
+//   TMEM[128,..)  = H2 W3^T                   the <= 4 coordinates' logits
+//   spline forward + backward                 registers, thread = (row,
+//                                             coordinate); dL/dout -> bf16
+//   TMEM[0,128)   = dL/dout W3                B = the W3 image read MN-major
+//   dH2' = . relu'(H2)                        epilogue -> bf16 A operand
+//   TMEM[128,256) = dH2' W2                   B = the W2 image read MN-major
+//   dH1' = . relu'(H1)                        epilogue -> bf16; dL/dz_A
+//   TMEM[448,480) += dH1'^T [z_A hi|lo|1]     dW1, db1 over the CTA's tiles
+// The bf16 tiles H1, H2, dL/dout and dH2' go out by bulk copy as images
+// (byte-identical to the shared-memory tiles) for flow_wgrad_img_kernel.
+// The relu masks of H1 and H2 stay in registers (thread = row, 32 columns).
+// Every wait is bounded; one that gives up sets g_flow_status.
+template <int K>
+__global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
+    FlowGeom g, int l, const float *__restrict__ theta, const __nv_bfloat16 *__restrict__ mirror, int64_t n,
+    int64_t ntiles, const float *__restrict__ zl, const float *__restrict__ gout, const float *__restrict__ w,
+    float *__restrict__ gin, uint8_t *__restrict__ imgH1, uint8_t *__restrict__ imgH2, uint8_t *__restrict__ imgD,
+    uint8_t *__restrict__ imgG2, float *__restrict__ grad, double *__restrict__ loss)
+{
+    constexpr int NR = 2 * K + 1;
+    constexpr int CHT = (NR + 7) / 8 * 8;   // output rows per coordinate in the images (g.CH)
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t bars[2];            // 0 weights, 1 MMA completion
+    __shared__ uint32_t tslot;
+    __shared__ int abort_flag;
+    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    const BwdPlan pl = bwd_plan(g);
+    const FlowLayer &y = g.ly[l];
+    uint8_t *sW2 = base + pl.oW2, *sW3 = base + pl.oW3, *sRA = base + pl.oRA, *sBz = base + pl.oBz;
+    uint8_t *sH1 = sRA, *sH2 = sRA + 2 * BLK, *sD = sRA, *sG2 = sRA, *sG1 = sRA + 2 * BLK;
+    float *sW1 = (float *)(base + pl.oW1), *sb1 = (float *)(base + pl.ob1);
+    float *sb2 = (float *)(base + pl.ob2), *sb3 = (float *)(base + pl.ob3);
+    float *sZ = (float *)(base + pl.oZ), *sG = (float *)(base + pl.oG);
+    float *sLW = (float *)(base + pl.oLW), *sRED = (float *)(base + pl.oRED);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & (FROWS - 1), h = tid >> 7;
+    const int dim = g.dim, zst = dim | 1;
+    const int dA = y.realA ? y.dA : 1, dB = y.dB, NPl = y.NP;
+    const int nb3l = (NPl + 63) / 64;
+    const uint32_t bar_w = umma::smem_u32(&bars[0]), bar_m = umma::smem_u32(&bars[1]);
+    if (warp == 0) umma::tmem_alloc(umma::smem_u32(&tslot), 512);
+    if (tid == 0) {
+        umma::mbar_init(bar_w, 1);
+        umma::mbar_init(bar_m, 1);
+        abort_flag = 0;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tslot;
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+    uint32_t ph_m = 0;
+    // the layer's weights, once per CTA
+    if (tid == 0) {
+        const uint32_t b2 = (uint32_t)FH * FH * 2, b3 = (uint32_t)NPl * FH * 2;
+        umma::mbar_expect_tx(bar_w, b2 + b3);
+        umma::bulk_g2s(umma::smem_u32(sW2), mirror + y.mU2, b2, bar_w);
+        for (uint32_t off = 0; off < b3; off += 32768u) {
+            const uint32_t sz = (b3 - off) < 32768u ? (b3 - off) : 32768u;
+            umma::bulk_g2s(umma::smem_u32(sW3) + off, (const uint8_t *)(mirror + y.mU3) + off, sz, bar_w);
+        }
+    }
+    for (int i = tid; i < FH * 8; i += BNT) {
+        const int c = i >> 3, a = i & 7;
+        sW1[i] = a < dA ? theta[y.oW1 + c * dA + a] : 0.f;
+    }
+    for (int i = tid; i < FH; i += BNT) {
+        sb1[i] = theta[y.ob1 + i];
+        sb2[i] = theta[y.ob2 + i];
+    }
+    for (int i = tid; i < dB * NR; i += BNT) sb3[i] = theta[y.ob3 + i];
+    if (tid == 0 && !umma::mbar_wait(bar_w, 0)) abort_flag = 1;
+    __syncthreads();
+    int ndone = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x) {
+        const int64_t r0 = tile * FROWS;
+        for (int i = tid; i < FROWS * dim; i += BNT) {
+            const int rr = i / dim, d = i % dim;
+            const bool ok = r0 + rr < n;
+            sZ[rr * zst + d] = ok ? zl[((int64_t)l * n + r0 + rr) * dim + d] : 0.5f;
+            sG[rr * zst + d] = ok ? gout[(r0 + rr) * dim + d] : 0.f;
+        }
+        if (tid < FROWS) sLW[tid] = (r0 + tid < n) ? -w[r0 + tid] : 0.f;   // dL/dlogpdf
+        __syncthreads();
+        // ---- H1 (FP32) -> A operand, its relu mask; the [z_A hi | lo | 1] operand
+        uint32_t m1 = 0, m2 = 0;
+        {
+            float xa[8];
+#pragma unroll
+            for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? sZ[r * zst + y.A[a]] : 0.f;
+            const bool wide = dA > 4;
+#pragma unroll 2
+            for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
+                float v[8];
+                const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
+                const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
+                v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
+                v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
+                    float acc = v[q];
+                    acc = fmaf(w0.x, xa[0], acc);
+                    acc = fmaf(w0.y, xa[1], acc);
+                    acc = fmaf(w0.z, xa[2], acc);
+                    acc = fmaf(w0.w, xa[3], acc);
+                    if (wide) {
+                        const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
+                        acc = fmaf(w1.x, xa[4], acc);
+                        acc = fmaf(w1.y, xa[5], acc);
+                        acc = fmaf(w1.z, xa[6], acc);
+                        acc = fmaf(w1.w, xa[7], acc);
+                    }
+                    m1 |= (acc > 0.f ? 1u : 0u) << (c0 - UCOL * h + q);
+                    v[q] = fmaxf(acc, 0.f);
+                }
+                uint4 pk;
+                pk.x = pack_bf16(v[0], v[1]);
+                pk.y = pack_bf16(v[2], v[3]);
+                pk.z = pack_bf16(v[4], v[5]);
+                pk.w = pack_bf16(v[6], v[7]);
+                *reinterpret_cast<uint4 *>(sH1 + umma::sw128_offset(FROWS, r, c0)) = pk;
+            }
+            // rows 8h..8h+7 of the 32 x 128 operand: z_A hi (h = 0), z_A lo (h = 1), ones (row 16), zeros
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const __nv_bfloat16 hi = __float2bfloat16(xa[q]);
+                const __nv_bfloat16 lo = __float2bfloat16(xa[q] - __bfloat162float(hi));
+                const __nv_bfloat16 v = h == 0 ? hi : h == 1 ? lo : __float2bfloat16((h == 2 && q == 0) ? 1.f : 0.f);
+                *reinterpret_cast<__nv_bfloat16 *>(sBz + umma::sw128_offset(32, 8 * h + q, r)) = v;
+            }
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {   // TMEM[0,128) = H1 W2^T; the H1 image out
+            umma::fence_after_sync();
+            umma::gemm_128xN(tmem, umma::smem_u32(sH1), umma::smem_u32(sW2), FH, FH, FH, 0);
+            umma::mma_commit(bar_m);
+            umma::bulk_s2g(imgH1 + tile * 2 * BLK, umma::smem_u32(sH1), BLK);
+            umma::bulk_s2g(imgH1 + tile * 2 * BLK + BLK, umma::smem_u32(sH1) + BLK, BLK);
+            umma::bulk_commit();
+            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+        }
+        ph_m ^= 1;
+        __syncthreads();
+        umma::fence_after_sync();
+        if (abort_flag) break;
+        // ---- H2 = relu(TMEM + b2) -> A operand, its relu mask
+        {
+            const int c0 = UCOL * h;
+            float v[32];
+            umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int q8 = 0; q8 < 32; q8 += 8) {
+                float a[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    a[i] = v[q8 + i] + sb2[c0 + q8 + i];
+                    m2 |= (a[i] > 0.f ? 1u : 0u) << (q8 + i);
+                    a[i] = fmaxf(a[i], 0.f);
+                }
+                uint4 pk;
+                pk.x = pack_bf16(a[0], a[1]);
+                pk.y = pack_bf16(a[2], a[3]);
+                pk.z = pack_bf16(a[4], a[5]);
+                pk.w = pack_bf16(a[6], a[7]);
+                *reinterpret_cast<uint4 *>(sH2 + umma::sw128_offset(FROWS, r, c0 + q8)) = pk;
+            }
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {   // logits of the transformed coordinates (pairs); the H2 image out
+            umma::fence_after_sync();
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+                const int first = 2 * p;
+                if (first >= dB) break;
+                const int N = (first + 1 < dB) ? 2 * CHT : (CHT + 15) / 16 * 16;
+                umma::gemm_128xN(tmem + (uint32_t)(FH + first * CHT), umma::smem_u32(sH2),
+                                 umma::smem_u32(sW3) + (uint32_t)(first * CHT) * 128u, N, FH, NPl, 0);
+            }
+            umma::mma_commit(bar_m);
+            umma::bulk_s2g(imgH2 + tile * 2 * BLK, umma::smem_u32(sH2), BLK);
+            umma::bulk_s2g(imgH2 + tile * 2 * BLK + BLK, umma::smem_u32(sH2) + BLK, BLK);
+            umma::bulk_commit();
+            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+            umma::bulk_wait_read();   // H1 and H2 images read out: RA may be overwritten
+        }
+        ph_m ^= 1;
+        __syncthreads();
+        umma::fence_after_sync();
+        if (abort_flag) break;
+        // ---- spline forward + backward of (row r, coordinate h); dL/dout -> A operand
+        {
+            float lterm = 0.f;
+            if (h < dB) {
+                const int cz = y.B[h];
+                const float gL = sLW[r];
+                const float2 gl = spline_grad_row<K>(tmem + lane_base + (uint32_t)(FH + h * CHT), sb3 + h * NR,
+                                                     sZ[r * zst + cz], sG[r * zst + cz], gL, sD, r, h * CHT);
+                sG[r * zst + cz] = gl.x;   // dL/d(layer input) of a transformed coordinate
+                lterm = (r0 + r < n) ? gL * gl.y : 0.f;
+            } else if (h == 3) {   // dB <= 3: zero the padding columns [dB CH, NP) of the tile
+                for (int c8 = dB * CHT; c8 < NPl; c8 += 8)
+                    *reinterpret_cast<uint4 *>(sD + umma::sw128_offset(FROWS, r, c8)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) lterm += __shfl_xor_sync(0xffffffffu, lterm, off);
+            if ((tid & 31) == 0 && lterm != 0.f) atomicAdd(loss, (double)lterm);
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {   // TMEM[0,128) = dL/dout W3; the dL/dout image out
+            umma::fence_after_sync();
+            umma::gemm_128xN_ex(tmem, umma::smem_u32(sD), 0, FROWS, umma::smem_u32(sW3), 1, 0, FH, NPl, 0);
+            umma::mma_commit(bar_m);
+            for (int q = 0; q < nb3l; q++)
+                umma::bulk_s2g(imgD + (tile * pl.NB3 + q) * (int64_t)BLK, umma::smem_u32(sD) + (uint32_t)q * BLK, BLK);
+            umma::bulk_commit();
+            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+            umma::bulk_wait_read();
+        }
+        ph_m ^= 1;
+        __syncthreads();
+        umma::fence_after_sync();
+        if (abort_flag) break;
+        // ---- dH2' = dH2 relu'(H2) -> A operand
+        {
+            const int c0 = UCOL * h;
+            float v[32];
+            umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+#pragma unroll
+            for (int q8 = 0; q8 < 32; q8 += 8) {
+                float a[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) a[i] = ((m2 >> (q8 + i)) & 1u) ? v[q8 + i] : 0.f;
+                uint4 pk;
+                pk.x = pack_bf16(a[0], a[1]);
+                pk.y = pack_bf16(a[2], a[3]);
+                pk.z = pack_bf16(a[4], a[5]);
+                pk.w = pack_bf16(a[6], a[7]);
+                *reinterpret_cast<uint4 *>(sG2 + umma::sw128_offset(FROWS, r, c0 + q8)) = pk;
+            }
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        if (tid == 0) {   // TMEM[128,256) = dH2' W2; the dH2' image out
+            umma::fence_after_sync();
+            umma::gemm_128xN_ex(tmem + FH, umma::smem_u32(sG2), 0, FROWS, umma::smem_u32(sW2), 1, 0, FH, FH, 0);
+            umma::mma_commit(bar_m);
+            umma::bulk_s2g(imgG2 + tile * 2 * BLK, umma::smem_u32(sG2), BLK);
+            umma::bulk_s2g(imgG2 + tile * 2 * BLK + BLK, umma::smem_u32(sG2) + BLK, BLK);
+            umma::bulk_commit();
+            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+        }
+        ph_m ^= 1;
+        __syncthreads();
+        umma::fence_after_sync();
+        if (abort_flag) break;
+        // ---- dH1' = dH1 relu'(H1) (bf16) -> operand of dW1; dL/dz_A over this thread's 32 units
+        float part[8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) part[a] = 0.f;
+        {
+            const int c0 = UCOL * h;
+            float v[32];
+            umma::tmem_ld32(tmem + lane_base + (uint32_t)(FH + c0), v);
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                v[q] = ((m1 >> q) & 1u) ? __bfloat162float(__float2bfloat16(v[q])) : 0.f;
+#pragma unroll
+            for (int q8 = 0; q8 < 32; q8 += 8) {
+                uint4 pk;
+                pk.x = pack_bf16(v[q8 + 0], v[q8 + 1]);
+                pk.y = pack_bf16(v[q8 + 2], v[q8 + 3]);
+                pk.z = pack_bf16(v[q8 + 4], v[q8 + 5]);
+                pk.w = pack_bf16(v[q8 + 6], v[q8 + 7]);
+                *reinterpret_cast<uint4 *>(sG1 + umma::sw128_offset(FROWS, r, c0 + q8)) = pk;
+            }
+            if (y.realA) {
+#pragma unroll 4
+                for (int q = 0; q < 32; q++) {
+                    const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
+                    const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
+                    part[0] = fmaf(v[q], w0.x, part[0]);
+                    part[1] = fmaf(v[q], w0.y, part[1]);
+                    part[2] = fmaf(v[q], w0.z, part[2]);
+                    part[3] = fmaf(v[q], w0.w, part[3]);
+                    part[4] = fmaf(v[q], w1.x, part[4]);
+                    part[5] = fmaf(v[q], w1.y, part[5]);
+                    part[6] = fmaf(v[q], w1.z, part[6]);
+                    part[7] = fmaf(v[q], w1.w, part[7]);
+                }
+            }
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        if (h > 0) {
+            float4 *dst = reinterpret_cast<float4 *>(sRED + ((size_t)(h - 1) * FROWS + r) * 8);
+            dst[0] = make_float4(part[0], part[1], part[2], part[3]);
+            dst[1] = make_float4(part[4], part[5], part[6], part[7]);
+        }
+        __syncthreads();
+        if (tid == 0) {   // TMEM[448,480) += dH1'^T [z_A hi | lo | 1] (A read MN-major)
+            umma::fence_after_sync();
+            umma::gemm_128xN_ex(tmem + TW1_COL, umma::smem_u32(sG1), 1, 0, umma::smem_u32(sBz), 0, 32, 32, FROWS,
+                                ndone > 0 ? 1u : 0u);
+            umma::mma_commit(bar_m);
+        }
+        if (h == 0 && y.realA) {   // dL/dz_A: the four column groups added in order
+            for (int a = 0; a < dA; a++)
+                sG[r * zst + y.A[a]] += ((part[a] + sRED[(0 * FROWS + r) * 8 + a]) + sRED[(1 * FROWS + r) * 8 + a]) +
+                                        sRED[(2 * FROWS + r) * 8 + a];
+        }
+        __syncthreads();
+        for (int i = tid; i < FROWS * dim; i += BNT) {
+            const int rr = i / dim, d = i % dim;
+            if (r0 + rr < n) gin[(r0 + rr) * dim + d] = sG[rr * zst + d];
+        }
+        if (tid == 0) {   // dW1 MMA done (its operands are rewritten by the next tile), dH2' image read out
+            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+            umma::bulk_wait_read();
+        }
+        ph_m ^= 1;
+        ndone++;
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+    }
+    // drain every MMA and bulk copy, then flush the dW1 | db1 accumulator
+    if (tid == 0) {
+        umma::mma_commit(bar_m);
+        if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+        umma::bulk_wait_all();
+        if (abort_flag) atomicExch(&g_flow_status, VG_ERR_TIMEOUT);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (!abort_flag && ndone > 0 && h == 0) {
+        float v[32];
+        umma::tmem_ld32(tmem + lane_base + TW1_COL, v);
+        const int c = r;   // TMEM lane = hidden unit
+        if (y.realA) {
+#pragma unroll
+            for (int a = 0; a < 8; a++)
+                if (a < dA) atomicAdd(&grad[y.oW1 + (int64_t)c * dA + a], v[a] + v[8 + a]);
+        }
+        atomicAdd(&grad[y.ob1 + c], v[16]);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (warp == 0) umma::tmem_dealloc(tmem, 512);
+}
+
+constexpr int WGI_NT = 128;   // threads of the image weight-gradient kernel
+// floats between two splits' partials: 128 x Mtot plus 64, so that the
+// reduction's loads of one element's splits are not a power of two apart
+#define WGI_SPLIT_STRIDE(Mtot) ((int64_t)FH * (Mtot) + 64)
+
+// Weight gradients from the backward's tile images.  blockIdx.y = job: 0 is
+// dW2 = dH2'^T H1, c >= 1 rows [128(c-1), 128c) of the W3 image of
+// dW3 = dL/dout^T H2; blockIdx.x = split over the 128-row tiles.  A K-major
+// image of a 128-row tile is the MN-major tile of its transpose with K =
+// 128 rows, so both operands are read as they are: two stages by bulk copy,
+// thread 0 issues the MMAs (D in TMEM[0,128)) and the row sums against a
+// ones operand (the bias gradients, TMEM[128,144)).  part[split][col][Mtot],
+// partb[split][Mtot] (column-major, so that the epilogue's stores coalesce;
+// splits WGI_SPLIT_STRIDE floats apart).
+__global__ void __launch_bounds__(WGI_NT) flow_wgrad_img_kernel(
+    const uint8_t *__restrict__ imgH1, const uint8_t *__restrict__ imgH2, const uint8_t *__restrict__ imgD,
+    const uint8_t *__restrict__ imgG2, int NB3, int nb3l, int64_t ntiles, int tps, int Mtot,
+    float *__restrict__ part, float *__restrict__ partb)
+{
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t bars[5];   // full 0/1, empty 0/1, drain
+    __shared__ uint32_t slot;
+    __shared__ int s_ok;
+    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *sOnes = base;                    // 16 x 128 K-major ones (4 KB)
+    uint8_t *stg = base + 4096;               // 2 stages x (A 2 blocks + B 2 blocks)
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int job = blockIdx.y;
+    const int64_t t0 = (int64_t)blockIdx.x * tps;
+    const int64_t t1 = t0 + tps < ntiles ? t0 + tps : ntiles;
+    const int nst = t1 > t0 ? (int)(t1 - t0) : 0;
+    const int ablk0 = job == 0 ? 0 : 2 * (job - 1);
+    const int anb = job == 0 ? 2 : (nb3l - ablk0 < 2 ? nb3l - ablk0 : 2);
+    const uint8_t *Asrc = job == 0 ? imgG2 : imgD;
+    const int64_t astride = job == 0 ? 2 * (int64_t)BLK : (int64_t)NB3 * BLK;
+    const uint8_t *Bsrc = job == 0 ? imgH1 : imgH2;
+    for (int i = tid; i < 16 * FROWS; i += WGI_NT)
+        *reinterpret_cast<__nv_bfloat16 *>(sOnes + umma::sw128_offset(16, i >> 7, i & 127)) = __float2bfloat16(1.f);
+    umma::fence_async_smem();
+    if (warp == 0) umma::tmem_alloc(umma::smem_u32(&slot), 256);
+    if (tid == 0) {
+        for (int i = 0; i < 5; i++) umma::mbar_init(umma::smem_u32(&bars[i]), 1);
+        s_ok = 1;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = slot;
+    if (tid == 0 && anb > 0) {
+        uint32_t pf[2] = {0u, 0u}, pe[2] = {0u, 0u};
+        int issued = 0, used = 0;
+        bool ok = true;
+        auto issue = [&](int st) {
+            const int b = st & 1;
+            uint8_t *sA = stg + (uint32_t)b * 4u * BLK, *sB = sA + 2 * BLK;
+            const int64_t t = t0 + st;
+            const uint32_t fb = umma::smem_u32(&bars[b]);
+            umma::mbar_expect_tx(fb, (uint32_t)(anb + 2) * BLK);
+            umma::bulk_g2s(umma::smem_u32(sA), Asrc + t * astride + (int64_t)ablk0 * BLK, (uint32_t)anb * BLK, fb);
+            umma::bulk_g2s(umma::smem_u32(sB), Bsrc + t * 2 * (int64_t)BLK, 2 * BLK, fb);
+            issued++;
+        };
+        if (nst > 0) issue(0);
+        if (nst > 1) issue(1);
+        for (int st = 0; st < nst; st++) {
+            const int b = st & 1;
+            if (!umma::mbar_wait(umma::smem_u32(&bars[b]), pf[b])) { ok = false; break; }
+            pf[b] ^= 1u;
+            used++;
+            const uint32_t sA = umma::smem_u32(stg + (uint32_t)b * 4u * BLK), sB = sA + 2 * BLK;
+            umma::gemm_128xN_ex(tmem, sA, 1, 0, sB, 1, 0, FH, FROWS, st > 0 ? 1u : 0u);
+            umma::gemm_128xN_ex(tmem + FH, sA, 1, 0, umma::smem_u32(sOnes), 0, 16, 16, FROWS, st > 0 ? 1u : 0u);
+            umma::mma_commit(umma::smem_u32(&bars[2 + b]));
+            if (st + 2 < nst) {
+                if (!umma::mbar_wait(umma::smem_u32(&bars[2 + b]), pe[b])) { ok = false; break; }
+                pe[b] ^= 1u;
+                issue(st + 2);
+            }
+        }
+        // loads still in flight (after a wait gave up) land before the CTA exits
+        for (int s = used; s < issued; s++) {
+            const int b = s & 1;
+            if (!umma::mbar_wait(umma::smem_u32(&bars[b]), pf[b])) ok = false;
+            pf[b] ^= 1u;
+        }
+        umma::mma_commit(umma::smem_u32(&bars[4]));
+        if (!umma::mbar_wait(umma::smem_u32(&bars[4]), 0)) ok = false;
+        if (!ok) s_ok = 0;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const bool ok = s_ok != 0 && nst > 0 && anb > 0;
+    if (s_ok == 0 && tid == 0) atomicExch(&g_flow_status, VG_ERR_TIMEOUT);
+    const int m = 32 * warp + (tid & 31);
+    const int mrow = job * FH + m;
+    float *P = part + (int64_t)blockIdx.x * WGI_SPLIT_STRIDE(Mtot);
+    for (int c = 0; c < FH; c += 32) {
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+        for (int i = 0; i < 32; i++) P[(int64_t)(c + i) * Mtot + mrow] = ok ? v[i] : 0.f;
+    }
+    {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)FH, v);
+        partb[(int64_t)blockIdx.x * Mtot + mrow] = ok ? v[0] : 0.f;
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
+// grad += the splits' sums: rows m < 128 of part are dW2 (db2), rows 128 + q
+// the W3 image row q = j CH + o (dW3 row j NR + o, db3); image padding rows
+// are skipped.  Four lanes per element, lane p adding splits p, p + 4, ...
+// in order, the four partial sums combined in a fixed tree (deterministic).
+__global__ void flow_wgrad_img_reduce_kernel(const float *__restrict__ part, const float *__restrict__ partb,
+                                             int nsplit, int Mtot, int Mrows, int64_t oW2, int64_t ob2,
+                                             int64_t oW3, int64_t ob3, int dB, int CH, int NR,
+                                             float *__restrict__ grad)
+{
+    const int64_t nw = (int64_t)FH * Mrows, ne = nw + Mrows;
+    const int sub = threadIdx.x & 3;
+    const int64_t e0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int64_t estride = ((int64_t)gridDim.x * blockDim.x) >> 2;
+    for (int64_t e = e0; (e & ~7LL) < ne; e += estride) {   // a warp's 8 elements (a multiple-of-8 base) move together
+        const bool live = e < ne;
+        const bool bias = e >= nw;
+        const int m = live ? (bias ? (int)(e - nw) : (int)(e % Mrows)) : 0;
+        const int c = (live && !bias) ? (int)(e / Mrows) : 0;
+        const float *src = bias ? partb + m : part + (int64_t)c * Mtot + m;
+        const int64_t step = bias ? (int64_t)Mtot : WGI_SPLIT_STRIDE(Mtot);
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int sp = sub + 4 * q;
+            v[q] = (live && sp < nsplit) ? src[(int64_t)sp * step] : 0.f;
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < 16; q++) s += v[q];
+        for (int sp = sub + 64; live && sp < nsplit; sp += 4) s += src[(int64_t)sp * step];
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (!live || sub != 0) continue;
+        int64_t dst;
+        if (m < FH) {
+            dst = bias ? ob2 + m : oW2 + (int64_t)m * FH + c;
+        } else {
+            const int q = m - FH, j = q / CH, o = q % CH;
+            if (j >= dB || o >= NR) continue;
+            dst = bias ? ob3 + (int64_t)j * NR + o : oW3 + ((int64_t)j * NR + o) * FH + c;
+        }
+        grad[dst] += s;
+    }
+}
+
 // ------------------------------------------------------- training batch
 // Draw m of the iteration's n samples (Philox: counter (i, step, 0, 0x7f00),
 // key = seed; index = high 32 bits of word x times n), gather their z and
@@ -1328,6 +2059,58 @@ int set_smem(const void *kern, size_t bytes)
     return VG_OK;
 }
 
+// Images and split-K partials of the tcgen05 backward for n rows: 128-row
+// tiles, dL/dout blocks per tile, 128-row chunks of the W3 image, the
+// weight-gradient grid (about one CTA per SM over all jobs).
+struct BwdSizes {
+    int64_t ntiles;
+    int NB3, NC3, Mtot, nsplit, tps;
+};
+
+BwdSizes bwd_sizes(const FlowGeom &g, int64_t n)
+{
+    BwdSizes s;
+    s.ntiles = (n + FROWS - 1) / FROWS;
+    s.NB3 = (g.NPmax + 63) / 64;
+    s.NC3 = (g.NPmax + 127) / 128;
+    s.Mtot = FH * (1 + s.NC3);
+    int64_t target = vg_num_sms() / (1 + s.NC3);
+    if (target < 1) target = 1;
+    s.tps = (int)((s.ntiles + target - 1) / target);
+    if (s.tps < 1) s.tps = 1;
+    s.nsplit = (int)((s.ntiles + s.tps - 1) / s.tps);
+    return s;
+}
+
+// Workspace carve of the tcgen05 backward (the same order in both uses).
+struct BwdWork {
+    float *zl, *ga, *gb, *part, *partb, *ld, *zh;
+    uint8_t *imgH1, *imgH2, *imgG2, *imgD;
+    int64_t bytes;
+};
+
+BwdWork bwd_work(const FlowGeom &g, int64_t n, void *work)
+{
+    const BwdSizes s = bwd_sizes(g, n);
+    BwdWork b;
+    char *p = (char *)work;
+    int64_t o = 0;
+    auto take = [&](int64_t bytes) { char *q = p + o; o += (bytes + 255) & ~255LL; return q; };
+    b.zl = (float *)take((int64_t)g.L * n * g.dim * 4);
+    b.ga = (float *)take(n * g.dim * 4);
+    b.gb = (float *)take(n * g.dim * 4);
+    b.imgH1 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
+    b.imgH2 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
+    b.imgG2 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
+    b.imgD = (uint8_t *)take(s.ntiles * s.NB3 * (int64_t)BLK);
+    b.part = (float *)take((int64_t)s.nsplit * WGI_SPLIT_STRIDE(s.Mtot) * 4);
+    b.partb = (float *)take((int64_t)s.nsplit * s.Mtot * 4);
+    b.ld = (float *)take(n * 4);
+    b.zh = (float *)take(n * g.dim * 4);
+    b.bytes = o;
+    return b;
+}
+
 }  // namespace
 
 // ====================================================================== ABI
@@ -1359,7 +2142,8 @@ extern "C" int64_t vg_flow_train_bytes(const vg_flow *fl, int64_t nrows)
     b += (int64_t)maxP * ldn * 2;                 // dout^T
     b += WG_SPLIT * (int64_t)(maxP > FH ? maxP : FH) * FH * 4;   // split-K partials (dW3, dW2)
     b += nrows * 4 + nrows * g.dim * 4;           // logdet + zhat scratch
-    return b + 4096;
+    const int64_t bu = bwd_work(g, nrows, nullptr).bytes;   // the tcgen05 backward's carve
+    return (bu > b ? bu : b) + 4096;
 }
 
 extern "C" int vg_flow_refresh(const vg_flow *fl, void *stream)
@@ -1454,6 +2238,64 @@ static int flow_pass(const vg_flow *fl, int dir, int64_t n, const float *zin, fl
     return VG_OK;
 }
 
+// Gradient through the tcgen05 backward when the configuration fits it (K in
+// {16, 32}, at most 4 transformed and 8 conditioning coordinates per layer,
+// shared memory): the training forward, then per layer (last first) the
+// backward, the weight-gradient GEMMs over its images and their reduction.
+// *used = 0 when the caller should use the mma.sync backward.
+static int flow_grad_umma(const FlowGeom &g, const vg_flow *fl, int64_t n, const float *z, const float *w,
+                          void *work, size_t work_bytes, cudaStream_t st, int *used)
+{
+    *used = 0;
+    if (g_flow_force_legacy || (g.K != 32 && g.K != 16) || g.dBmax > 4 || g.dAmax > 8) return VG_OK;
+    const void *kb = g.K == 32 ? (const void *)flow_bwd_umma_kernel<32> : (const void *)flow_bwd_umma_kernel<16>;
+    size_t stat = 0;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kb) == cudaSuccess) stat = fa.sharedSizeBytes;
+    else (void)cudaGetLastError();
+    const BwdPlan pl = bwd_plan(g);
+    if (pl.total + stat > VG_FLOW_SMEM_MAX) return VG_OK;
+    const size_t wsm = 4096 + 8 * (size_t)BLK + 1024;
+    if (cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)flow_wgrad_img_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)wsm) != cudaSuccess) {
+        (void)cudaGetLastError();   // not enough shared memory on this part: the mma.sync backward instead
+        return VG_OK;
+    }
+    *used = 1;
+    const BwdSizes s = bwd_sizes(g, n);
+    const BwdWork b = bwd_work(g, n, work);
+    if ((int64_t)work_bytes < b.bytes) return vg_fail(VG_ERR_VALUE, "flow workspace too small");
+    int rc;
+    if ((rc = flow_pass(fl, 0, n, z, b.zh, b.ld, b.zl, st))) return rc;
+    VG_CUDA_CHECK(cudaMemsetAsync(b.ga, 0, n * g.dim * 4, st));
+    const int64_t grid = s.ntiles < vg_num_sms() ? s.ntiles : vg_num_sms();
+    float *gcur = b.ga, *gnext = b.gb;
+    for (int l = g.L - 1; l >= 0; l--) {
+        const FlowLayer &y = g.ly[l];
+        if (g.K == 32)
+            flow_bwd_umma_kernel<32><<<(unsigned)grid, BNT, pl.total, st>>>(
+                g, l, fl->theta, (const __nv_bfloat16 *)fl->mirror, n, s.ntiles, b.zl, gcur, w, gnext, b.imgH1,
+                b.imgH2, b.imgD, b.imgG2, fl->grad, fl->loss);
+        else
+            flow_bwd_umma_kernel<16><<<(unsigned)grid, BNT, pl.total, st>>>(
+                g, l, fl->theta, (const __nv_bfloat16 *)fl->mirror, n, s.ntiles, b.zl, gcur, w, gnext, b.imgH1,
+                b.imgH2, b.imgD, b.imgG2, fl->grad, fl->loss);
+        VG_LAUNCH_CHECK();
+        const int nb3l = (y.NP + 63) / 64, nc3l = (y.NP + 127) / 128;
+        flow_wgrad_img_kernel<<<dim3((unsigned)s.nsplit, (unsigned)(1 + nc3l)), WGI_NT, wsm, st>>>(
+            b.imgH1, b.imgH2, b.imgD, b.imgG2, s.NB3, nb3l, s.ntiles, s.tps, s.Mtot, b.part, b.partb);
+        VG_LAUNCH_CHECK();
+        flow_wgrad_img_reduce_kernel<<<1024, 256, 0, st>>>(b.part, b.partb, s.nsplit, s.Mtot, FH * (1 + nc3l), y.oW2,
+                                                          y.ob2, y.oW3, y.ob3, y.dB, g.CH, 2 * g.K + 1, fl->grad);
+        VG_LAUNCH_CHECK();
+        float *tmp = gcur;
+        gcur = gnext;
+        gnext = tmp;
+    }
+    return VG_OK;
+}
+
 extern "C" int vg_flow_sample(const vg_flow *fl, int64_t n, const float *zhat, float *z,
                               float *logdet, void *stream)
 {
@@ -1482,6 +2324,9 @@ extern "C" int vg_flow_grad(const vg_flow *fl, int64_t n, const float *z, const 
     const int64_t need = vg_flow_train_bytes(fl, n);
     if ((int64_t)work_bytes < need) return vg_fail(VG_ERR_VALUE, "flow workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
+    int used = 0;
+    rc = flow_grad_umma(g, fl, n, z, w, work, work_bytes, st, &used);
+    if (used) return rc;
     const int64_t ldn = (n + FROWS - 1) / FROWS * FROWS;
     int maxP = 0;
     for (int l = 0; l < g.L; l++) maxP = g.ly[l].P > maxP ? g.ly[l].P : maxP;
