@@ -40,14 +40,16 @@ def test_flow_beats_plain_vegas_on_mixture():
     F = FlowIntegrator(8 * [[0, 1]], neval=neval, seed=11, plain_itn=10, kl_itn=10, train_itn=40,
                        grace=1000, train_steps=6, train_batch=1 << 15)
     F(f, nitn=50)                      # 10 plain + 40 training flow iterations
-    rf = F(f, nitn=10)                 # frozen flow
+    rf = F(f, nitn=20)                 # frozen flow
     assert F.flow_on
-    v_flow = np.median([h['sdev'] ** 2 * h['neval'] for h in F.history[-10:]])
+    # medians over 20 iterations each (a median of 10 variance estimates
+    # moves by about 15 % with the rounding of the training run)
+    v_flow = np.median([h['sdev'] ** 2 * h['neval'] for h in F.history[-20:]])
     # the same map and strata without the flow: plain vegas+ continued from
     # the integrator the flow was inserted into, map frozen (alpha = 0)
     base = vg.Integrator(F.vegas, alpha=0.0, seed=12)
     base(f, nitn=10)
-    rb = base(f, nitn=10)
+    rb = base(f, nitn=20)
     v_base = np.median([r.sdev ** 2 for r in rb.itn_results]) * base.last_neval
     assert v_flow * 5 <= v_base, (v_flow, v_base, v_plain)
     assert v_flow <= v_plain, (v_flow, v_plain)

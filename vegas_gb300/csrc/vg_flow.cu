@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(WGU_NT) flow_wgrad_umma_kernel(const __nv_bflo
     __shared__ uint64_t bars[3];   // buffer 0, buffer 1, drain
     __shared__ uint32_t slot;
     __shared__ int s_ok;
-    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *base = umma::align1024(dsm);
     constexpr uint32_t TILE = 128 * 128;   // bytes of a 128 x 64 bf16 tile
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m0 = blockIdx.x * 128;
@@ -914,30 +914,38 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
     for (int k = 4; k <= K; k++) v4[k & 3] = fmaxf(v4[k & 3], o[K + k]);
     const float mx = fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3]));
     const float mv = fmaxf(fmaxf(v4[0], v4[1]), fmaxf(v4[2], v4[3]));
-    float s4[4] = {0.f, 0.f, 0.f, 0.f};
+    // exponentials as 2^(v log2 e - max log2 e): one FMA and the MUFU each;
+    // the vertex heights are stored halved (exponent - 1), which absorbs the
+    // trapezoid's 1/2 in the segment areas (the partial-bin formulas at the
+    // end restore the factor 2)
+    constexpr float L2E = 1.4426950408889634f;
+    const float mxl = mx * L2E, mvl = fmaf(mv, L2E, 1.f);
+    // width exponentials, summed per block of 8 bins (NB independent chains)
+    float sB[NB];
+#pragma unroll
+    for (int b = 0; b < NB; b++) sB[b] = 0.f;
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        o[k] = __expf(o[k] - mx);
-        s4[k & 3] += o[k];
+        o[k] = vg_ex2_approx(fmaf(o[k], L2E, -mxl));
+        sB[k >> 3] += o[k];
     }
-    const float cw = __fdividef(c1, (s4[0] + s4[1]) + (s4[2] + s4[3]));
+    float stot = 0.f;
+#pragma unroll
+    for (int b = 0; b < NB; b++) stot += sB[b];
+    const float cw = __fdividef(c1, stot);
 #pragma unroll
     for (int k = 0; k < K; k++) o[k] = fmaf(cw, o[k], EPS_W);   // bin widths
 #pragma unroll
-    for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);   // vertex heights (unnormalised)
-    float seg[K];
+    for (int k = 0; k <= K; k++) o[K + k] = vg_ex2_approx(fmaf(o[K + k], L2E, -mvl));   // vertex heights / 2
+    // per block: width EB = cw sum(exp) + 8 EPS_W, area PB = sum (u_k + u_k+1) W_k
     float EB[NB], PB[NB];
 #pragma unroll
     for (int b = 0; b < NB; b++) {
-        EB[b] = 0.f;
+        EB[b] = fmaf(cw, sB[b], 8.f * EPS_W);
         PB[b] = 0.f;
     }
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        seg[k] = 0.5f * (o[K + k] + o[K + k + 1]) * o[k];
-        EB[k >> 3] += o[k];
-        PB[k >> 3] += seg[k];
-    }
+    for (int k = 0; k < K; k++) PB[k >> 3] = fmaf(o[K + k] + o[K + k + 1], o[k], PB[k >> 3]);
     float Es[NB], Ps[NB];
     Es[0] = 0.f;
     Ps[0] = 0.f;
@@ -949,8 +957,9 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
     const float Z = Ps[NB - 1] + PB[NB - 1];
     const float t = DIR == 0 ? x : x * Z;
     // two-level search: the block of 8 bins that holds t (compares of the
-    // block prefixes), then a scan of that block's 8 bins, whose values are
-    // selected from the NB blocks' registers (no dynamic register indexing)
+    // block prefixes), then a scan of that block's 8 bins, whose widths and
+    // heights are selected from the NB blocks' registers once (no dynamic
+    // register indexing) and whose areas are recomputed from them
     int bsel = 0;
 #pragma unroll
     for (int b = 1; b < NB; b++) bsel += (DIR == 0 ? (t >= Es[b]) : (t >= Ps[b])) ? 1 : 0;
@@ -960,41 +969,49 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
         E = bsel == b ? Es[b] : E;
         P = bsel == b ? Ps[b] : P;
     }
+    float wsel[8], usel[9];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        wsel[q] = o[q];
+#pragma unroll
+        for (int b = 1; b < NB; b++) wsel[q] = bsel == b ? o[8 * b + q] : wsel[q];
+    }
+#pragma unroll
+    for (int q = 0; q <= 8; q++) {
+        usel[q] = o[K + q];
+#pragma unroll
+        for (int b = 1; b < NB; b++) usel[q] = bsel == b ? o[K + 8 * b + q] : usel[q];
+    }
     float Wb = 0.f, ub = 0.f, ub1 = 0.f, Eb = 0.f, Pb = 0.f;
     bool f = false;
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-        float wq = o[q], sq = seg[q], uq = o[K + q], uq1 = o[K + q + 1];
-#pragma unroll
-        for (int b = 1; b < NB; b++) {
-            wq = bsel == b ? o[8 * b + q] : wq;
-            sq = bsel == b ? seg[8 * b + q] : sq;
-            uq = bsel == b ? o[K + 8 * b + q] : uq;
-            uq1 = bsel == b ? o[K + 8 * b + q + 1] : uq1;
-        }
+        const float wq = wsel[q], sq = (usel[q] + usel[q + 1]) * wq;
         // the last bin of the block takes t when no earlier bin did
         const bool here = !f && (q == 7 || (DIR == 0 ? (t < E + wq) : (t < P + sq)));
         Wb = here ? wq : Wb;
-        ub = here ? uq : ub;
-        ub1 = here ? uq1 : ub1;
+        ub = here ? usel[q] : ub;
+        ub1 = here ? usel[q + 1] : ub1;
         Eb = here ? E : Eb;
         Pb = here ? P : Pb;
         f = f || here;
         E += wq;
         P += sq;
     }
+    // ub, ub1 are half the vertex heights: the area of the first al of the
+    // bin is Wb (al 2 ub + al^2 (ub1 - ub)), the pdf 2 ((1 - al) ub + al ub1) / Z
     float al, xo;
     if (DIR == 0) {
         al = fminf(fmaxf(__fdividef(x - Eb, Wb), 0.f), 1.f);
-        xo = __fdividef(Pb + Wb * (al * ub + 0.5f * al * al * (ub1 - ub)), Z);
+        xo = __fdividef(Pb + Wb * al * (2.f * ub + al * (ub1 - ub)), Z);
     } else {
-        const float qa = 0.5f * Wb * (ub1 - ub), qb = Wb * ub;
+        const float qa = Wb * (ub1 - ub), qb = 2.f * Wb * ub;
         const float r = fmaxf(t - Pb, 0.f);
         al = __fdividef(2.f * r, fmaxf(qb + sqrtf(fmaxf(qb * qb + 4.f * qa * r, 0.f)), 1e-30f));
         al = fminf(fmaxf(al, 0.f), 1.f);
         xo = Eb + al * Wb;
     }
-    const float pdfu = (1.f - al) * ub + al * ub1;
+    const float pdfu = 2.f * ((1.f - al) * ub + al * ub1);
     lp = __logf(pdfu) - __logf(Z);
     return xo;
 }
@@ -1009,7 +1026,7 @@ constexpr int UCOL = FH / UNH;   // H columns per thread in the epilogues (32)
 struct UmmaPlan {
     int ST;                      // sub-tiles per super-tile
     int zst;                     // row stride of the state in shared memory (odd)
-    size_t oW2, oW3, oA, oW1, ob1, ob2, ob3, oZ, oLD, total;
+    size_t oW2, oW3, oA, oA2, oW1, ob1, ob2, ob3, oZ, oLD, total;
 };
 
 __host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
@@ -1021,6 +1038,11 @@ __host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
     p.oW2 = o; o += (size_t)FH * FH * 2;
     p.oW3 = o; o += (size_t)g.NPmax * FH * 2;
     p.oA = o;  o += (size_t)FH * FH * 2;
+    p.oA2 = 0;   // second A buffer of the sub-tile pipeline (layers of at most UNH transformed coordinates)
+    if (g.dBmax <= UNH) {
+        p.oA2 = o;
+        o += (size_t)FH * FH * 2;
+    }
     p.oW1 = o; o += sizeof(float) * FH * 8;
     p.ob1 = o; o += sizeof(float) * FH;
     p.ob2 = o; o += sizeof(float) * FH;
@@ -1058,12 +1080,13 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
     __shared__ uint64_t bars[5];   // 0 weights, 1 GEMM1, 2-3 GEMM2 buffers, 4 drain
     __shared__ uint32_t tslot;
     __shared__ int abort_flag;
-    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *base = umma::align1024(dsm);
     const UmmaPlan pl = umma_plan(g, ST);
     uint8_t *sW2 = base + pl.oW2, *sW3 = base + pl.oW3, *sA = base + pl.oA;
     float *sW1 = (float *)(base + pl.oW1), *sb1 = (float *)(base + pl.ob1);
     float *sb2 = (float *)(base + pl.ob2), *sb3 = (float *)(base + pl.ob3);
     float *sZ = (float *)(base + pl.oZ), *sLD = (float *)(base + pl.oLD);
+    uint8_t *sA2 = pl.oA2 ? base + pl.oA2 : nullptr;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int r = tid & (FROWS - 1), h = tid >> 7;
     const int dim = g.dim, zst = pl.zst, CH = g.CH;
@@ -1123,66 +1146,57 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
             ph_w ^= 1;
             __syncthreads();
             if (abort_flag) { aborted = true; break; }
-            for (int s = 0; s < nsub; s++) {
-                float *Zs = sZ + (size_t)s * FROWS * zst;
-                if (zl != nullptr) {
-                    for (int i = tid; i < FROWS * dim; i += UNT) {
-                        const int rr = i / dim, d = i % dim;
-                        const int64_t grow = r0 + (int64_t)s * FROWS + rr;
-                        if (grow < n) zl[((int64_t)l * n + grow) * dim + d] = Zs[rr * zst + d];
-                    }
+            // ---- phases of one 128-row sub-tile (thread work; thread 0 issues the MMAs)
+            auto store_zl = [&](int s) {
+                if (zl == nullptr) return;
+                const float *Zs = sZ + (size_t)s * FROWS * zst;
+                for (int i = tid; i < FROWS * dim; i += UNT) {
+                    const int rr = i / dim, d = i % dim;
+                    const int64_t grow = r0 + (int64_t)s * FROWS + rr;
+                    if (grow < n) zl[((int64_t)l * n + grow) * dim + d] = Zs[rr * zst + d];
                 }
-                // ---- H1 (FP32) -> A operand
-                {
-                    float xa[8];
+            };
+            // H1 = relu(W1 z_A + b1) in FP32 -> A operand
+            auto h1_phase = [&](int s, uint8_t *A) {
+                const float *Zs = sZ + (size_t)s * FROWS * zst;
+                float xa[8];
 #pragma unroll
-                    for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? Zs[r * zst + y.A[a]] : 0.f;
-                    const bool wide = dA > 4;
+                for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? Zs[r * zst + y.A[a]] : 0.f;
+                const bool wide = dA > 4;
 #pragma unroll 2
-                    for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
-                        float v[8];
-                        const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
-                        const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
-                        v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
-                        v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
+                for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
+                    float v[8];
+                    const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
+                    const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
+                    v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
+                    v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
 #pragma unroll
-                        for (int q = 0; q < 8; q++) {
-                            const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
-                            float acc = v[q];
-                            acc = fmaf(w0.x, xa[0], acc);
-                            acc = fmaf(w0.y, xa[1], acc);
-                            acc = fmaf(w0.z, xa[2], acc);
-                            acc = fmaf(w0.w, xa[3], acc);
-                            if (wide) {
-                                const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
-                                acc = fmaf(w1.x, xa[4], acc);
-                                acc = fmaf(w1.y, xa[5], acc);
-                                acc = fmaf(w1.z, xa[6], acc);
-                                acc = fmaf(w1.w, xa[7], acc);
-                            }
-                            v[q] = fmaxf(acc, 0.f);
+                    for (int q = 0; q < 8; q++) {
+                        const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
+                        float acc = v[q];
+                        acc = fmaf(w0.x, xa[0], acc);
+                        acc = fmaf(w0.y, xa[1], acc);
+                        acc = fmaf(w0.z, xa[2], acc);
+                        acc = fmaf(w0.w, xa[3], acc);
+                        if (wide) {
+                            const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
+                            acc = fmaf(w1.x, xa[4], acc);
+                            acc = fmaf(w1.y, xa[5], acc);
+                            acc = fmaf(w1.z, xa[6], acc);
+                            acc = fmaf(w1.w, xa[7], acc);
                         }
-                        uint4 pk;
-                        pk.x = pack_bf16(v[0], v[1]);
-                        pk.y = pack_bf16(v[2], v[3]);
-                        pk.z = pack_bf16(v[4], v[5]);
-                        pk.w = pack_bf16(v[6], v[7]);
-                        *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(FH, r, c0)) = pk;
+                        v[q] = fmaxf(acc, 0.f);
                     }
+                    uint4 pk;
+                    pk.x = pack_bf16(v[0], v[1]);
+                    pk.y = pack_bf16(v[2], v[3]);
+                    pk.z = pack_bf16(v[4], v[5]);
+                    pk.w = pack_bf16(v[6], v[7]);
+                    *reinterpret_cast<uint4 *>(A + umma::sw128_offset(FH, r, c0)) = pk;
                 }
-                umma::fence_async_smem();
-                umma::fence_before_sync();
-                __syncthreads();
-                if (tid == 0) {
-                    umma::fence_after_sync();
-                    umma::gemm_128xN(tmem, umma::smem_u32(sA), umma::smem_u32(sW2), FH, FH, FH, 0);
-                    umma::mma_commit(bar_h);
-                }
-                if (tid == 0 && !umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
-                ph_h ^= 1;
-                __syncthreads();
-                umma::fence_after_sync();
-                // ---- H2 epilogue: TMEM -> +b2, relu -> A operand
+            };
+            // H2 epilogue: TMEM[0,128) + b2, relu -> A operand (in place of H1)
+            auto h2_phase = [&](uint8_t *A) {
                 for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 32) {
                     float v[32];
                     umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
@@ -1196,67 +1210,170 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                         pk.y = pack_bf16(fmaxf(v[q8 + 2] + bl.z, 0.f), fmaxf(v[q8 + 3] + bl.w, 0.f));
                         pk.z = pack_bf16(fmaxf(v[q8 + 4] + bh.x, 0.f), fmaxf(v[q8 + 5] + bh.y, 0.f));
                         pk.w = pack_bf16(fmaxf(v[q8 + 6] + bh.z, 0.f), fmaxf(v[q8 + 7] + bh.w, 0.f));
-                        *reinterpret_cast<uint4 *>(sA + umma::sw128_offset(FH, r, c)) = pk;
+                        *reinterpret_cast<uint4 *>(A + umma::sw128_offset(FH, r, c)) = pk;
                     }
                 }
-                umma::fence_async_smem();
-                umma::fence_before_sync();
-                __syncthreads();
-                if (abort_flag) { aborted = true; break; }
-                // ---- output layer in groups of UNH coordinates (one per column
-                // group of threads): two MMAs of up to two coordinates each
-                const int ngroups = (y.dB + UNH - 1) / UNH;
-                for (int gi = 0; gi < ngroups; gi++) {
-                    if (tid == 0) {
-                        umma::fence_after_sync();
+            };
+            // output layer of coordinate group gi (UNH coordinates, one per
+            // column group of threads): two MMAs of up to two coordinates each
+            // into TMEM[128, 128 + 4 CH); thread 0 only
+            auto issue_out = [&](int gi, const uint8_t *A) {
 #pragma unroll
-                        for (int p = 0; p < UNH / 2; p++) {
-                            const int first = UNH * gi + 2 * p;
-                            if (first >= y.dB) break;
-                            const int ncoord = (first + 1 < y.dB) ? 2 : 1;
-                            const int N = ncoord == 2 ? 2 * CH : (CH + 15) / 16 * 16;
-                            umma::gemm_128xN(tmem + (uint32_t)(FH + 2 * p * CH), umma::smem_u32(sA),
-                                             umma::smem_u32(sW3) + (uint32_t)(first * CH) * 128u, N, FH, y.NP, 0);
-                        }
-                        umma::mma_commit(bar_o0);
-                        if (!umma::mbar_wait(bar_o0, ph_o0)) abort_flag = 1;
+                for (int p = 0; p < UNH / 2; p++) {
+                    const int first = UNH * gi + 2 * p;
+                    if (first >= y.dB) break;
+                    const int ncoord = (first + 1 < y.dB) ? 2 : 1;
+                    const int N = ncoord == 2 ? 2 * CH : (CH + 15) / 16 * 16;
+                    umma::gemm_128xN(tmem + (uint32_t)(FH + 2 * p * CH), umma::smem_u32(A),
+                                     umma::smem_u32(sW3) + (uint32_t)(first * CH) * 128u, N, FH, y.NP, 0);
+                }
+            };
+            // spline of (row r, coordinate UNH gi + h) from the group's logits in TMEM
+            auto spline_phase = [&](int s, int gi) {
+                const int j = UNH * gi + h;
+                if (j >= y.dB) return;
+                float *Zs = sZ + (size_t)s * FROWS * zst;
+                const uint32_t col = (uint32_t)(FH + h * CH);
+                float o[NR];
+                {
+                    float v[32];
+                    umma::tmem_ld32(tmem + lane_base + col, v);
+#pragma unroll
+                    for (int q = 0; q < 32; q++) o[q] = v[q];
+                    if (NR > 32) {
+                        umma::tmem_ld32(tmem + lane_base + col + 32u, v);
+#pragma unroll
+                        for (int q = 0; q < 32; q++)
+                            if (32 + q < NR) o[32 + q] = v[q];
                     }
-                    ph_o0 ^= 1;
-                    __syncthreads();
-                    const bool ok = abort_flag == 0;
-                    umma::fence_after_sync();
-                    const int j = UNH * gi + h;
-                    if (ok && j < y.dB) {
-                        const uint32_t col = (uint32_t)(FH + h * CH);
-                        float o[NR];
-                        {
-                            float v[32];
-                            umma::tmem_ld32(tmem + lane_base + col, v);
+                    if (NR > 64) o[64] = umma::tmem_ld1(tmem + lane_base + col + 64u);
+                }
+                const float *bb = sb3 + j * NR;
 #pragma unroll
-                            for (int q = 0; q < 32; q++) o[q] = v[q];
-                            if (NR > 32) {
-                                umma::tmem_ld32(tmem + lane_base + col + 32u, v);
-#pragma unroll
-                                for (int q = 0; q < 32; q++)
-                                    if (32 + q < NR) o[32 + q] = v[q];
-                            }
-                            if (NR > 64) o[64] = umma::tmem_ld1(tmem + lane_base + col + 64u);
-                        }
-                        const float *bb = sb3 + j * NR;
-#pragma unroll
-                        for (int q = 0; q < NR; q++) o[q] += bb[q];
-                        const int cz = y.B[j];
-                        const float xin = Zs[r * zst + cz];
-                        float lp;
-                        const float xo = spline_reg<K, DIR>(o, xin, lp);
-                        Zs[r * zst + cz] = fminf(fmaxf(xo, 0.f), 1.f);
-                        sLD[(size_t)h * ST * FROWS + s * FROWS + r] += lp;
-                    }
+                for (int q = 0; q < NR; q++) o[q] += bb[q];
+                const int cz = y.B[j];
+                const float xin = Zs[r * zst + cz];
+                float lp;
+                const float xo = spline_reg<K, DIR>(o, xin, lp);
+                Zs[r * zst + cz] = fminf(fmaxf(xo, 0.f), 1.f);
+                sLD[(size_t)h * ST * FROWS + s * FROWS + r] += lp;
+            };
+            const int ngroups = (y.dB + UNH - 1) / UNH;
+            if (sA2 != nullptr && ngroups == 1) {
+                // Software pipeline over the sub-tiles (one coordinate group):
+                // the tensor core runs sub-tile s+1's hidden-layer MMA during
+                // sub-tile s's splines, and sub-tile s's output MMAs during
+                // sub-tile s+1's H1; the two A buffers alternate.
+                uint8_t *Ab[2] = {sA, sA2};
+                do {
+                    store_zl(0);
+                    h1_phase(0, Ab[0]);
+                    umma::fence_async_smem();
                     umma::fence_before_sync();
                     __syncthreads();
-                    if (!ok) break;
+                    if (tid == 0) {
+                        umma::fence_after_sync();
+                        umma::gemm_128xN(tmem, umma::smem_u32(Ab[0]), umma::smem_u32(sW2), FH, FH, FH, 0);
+                        umma::mma_commit(bar_h);
+                        if (!umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
+                    }
+                    ph_h ^= 1;
+                    __syncthreads();
+                    umma::fence_after_sync();
+                    if (abort_flag) { aborted = true; break; }
+                    h2_phase(Ab[0]);
+                    umma::fence_async_smem();
+                    umma::fence_before_sync();
+                    __syncthreads();
+                    if (tid == 0) {
+                        umma::fence_after_sync();
+                        issue_out(0, Ab[0]);
+                        umma::mma_commit(bar_o0);
+                    }
+                    for (int s = 0; s < nsub; s++) {
+                        uint8_t *nxt = Ab[(s + 1) & 1];
+                        const bool more = s + 1 < nsub;
+                        if (more) {   // overlaps sub-tile s's output MMAs
+                            store_zl(s + 1);
+                            h1_phase(s + 1, nxt);
+                        }
+                        umma::fence_async_smem();
+                        umma::fence_before_sync();
+                        __syncthreads();
+                        if (tid == 0) {
+                            umma::fence_after_sync();
+                            if (more) {
+                                umma::gemm_128xN(tmem, umma::smem_u32(nxt), umma::smem_u32(sW2), FH, FH, FH, 0);
+                                umma::mma_commit(bar_h);
+                            }
+                            if (!umma::mbar_wait(bar_o0, ph_o0)) abort_flag = 1;
+                        }
+                        ph_o0 ^= 1;
+                        __syncthreads();
+                        umma::fence_after_sync();
+                        if (abort_flag) { aborted = true; break; }
+                        spline_phase(s, 0);   // overlaps sub-tile s+1's hidden-layer MMA
+                        umma::fence_before_sync();
+                        __syncthreads();
+                        if (more) {
+                            if (tid == 0 && !umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
+                            ph_h ^= 1;
+                            __syncthreads();
+                            umma::fence_after_sync();
+                            if (abort_flag) { aborted = true; break; }
+                            h2_phase(nxt);
+                            umma::fence_async_smem();
+                            umma::fence_before_sync();
+                            __syncthreads();
+                            if (tid == 0) {
+                                umma::fence_after_sync();
+                                issue_out(0, nxt);
+                                umma::mma_commit(bar_o0);
+                            }
+                        }
+                    }
+                } while (0);
+                if (aborted) break;
+            } else {
+                for (int s = 0; s < nsub; s++) {
+                    store_zl(s);
+                    h1_phase(s, sA);
+                    umma::fence_async_smem();
+                    umma::fence_before_sync();
+                    __syncthreads();
+                    if (tid == 0) {
+                        umma::fence_after_sync();
+                        umma::gemm_128xN(tmem, umma::smem_u32(sA), umma::smem_u32(sW2), FH, FH, FH, 0);
+                        umma::mma_commit(bar_h);
+                        if (!umma::mbar_wait(bar_h, ph_h)) abort_flag = 1;
+                    }
+                    ph_h ^= 1;
+                    __syncthreads();
+                    umma::fence_after_sync();
+                    h2_phase(sA);
+                    umma::fence_async_smem();
+                    umma::fence_before_sync();
+                    __syncthreads();
+                    if (abort_flag) { aborted = true; break; }
+                    for (int gi = 0; gi < ngroups; gi++) {
+                        if (tid == 0) {
+                            umma::fence_after_sync();
+                            issue_out(gi, sA);
+                            umma::mma_commit(bar_o0);
+                            if (!umma::mbar_wait(bar_o0, ph_o0)) abort_flag = 1;
+                        }
+                        ph_o0 ^= 1;
+                        __syncthreads();
+                        const bool ok = abort_flag == 0;
+                        umma::fence_after_sync();
+                        if (ok) spline_phase(s, gi);
+                        umma::fence_before_sync();
+                        __syncthreads();
+                        if (!ok) break;
+                    }
+                    if (abort_flag) { aborted = true; break; }
                 }
-                if (abort_flag) { aborted = true; break; }
+                if (aborted) break;
             }
             __syncthreads();
         }
@@ -1318,17 +1435,19 @@ __device__ __forceinline__ float spline_grad_reg(float (&o)[2 * K + 1], float x,
     for (int k = 4; k <= K; k++) v4[k & 3] = fmaxf(v4[k & 3], o[K + k]);
     const float mx = fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3]));
     const float mv = fmaxf(fmaxf(v4[0], v4[1]), fmaxf(v4[2], v4[3]));
+    constexpr float L2E = 1.4426950408889634f;   // exponentials as 2^(v log2 e - max log2 e)
+    const float mxl = mx * L2E, mvl = mv * L2E;
     float s4[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < K; k++) {
-        o[k] = __expf(o[k] - mx);
+        o[k] = vg_ex2_approx(fmaf(o[k], L2E, -mxl));
         s4[k & 3] += o[k];
     }
     const float rse = 1.f / ((s4[0] + s4[1]) + (s4[2] + s4[3]));
 #pragma unroll
     for (int k = 0; k < K; k++) o[k] *= rse;                               // softmax s_k
 #pragma unroll
-    for (int k = 0; k <= K; k++) o[K + k] = __expf(o[K + k] - mv);          // vertex heights u_k
+    for (int k = 0; k <= K; k++) o[K + k] = vg_ex2_approx(fmaf(o[K + k], L2E, -mvl));   // vertex heights u_k
     // bin of x with the prefix sums at it, in the CDF's sequential order
     float E = 0.f, P = 0.f, Eb = 0.f, Pb = 0.f, Wb = 1.f, ub = 0.f, ub1 = 0.f;
     int b = K - 1;
@@ -1514,7 +1633,7 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
     __shared__ uint64_t bars[2];            // 0 weights, 1 MMA completion
     __shared__ uint32_t tslot;
     __shared__ int abort_flag;
-    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *base = umma::align1024(dsm);
     const BwdPlan pl = bwd_plan(g);
     const FlowLayer &y = g.ly[l];
     uint8_t *sW2 = base + pl.oW2, *sW3 = base + pl.oW3, *sRA = base + pl.oRA, *sBz = base + pl.oBz;
@@ -1872,7 +1991,7 @@ __global__ void __launch_bounds__(WGI_NT) flow_wgrad_img_kernel(
     __shared__ uint64_t bars[5];   // full 0/1, empty 0/1, drain
     __shared__ uint32_t slot;
     __shared__ int s_ok;
-    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *base = umma::align1024(dsm);
     uint8_t *sOnes = base;                    // 16 x 128 K-major ones (4 KB)
     uint8_t *stg = base + 4096;               // 2 stages x (A 2 blocks + B 2 blocks)
     const int tid = threadIdx.x, warp = tid >> 5;

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t bar;
     __shared__ uint32_t slot;
-    uint8_t *base = (uint8_t *)(((uintptr_t)dsm + 1023) & ~(uintptr_t)1023);
+    uint8_t *base = umma::align1024(dsm);
     uint8_t *sa = base;
     uint8_t *sb = base + 128 * K * 2;
     const int tid = threadIdx.x, warp = tid >> 5;

@@ -23,6 +23,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p)
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// The 1024-byte aligned start of a dynamic shared-memory array, derived by
+// pointer arithmetic on the array itself (not through an integer), so that
+// the compiler keeps shared-space addressing (32-bit, LDS / STS) for every
+// pointer into it.
+__device__ __forceinline__ uint8_t *align1024(uint8_t *dsm)
+{
+    return dsm + ((1024u - (smem_u32(dsm) & 1023u)) & 1023u);
+}
+
 // byte offset of element (r, k) inside a K-major SW128 tile of R rows
 __device__ __forceinline__ uint32_t sw128_offset(int R, int r, int k)
 {
