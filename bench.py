@@ -53,10 +53,13 @@ def parse():
     ap.add_argument('--no-tta', action='store_true')
     ap.add_argument('--device-loop-only', action='store_true',
                     help='run only the device-resident iteration loop (for profilers)')
-    ap.add_argument('--case', default='ridge', choices=['ridge', 'flow', 'batch', 'dropin', 'lattice'],
+    ap.add_argument('--case', default='ridge',
+                    choices=['ridge', 'flow', 'flow_train', 'batch', 'dropin', 'lattice'],
                     help='with --device-loop-only: which kernel family to run (for profilers): '
                          'ridge = the fused vegas+ iteration, flow = the flow sampling pass '
-                         '(dim 8, 2^18 rows), batch = the batched launch on 256 Lorentzian integrals, '
+                         '(dim 8, 2^18 rows), flow_train = flow training steps (dim 8, 2^15 rows: '
+                         'forward, per layer backward + weight gradients, Adam), '
+                         'batch = the batched launch on 256 Lorentzian integrals, '
                          'dropin = the drop-in path (torch integrand, sampling and reduction kernels), '
                          'lattice = the lambda-scan launch on 16 couplings x 2e6 evaluations')
     ap.add_argument('--no-batch', action='store_true', help='skip the batched many-integral line')
@@ -132,6 +135,14 @@ def profile_case(args, dev):
         u = torch.rand(1 << 18, 8, device=dev, generator=g)
         for _ in range(args.warmup + args.steps):
             fl.sample(u)
+    elif args.case == 'flow_train':
+        from vegas_gb300.flow import Flow
+        fl = Flow(8, seed=3, device=dev)
+        g = torch.Generator(device=dev).manual_seed(0)
+        z = torch.rand(1 << 15, 8, device=dev, generator=g)
+        w = 2 * torch.rand(1 << 15, device=dev, generator=g)
+        for _ in range(args.warmup + args.steps):
+            fl.train_step_normalized(z, w)
     elif args.case == 'dropin':
         # the drop-in path's sampling and reduction kernels, 1e7 evaluations
         dropin_line(dev, neval=10 ** 7, nitn=1, reps=max(1, args.steps))
