@@ -180,7 +180,7 @@ def test_gpu_flow_large_batch_paths_agree():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('dim', [3, 4, 8])
+@pytest.mark.parametrize('dim', [3, 4, 8, 16])
 def test_gpu_flow_gradient_vs_oracle(dim, flow_path):
     theta = _theta(dim, seed=2, out_scale=0.3)
     fl = _gpu_flow(dim, theta)
@@ -209,11 +209,13 @@ def test_gpu_flow_gradient_vs_oracle(dim, flow_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('dim,K', [(8, 32), (4, 16), (3, 32)])
+@pytest.mark.parametrize('dim,K', [(8, 32), (4, 16), (3, 32), (16, 32), (9, 16)])
 def test_gpu_flow_backward_paths_agree(dim, K):
     """40000 rows (313 tiles: several per CTA of the tcgen05 backward, so its
     dW1 accumulator carries across tiles, and a multi-stage weight-gradient
-    pipeline): the tcgen05 backward against the mma.sync backward.  Both
+    pipeline; dim 16 and 9 have layers of 8 and 5 transformed coordinates,
+    two coordinate groups with the W3 rows streamed per group): the tcgen05
+    backward against the mma.sync backward.  Both
     round the same operands to BF16; they differ in summation order and in
     rare BF16 rounding flips.  Each path is within 2u of the oracle overall
     and 4u per block (test above), so the two agree within the same bounds

@@ -1568,58 +1568,73 @@ constexpr uint32_t BLK = FROWS * 128;    // bytes of one 64-column block of a 12
 constexpr uint32_t TW1_COL = 448;        // TMEM columns [448, 480): dW1 | db1 accumulator
 
 // Shared-memory plan of the tcgen05 backward (offsets from the 1024-aligned
-// dynamic base).  RA holds, in turn: H1 | H2 (A operands of the forward
-// recomputation), dL/dout (A operand of dH2, NB3 blocks), dH2' | dH1'.
+// dynamic base).  The transformed coordinates of a layer go in groups of up
+// to four (TMEM columns [128, 128 + 4 CH) hold one group's logits); W3 holds
+// one group's rows of the W3 image (all of it when a layer has one group).
+// RA holds, in turn: H1 | H2 (A operands of the forward recomputation),
+// dL/dout of a group (A operand of dH2, NB3G blocks), dH2' | dH1' and the
+// partial sums of dL/dz_A at 4 blocks.
 struct BwdPlan {
-    int NB3;                             // 64-column blocks of the dL/dout tile (widest layer)
-    size_t oW2, oW3, oRA, oBz, oW1, ob1, ob2, ob3, oZ, oG, oLW, oRED, total;
+    int NPG;                             // W3 rows of a group of four coordinates (4 CH, padded to 16)
+    int NB3G;                            // 64-column blocks of a group's dL/dout tile
+    size_t oW2, oW3, oRA, oRED, oBz, oW1, ob1, ob2, ob3, oZ, oG, oLW, total;
 };
 
 __host__ __device__ inline BwdPlan bwd_plan(const FlowGeom &g)
 {
     BwdPlan p;
-    p.NB3 = (g.NPmax + 63) / 64;
+    const int ncg = g.dBmax < 4 ? g.dBmax : 4;
+    p.NPG = (ncg * g.CH + 15) / 16 * 16;
+    p.NB3G = (p.NPG + 63) / 64;
     const int zst = g.dim | 1;
     size_t o = 0;
     p.oW2 = o; o += (size_t)FH * FH * 2;
-    p.oW3 = o; o += ((size_t)g.NPmax * FH * 2 + 1023) / 1024 * 1024;
+    p.oW3 = o; o += ((size_t)p.NPG * FH * 2 + 1023) / 1024 * 1024;
     p.oRA = o;
+    p.oRED = o + (size_t)4 * BLK;              // dL/dz_A partials of column groups 1..3: [3][128][8] floats
     {
-        const size_t a = (size_t)4 * BLK, d = (size_t)p.NB3 * BLK;
-        o += a > d ? a : d;
+        const size_t a = (size_t)4 * BLK + sizeof(float) * 3 * FROWS * 8, d = (size_t)p.NB3G * BLK;
+        o += ((a > d ? a : d) + 1023) / 1024 * 1024;
     }
     p.oBz = o; o += (size_t)32 * FROWS * 2;    // [z_A hi (8) | z_A lo (8) | 1 | 0...] x 128 rows, K-major
     p.oW1 = o; o += sizeof(float) * FH * 8;
     p.ob1 = o; o += sizeof(float) * FH;
     p.ob2 = o; o += sizeof(float) * FH;
-    p.ob3 = o; o += sizeof(float) * 4 * (2 * g.K + 1);
+    p.ob3 = o; o += sizeof(float) * g.dBmax * (2 * g.K + 1);
     p.oZ = o;  o += sizeof(float) * FROWS * zst;
     p.oG = o;  o += sizeof(float) * FROWS * zst;
     p.oLW = o; o += sizeof(float) * FROWS;
-    p.oRED = o; o += sizeof(float) * 3 * FROWS * 8;
     p.total = o + 1024;
     return p;
 }
 
 // Training backward of layer l on the 5th-generation tensor cores (layers
-// with at most 4 transformed and 8 conditioning coordinates).  One CTA (16
-// warps) per SM, persistent over 128-row tiles; the layer's W2 and W3
-// operand images are fetched once per CTA.  Per tile:
+// with at most 8 transformed and 8 conditioning coordinates).  One CTA (16
+// warps) per SM, persistent over 128-row tiles; the layer's W2 image is
+// fetched once per CTA, its W3 image once per CTA when the layer has one
+// group of (up to four) transformed coordinates, else one group's rows at a
+// time (the next group's copy overlaps the recomputation of H1 and H2).
+// Per tile and group g:
 //   H1 = relu(W1 z_A + b1)                    FP32 FMA -> bf16 A operand
-//   TMEM[0,128)   = H1 W2^T                   tcgen05, K-major A and B
+//   TMEM[T1, T1+128) = H1 W2^T                tcgen05, K-major A and B
+//                                             (T1 = 0 for the first group,
+//                                             128 after: [0,128) then holds
+//                                             the dH2 sum)
 //   H2 = relu(. + b2)                         epilogue -> bf16 A operand
-//   TMEM[128,..)  = H2 W3^T                   the <= 4 coordinates' logits
+//   TMEM[128,..)  = H2 W3_g^T                 the group's logits
 //   spline forward + backward                 registers, thread = (row,
 //                                             coordinate); dL/dout -> bf16
-//   TMEM[0,128)   = dL/dout W3                B = the W3 image read MN-major
+//   TMEM[0,128)  += dL/dout_g W3_g            B = the W3 rows read MN-major
+// then, per tile:
 //   dH2' = . relu'(H2)                        epilogue -> bf16 A operand
 //   TMEM[128,256) = dH2' W2                   B = the W2 image read MN-major
 //   dH1' = . relu'(H1)                        epilogue -> bf16; dL/dz_A
 //   TMEM[448,480) += dH1'^T [z_A hi|lo|1]     dW1, db1 over the CTA's tiles
-// The bf16 tiles H1, H2, dL/dout and dH2' go out by bulk copy as images
-// (byte-identical to the shared-memory tiles) for flow_wgrad_img_kernel.
-// The relu masks of H1 and H2 stay in registers (thread = row, 32 columns).
-// Every wait is bounded; one that gives up sets g_flow_status.
+// The bf16 tiles H1, H2, dL/dout (per group) and dH2' go out by bulk copy as
+// images (byte-identical to the shared-memory tiles) for
+// flow_wgrad_img_kernel.  The relu masks of H1 and H2 stay in registers
+// (thread = row, 32 columns).  Every wait is bounded; one that gives up
+// sets g_flow_status.
 template <int K>
 __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
     FlowGeom g, int l, const float *__restrict__ theta, const __nv_bfloat16 *__restrict__ mirror, int64_t n,
@@ -1646,7 +1661,8 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
     const int r = tid & (FROWS - 1), h = tid >> 7;
     const int dim = g.dim, zst = dim | 1;
     const int dA = y.realA ? y.dA : 1, dB = y.dB, NPl = y.NP;
-    const int nb3l = (NPl + 63) / 64;
+    const int ngr = (dB + 3) / 4;                 // groups of transformed coordinates
+    const int R3 = ngr == 1 ? NPl : pl.NPG;       // rows of the W3 tile in shared memory
     const uint32_t bar_w = umma::smem_u32(&bars[0]), bar_m = umma::smem_u32(&bars[1]);
     if (warp == 0) umma::tmem_alloc(umma::smem_u32(&tslot), 512);
     if (tid == 0) {
@@ -1659,16 +1675,25 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
     umma::fence_after_sync();
     const uint32_t tmem = tslot;
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-    uint32_t ph_m = 0;
-    // the layer's weights, once per CTA
+    uint32_t ph_m = 0, ph_w = 0;
+    // rows [g NPG, ...) of the W3 image (R = NPl rows, two 64-column blocks)
+    // into the R3-row tile of shared memory; thread 0, completes on bar_w
+    auto load_w3 = [&](int gi, uint32_t extra) {
+        const int row0 = gi * pl.NPG;
+        const int rows = ngr == 1 ? NPl : (NPl - row0 < pl.NPG ? NPl - row0 : pl.NPG);
+        const uint32_t bytes = (uint32_t)rows * 128u;
+        umma::mbar_expect_tx(bar_w, extra + 2u * bytes);
+        for (int b = 0; b < 2; b++)
+            for (uint32_t off = 0; off < bytes; off += 32768u)   // copies of at most 32 KB
+                umma::bulk_g2s(umma::smem_u32(sW3) + (uint32_t)(b * R3) * 128u + off,
+                               (const uint8_t *)(mirror + y.mU3) + ((size_t)b * NPl + row0) * 128 + off,
+                               bytes - off < 32768u ? bytes - off : 32768u, bar_w);
+    };
+    // the layer's weights: W2 and the first group's W3 rows
     if (tid == 0) {
-        const uint32_t b2 = (uint32_t)FH * FH * 2, b3 = (uint32_t)NPl * FH * 2;
-        umma::mbar_expect_tx(bar_w, b2 + b3);
+        const uint32_t b2 = (uint32_t)FH * FH * 2;
+        load_w3(0, b2);
         umma::bulk_g2s(umma::smem_u32(sW2), mirror + y.mU2, b2, bar_w);
-        for (uint32_t off = 0; off < b3; off += 32768u) {
-            const uint32_t sz = (b3 - off) < 32768u ? (b3 - off) : 32768u;
-            umma::bulk_g2s(umma::smem_u32(sW3) + off, (const uint8_t *)(mirror + y.mU3) + off, sz, bar_w);
-        }
     }
     for (int i = tid; i < FH * 8; i += BNT) {
         const int c = i >> 3, a = i & 7;
@@ -1679,9 +1704,11 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
         sb2[i] = theta[y.ob2 + i];
     }
     for (int i = tid; i < dB * NR; i += BNT) sb3[i] = theta[y.ob3 + i];
-    if (tid == 0 && !umma::mbar_wait(bar_w, 0)) abort_flag = 1;
+    if (tid == 0 && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
+    ph_w ^= 1;
     __syncthreads();
     int ndone = 0;
+    bool w3_pending = false;   // a W3 copy in flight (thread 0's view; all threads track it alike)
     for (int64_t tile = blockIdx.x; tile < ntiles && !abort_flag; tile += gridDim.x) {
         const int64_t r0 = tile * FROWS;
         for (int i = tid; i < FROWS * dim; i += BNT) {
@@ -1692,150 +1719,176 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
         }
         if (tid < FROWS) sLW[tid] = (r0 + tid < n) ? -w[r0 + tid] : 0.f;   // dL/dlogpdf
         __syncthreads();
-        // ---- H1 (FP32) -> A operand, its relu mask; the [z_A hi | lo | 1] operand
         uint32_t m1 = 0, m2 = 0;
-        {
-            float xa[8];
+        for (int gi = 0; gi < ngr; gi++) {
+            const uint32_t T1 = gi == 0 ? 0u : (uint32_t)FH;   // TMEM columns of H1 W2^T
+            const int nc = dB - 4 * gi < 4 ? dB - 4 * gi : 4;   // coordinates of this group
+            const int Kg = (nc * CHT + 15) / 16 * 16;             // their dL/dout columns (MMA K)
+            const int nbg = (Kg + 63) / 64;
+            // ---- H1 (FP32) -> A operand, its relu mask; the [z_A hi | lo | 1] operand (first group)
+            m1 = 0;
+            m2 = 0;
+            {
+                float xa[8];
 #pragma unroll
-            for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? sZ[r * zst + y.A[a]] : 0.f;
-            const bool wide = dA > 4;
+                for (int a = 0; a < 8; a++) xa[a] = (a < dA && y.realA) ? sZ[r * zst + y.A[a]] : 0.f;
+                const bool wide = dA > 4;
 #pragma unroll 2
-            for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
-                float v[8];
-                const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
-                const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
-                v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
-                v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
+                for (int c0 = UCOL * h; c0 < UCOL * h + UCOL; c0 += 8) {
+                    float v[8];
+                    const float4 bl = *reinterpret_cast<const float4 *>(sb1 + c0);
+                    const float4 bh = *reinterpret_cast<const float4 *>(sb1 + c0 + 4);
+                    v[0] = bl.x; v[1] = bl.y; v[2] = bl.z; v[3] = bl.w;
+                    v[4] = bh.x; v[5] = bh.y; v[6] = bh.z; v[7] = bh.w;
 #pragma unroll
-                for (int q = 0; q < 8; q++) {
-                    const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
-                    float acc = v[q];
-                    acc = fmaf(w0.x, xa[0], acc);
-                    acc = fmaf(w0.y, xa[1], acc);
-                    acc = fmaf(w0.z, xa[2], acc);
-                    acc = fmaf(w0.w, xa[3], acc);
-                    if (wide) {
-                        const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
-                        acc = fmaf(w1.x, xa[4], acc);
-                        acc = fmaf(w1.y, xa[5], acc);
-                        acc = fmaf(w1.z, xa[6], acc);
-                        acc = fmaf(w1.w, xa[7], acc);
+                    for (int q = 0; q < 8; q++) {
+                        const float4 w0 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8);
+                        float acc = v[q];
+                        acc = fmaf(w0.x, xa[0], acc);
+                        acc = fmaf(w0.y, xa[1], acc);
+                        acc = fmaf(w0.z, xa[2], acc);
+                        acc = fmaf(w0.w, xa[3], acc);
+                        if (wide) {
+                            const float4 w1 = *reinterpret_cast<const float4 *>(sW1 + (c0 + q) * 8 + 4);
+                            acc = fmaf(w1.x, xa[4], acc);
+                            acc = fmaf(w1.y, xa[5], acc);
+                            acc = fmaf(w1.z, xa[6], acc);
+                            acc = fmaf(w1.w, xa[7], acc);
+                        }
+                        m1 |= (acc > 0.f ? 1u : 0u) << (c0 - UCOL * h + q);
+                        v[q] = fmaxf(acc, 0.f);
                     }
-                    m1 |= (acc > 0.f ? 1u : 0u) << (c0 - UCOL * h + q);
-                    v[q] = fmaxf(acc, 0.f);
+                    uint4 pk;
+                    pk.x = pack_bf16(v[0], v[1]);
+                    pk.y = pack_bf16(v[2], v[3]);
+                    pk.z = pack_bf16(v[4], v[5]);
+                    pk.w = pack_bf16(v[6], v[7]);
+                    *reinterpret_cast<uint4 *>(sH1 + umma::sw128_offset(FROWS, r, c0)) = pk;
                 }
-                uint4 pk;
-                pk.x = pack_bf16(v[0], v[1]);
-                pk.y = pack_bf16(v[2], v[3]);
-                pk.z = pack_bf16(v[4], v[5]);
-                pk.w = pack_bf16(v[6], v[7]);
-                *reinterpret_cast<uint4 *>(sH1 + umma::sw128_offset(FROWS, r, c0)) = pk;
-            }
-            // rows 8h..8h+7 of the 32 x 128 operand: z_A hi (h = 0), z_A lo (h = 1), ones (row 16), zeros
+                if (gi == 0) {
+                    // rows 8h..8h+7 of the 32 x 128 operand: z_A hi (h = 0), z_A lo (h = 1), ones (row 16), zeros
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const __nv_bfloat16 hi = __float2bfloat16(xa[q]);
-                const __nv_bfloat16 lo = __float2bfloat16(xa[q] - __bfloat162float(hi));
-                const __nv_bfloat16 v = h == 0 ? hi : h == 1 ? lo : __float2bfloat16((h == 2 && q == 0) ? 1.f : 0.f);
-                *reinterpret_cast<__nv_bfloat16 *>(sBz + umma::sw128_offset(32, 8 * h + q, r)) = v;
-            }
-        }
-        umma::fence_async_smem();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {   // TMEM[0,128) = H1 W2^T; the H1 image out
-            umma::fence_after_sync();
-            umma::gemm_128xN(tmem, umma::smem_u32(sH1), umma::smem_u32(sW2), FH, FH, FH, 0);
-            umma::mma_commit(bar_m);
-            umma::bulk_s2g(imgH1 + tile * 2 * BLK, umma::smem_u32(sH1), BLK);
-            umma::bulk_s2g(imgH1 + tile * 2 * BLK + BLK, umma::smem_u32(sH1) + BLK, BLK);
-            umma::bulk_commit();
-            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
-        }
-        ph_m ^= 1;
-        __syncthreads();
-        umma::fence_after_sync();
-        if (abort_flag) break;
-        // ---- H2 = relu(TMEM + b2) -> A operand, its relu mask
-        {
-            const int c0 = UCOL * h;
-            float v[32];
-            umma::tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
-#pragma unroll
-            for (int q8 = 0; q8 < 32; q8 += 8) {
-                float a[8];
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    a[i] = v[q8 + i] + sb2[c0 + q8 + i];
-                    m2 |= (a[i] > 0.f ? 1u : 0u) << (q8 + i);
-                    a[i] = fmaxf(a[i], 0.f);
+                    for (int q = 0; q < 8; q++) {
+                        const __nv_bfloat16 hi = __float2bfloat16(xa[q]);
+                        const __nv_bfloat16 lo = __float2bfloat16(xa[q] - __bfloat162float(hi));
+                        const __nv_bfloat16 v =
+                            h == 0 ? hi : h == 1 ? lo : __float2bfloat16((h == 2 && q == 0) ? 1.f : 0.f);
+                        *reinterpret_cast<__nv_bfloat16 *>(sBz + umma::sw128_offset(32, 8 * h + q, r)) = v;
+                    }
                 }
-                uint4 pk;
-                pk.x = pack_bf16(a[0], a[1]);
-                pk.y = pack_bf16(a[2], a[3]);
-                pk.z = pack_bf16(a[4], a[5]);
-                pk.w = pack_bf16(a[6], a[7]);
-                *reinterpret_cast<uint4 *>(sH2 + umma::sw128_offset(FROWS, r, c0 + q8)) = pk;
             }
-        }
-        umma::fence_async_smem();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {   // logits of the transformed coordinates (pairs); the H2 image out
+            umma::fence_async_smem();
+            umma::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {   // TMEM[T1, T1+128) = H1 W2^T; the H1 image out (first group)
+                umma::fence_after_sync();
+                umma::gemm_128xN(tmem + T1, umma::smem_u32(sH1), umma::smem_u32(sW2), FH, FH, FH, 0);
+                umma::mma_commit(bar_m);
+                if (gi == 0) {
+                    umma::bulk_s2g(imgH1 + tile * 2 * BLK, umma::smem_u32(sH1), BLK);
+                    umma::bulk_s2g(imgH1 + tile * 2 * BLK + BLK, umma::smem_u32(sH1) + BLK, BLK);
+                    umma::bulk_commit();
+                }
+                if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+            }
+            ph_m ^= 1;
+            __syncthreads();
             umma::fence_after_sync();
+            if (abort_flag) break;
+            // ---- H2 = relu(TMEM + b2) -> A operand, its relu mask
+            {
+                const int c0 = UCOL * h;
+                float v[32];
+                umma::tmem_ld32(tmem + lane_base + T1 + (uint32_t)c0, v);
 #pragma unroll
-            for (int p = 0; p < 2; p++) {
-                const int first = 2 * p;
-                if (first >= dB) break;
-                const int N = (first + 1 < dB) ? 2 * CHT : (CHT + 15) / 16 * 16;
-                umma::gemm_128xN(tmem + (uint32_t)(FH + first * CHT), umma::smem_u32(sH2),
-                                 umma::smem_u32(sW3) + (uint32_t)(first * CHT) * 128u, N, FH, NPl, 0);
-            }
-            umma::mma_commit(bar_m);
-            umma::bulk_s2g(imgH2 + tile * 2 * BLK, umma::smem_u32(sH2), BLK);
-            umma::bulk_s2g(imgH2 + tile * 2 * BLK + BLK, umma::smem_u32(sH2) + BLK, BLK);
-            umma::bulk_commit();
-            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
-            umma::bulk_wait_read();   // H1 and H2 images read out: RA may be overwritten
-        }
-        ph_m ^= 1;
-        __syncthreads();
-        umma::fence_after_sync();
-        if (abort_flag) break;
-        // ---- spline forward + backward of (row r, coordinate h); dL/dout -> A operand
-        {
-            float lterm = 0.f;
-            if (h < dB) {
-                const int cz = y.B[h];
-                const float gL = sLW[r];
-                const float2 gl = spline_grad_row<K>(tmem + lane_base + (uint32_t)(FH + h * CHT), sb3 + h * NR,
-                                                     sZ[r * zst + cz], sG[r * zst + cz], gL, sD, r, h * CHT);
-                sG[r * zst + cz] = gl.x;   // dL/d(layer input) of a transformed coordinate
-                lterm = (r0 + r < n) ? gL * gl.y : 0.f;
-            } else if (h == 3) {   // dB <= 3: zero the padding columns [dB CH, NP) of the tile
-                for (int c8 = dB * CHT; c8 < NPl; c8 += 8)
-                    *reinterpret_cast<uint4 *>(sD + umma::sw128_offset(FROWS, r, c8)) = make_uint4(0u, 0u, 0u, 0u);
-            }
+                for (int q8 = 0; q8 < 32; q8 += 8) {
+                    float a[8];
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) lterm += __shfl_xor_sync(0xffffffffu, lterm, off);
-            if ((tid & 31) == 0 && lterm != 0.f) atomicAdd(loss, (double)lterm);
-        }
-        umma::fence_async_smem();
-        umma::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {   // TMEM[0,128) = dL/dout W3; the dL/dout image out
+                    for (int i = 0; i < 8; i++) {
+                        a[i] = v[q8 + i] + sb2[c0 + q8 + i];
+                        m2 |= (a[i] > 0.f ? 1u : 0u) << (q8 + i);
+                        a[i] = fmaxf(a[i], 0.f);
+                    }
+                    uint4 pk;
+                    pk.x = pack_bf16(a[0], a[1]);
+                    pk.y = pack_bf16(a[2], a[3]);
+                    pk.z = pack_bf16(a[4], a[5]);
+                    pk.w = pack_bf16(a[6], a[7]);
+                    *reinterpret_cast<uint4 *>(sH2 + umma::sw128_offset(FROWS, r, c0 + q8)) = pk;
+                }
+            }
+            umma::fence_async_smem();
+            umma::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {   // logits of the group's coordinates (pairs); the H2 image out (first group)
+                if (w3_pending && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
+                umma::fence_after_sync();
+#pragma unroll
+                for (int p = 0; p < 2; p++) {
+                    const int first = 2 * p;   // within the group
+                    if (first >= nc) break;
+                    const int N = (first + 1 < nc) ? 2 * CHT : (CHT + 15) / 16 * 16;
+                    umma::gemm_128xN(tmem + (uint32_t)(FH + first * CHT), umma::smem_u32(sH2),
+                                     umma::smem_u32(sW3) + (uint32_t)(first * CHT) * 128u, N, FH, R3, 0);
+                }
+                umma::mma_commit(bar_m);
+                if (gi == 0) {
+                    umma::bulk_s2g(imgH2 + tile * 2 * BLK, umma::smem_u32(sH2), BLK);
+                    umma::bulk_s2g(imgH2 + tile * 2 * BLK + BLK, umma::smem_u32(sH2) + BLK, BLK);
+                    umma::bulk_commit();
+                }
+                if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+                umma::bulk_wait_read();   // H1 and H2 images read out: RA may be overwritten
+            }
+            if (w3_pending) ph_w ^= 1;
+            w3_pending = false;
+            ph_m ^= 1;
+            __syncthreads();
             umma::fence_after_sync();
-            umma::gemm_128xN_ex(tmem, umma::smem_u32(sD), 0, FROWS, umma::smem_u32(sW3), 1, 0, FH, NPl, 0);
-            umma::mma_commit(bar_m);
-            for (int q = 0; q < nb3l; q++)
-                umma::bulk_s2g(imgD + (tile * pl.NB3 + q) * (int64_t)BLK, umma::smem_u32(sD) + (uint32_t)q * BLK, BLK);
-            umma::bulk_commit();
-            if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
-            umma::bulk_wait_read();
+            if (abort_flag) break;
+            // ---- spline forward + backward of (row r, coordinate 4 gi + h); dL/dout -> A operand
+            {
+                float lterm = 0.f;
+                if (h < nc) {
+                    const int j = 4 * gi + h;
+                    const int cz = y.B[j];
+                    const float gL = sLW[r];
+                    const float2 gl = spline_grad_row<K>(tmem + lane_base + (uint32_t)(FH + h * CHT), sb3 + j * NR,
+                                                         sZ[r * zst + cz], sG[r * zst + cz], gL, sD, r, h * CHT);
+                    sG[r * zst + cz] = gl.x;   // dL/d(layer input) of a transformed coordinate
+                    lterm = (r0 + r < n) ? gL * gl.y : 0.f;
+                } else if (h == 3) {   // fewer than 4 coordinates: zero the padding columns [nc CH, Kg)
+                    for (int c8 = nc * CHT; c8 < Kg; c8 += 8)
+                        *reinterpret_cast<uint4 *>(sD + umma::sw128_offset(FROWS, r, c8)) = make_uint4(0u, 0u, 0u, 0u);
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) lterm += __shfl_xor_sync(0xffffffffu, lterm, off);
+                if ((tid & 31) == 0 && lterm != 0.f) atomicAdd(loss, (double)lterm);
+            }
+            umma::fence_async_smem();
+            umma::fence_before_sync();
+            __syncthreads();
+            // next W3 rows: the following group of this tile, or the first group of the CTA's next tile
+            const bool more = gi + 1 < ngr || (ngr > 1 && tile + gridDim.x < ntiles);
+            if (tid == 0) {   // TMEM[0,128) (+)= dL/dout W3_g; the group's dL/dout image out
+                umma::fence_after_sync();
+                umma::gemm_128xN_ex(tmem, umma::smem_u32(sD), 0, FROWS, umma::smem_u32(sW3), 1, R3, FH, Kg,
+                                    gi > 0 ? 1u : 0u);
+                umma::mma_commit(bar_m);
+                for (int q = 0; q < nbg; q++)
+                    umma::bulk_s2g(imgD + ((tile * ngr + gi) * pl.NB3G + q) * (int64_t)BLK,
+                                   umma::smem_u32(sD) + (uint32_t)q * BLK, BLK);
+                umma::bulk_commit();
+                if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+                umma::bulk_wait_read();
+                if (ngr > 1 && more && !abort_flag) load_w3(gi + 1 < ngr ? gi + 1 : 0, 0u);
+            }
+            if (ngr > 1 && more) w3_pending = true;
+            ph_m ^= 1;
+            __syncthreads();
+            umma::fence_after_sync();
+            if (abort_flag) break;
         }
-        ph_m ^= 1;
-        __syncthreads();
-        umma::fence_after_sync();
         if (abort_flag) break;
         // ---- dH2' = dH2 relu'(H2) -> A operand
         {
@@ -1860,7 +1913,7 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
         __syncthreads();
         if (tid == 0) {   // TMEM[128,256) = dH2' W2; the dH2' image out
             umma::fence_after_sync();
-            umma::gemm_128xN_ex(tmem + FH, umma::smem_u32(sG2), 0, FROWS, umma::smem_u32(sW2), 1, 0, FH, FH, 0);
+            umma::gemm_128xN_ex(tmem + FH, umma::smem_u32(sG2), 0, FROWS, umma::smem_u32(sW2), 1, FH, FH, FH, 0);
             umma::mma_commit(bar_m);
             umma::bulk_s2g(imgG2 + tile * 2 * BLK, umma::smem_u32(sG2), BLK);
             umma::bulk_s2g(imgG2 + tile * 2 * BLK + BLK, umma::smem_u32(sG2) + BLK, BLK);
@@ -1941,10 +1994,12 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
         __syncthreads();
         umma::fence_after_sync();
     }
-    // drain every MMA and bulk copy, then flush the dW1 | db1 accumulator
+    // drain every MMA and bulk copy (a W3 copy is in flight only after a
+    // wait gave up), then flush the dW1 | db1 accumulator
     if (tid == 0) {
         umma::mma_commit(bar_m);
         if (!umma::mbar_wait(bar_m, ph_m)) abort_flag = 1;
+        if (w3_pending && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
         umma::bulk_wait_all();
         if (abort_flag) atomicExch(&g_flow_status, VG_ERR_TIMEOUT);
     }
@@ -1974,8 +2029,9 @@ constexpr int WGI_NT = 128;   // threads of the image weight-gradient kernel
 #define WGI_SPLIT_STRIDE(Mtot) ((int64_t)FH * (Mtot) + 64)
 
 // Weight gradients from the backward's tile images.  blockIdx.y = job: 0 is
-// dW2 = dH2'^T H1, c >= 1 rows [128(c-1), 128c) of the W3 image of
-// dW3 = dL/dout^T H2; blockIdx.x = split over the 128-row tiles.  A K-major
+// dW2 = dH2'^T H1; c >= 1 is chunk (c-1) % NCg (rows [128 chunk, +128)) of
+// coordinate group (c-1) / NCg of dW3 = dL/dout^T H2; blockIdx.x = split
+// over the 128-row tiles.  A K-major
 // image of a 128-row tile is the MN-major tile of its transpose with K =
 // 128 rows, so both operands are read as they are: two stages by bulk copy,
 // thread 0 issues the MMAs (D in TMEM[0,128)) and the row sums against a
@@ -1984,8 +2040,8 @@ constexpr int WGI_NT = 128;   // threads of the image weight-gradient kernel
 // splits WGI_SPLIT_STRIDE floats apart).
 __global__ void __launch_bounds__(WGI_NT) flow_wgrad_img_kernel(
     const uint8_t *__restrict__ imgH1, const uint8_t *__restrict__ imgH2, const uint8_t *__restrict__ imgD,
-    const uint8_t *__restrict__ imgG2, int NB3, int nb3l, int64_t ntiles, int tps, int Mtot,
-    float *__restrict__ part, float *__restrict__ partb)
+    const uint8_t *__restrict__ imgG2, int NB3G, int ngr, int NCg, int dB, int CH, int64_t ntiles, int tps,
+    int Mtot, float *__restrict__ part, float *__restrict__ partb)
 {
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t bars[5];   // full 0/1, empty 0/1, drain
@@ -1999,10 +2055,14 @@ __global__ void __launch_bounds__(WGI_NT) flow_wgrad_img_kernel(
     const int64_t t0 = (int64_t)blockIdx.x * tps;
     const int64_t t1 = t0 + tps < ntiles ? t0 + tps : ntiles;
     const int nst = t1 > t0 ? (int)(t1 - t0) : 0;
-    const int ablk0 = job == 0 ? 0 : 2 * (job - 1);
-    const int anb = job == 0 ? 2 : (nb3l - ablk0 < 2 ? nb3l - ablk0 : 2);
+    // job c >= 1: the group's dL/dout tile has nbg 64-column blocks; this chunk reads two of them
+    const int gq = job == 0 ? 0 : (job - 1) / NCg, cc = job == 0 ? 0 : (job - 1) % NCg;
+    const int ncg = dB - 4 * gq < 4 ? dB - 4 * gq : 4;
+    const int nbg = ((ncg * CH + 15) / 16 * 16 + 63) / 64;
+    const int ablk0 = job == 0 ? 0 : gq * NB3G + 2 * cc;
+    const int anb = job == 0 ? 2 : (nbg - 2 * cc < 2 ? nbg - 2 * cc : 2);
     const uint8_t *Asrc = job == 0 ? imgG2 : imgD;
-    const int64_t astride = job == 0 ? 2 * (int64_t)BLK : (int64_t)NB3 * BLK;
+    const int64_t astride = job == 0 ? 2 * (int64_t)BLK : (int64_t)ngr * NB3G * BLK;
     const uint8_t *Bsrc = job == 0 ? imgH1 : imgH2;
     for (int i = tid; i < 16 * FROWS; i += WGI_NT)
         *reinterpret_cast<__nv_bfloat16 *>(sOnes + umma::sw128_offset(16, i >> 7, i & 127)) = __float2bfloat16(1.f);
@@ -2083,11 +2143,12 @@ __global__ void __launch_bounds__(WGI_NT) flow_wgrad_img_kernel(
 }
 
 // grad += the splits' sums: rows m < 128 of part are dW2 (db2), rows 128 + q
-// the W3 image row q = j CH + o (dW3 row j NR + o, db3); image padding rows
-// are skipped.  Four lanes per element, lane p adding splits p, p + 4, ...
+// of coordinate group q / (128 NCg) row ql = q % (128 NCg) = jl CH + o of
+// the group (coordinate j = 4 group + jl: dW3 row j NR + o, db3); padding
+// rows are skipped.  Four lanes per element, lane p adding splits p, p + 4, ...
 // in order, the four partial sums combined in a fixed tree (deterministic).
 __global__ void flow_wgrad_img_reduce_kernel(const float *__restrict__ part, const float *__restrict__ partb,
-                                             int nsplit, int Mtot, int Mrows, int64_t oW2, int64_t ob2,
+                                             int nsplit, int Mtot, int Mrows, int NCg, int64_t oW2, int64_t ob2,
                                              int64_t oW3, int64_t ob3, int dB, int CH, int NR,
                                              float *__restrict__ grad)
 {
@@ -2119,8 +2180,9 @@ __global__ void flow_wgrad_img_reduce_kernel(const float *__restrict__ part, con
         if (m < FH) {
             dst = bias ? ob2 + m : oW2 + (int64_t)m * FH + c;
         } else {
-            const int q = m - FH, j = q / CH, o = q % CH;
-            if (j >= dB || o >= NR) continue;
+            const int q = m - FH, ql = q % (FH * NCg), jl = ql / CH, o = ql % CH;
+            const int j = 4 * (q / (FH * NCg)) + jl;
+            if (jl >= 4 || j >= dB || o >= NR) continue;
             dst = bias ? ob3 + (int64_t)j * NR + o : oW3 + ((int64_t)j * NR + o) * FH + c;
         }
         grad[dst] += s;
@@ -2183,17 +2245,19 @@ int set_smem(const void *kern, size_t bytes)
 // weight-gradient grid (about one CTA per SM over all jobs).
 struct BwdSizes {
     int64_t ntiles;
-    int NB3, NC3, Mtot, nsplit, tps;
+    int NB3G, NCg, ngr, Mtot, nsplit, tps;   // per coordinate group: image blocks, 128-row chunks
 };
 
 BwdSizes bwd_sizes(const FlowGeom &g, int64_t n)
 {
     BwdSizes s;
+    const BwdPlan pl = bwd_plan(g);
     s.ntiles = (n + FROWS - 1) / FROWS;
-    s.NB3 = (g.NPmax + 63) / 64;
-    s.NC3 = (g.NPmax + 127) / 128;
-    s.Mtot = FH * (1 + s.NC3);
-    int64_t target = vg_num_sms() / (1 + s.NC3);
+    s.NB3G = pl.NB3G;
+    s.NCg = (pl.NPG + 127) / 128;
+    s.ngr = (g.dBmax + 3) / 4;
+    s.Mtot = FH * (1 + s.ngr * s.NCg);
+    int64_t target = vg_num_sms() / (1 + s.ngr * s.NCg);
     if (target < 1) target = 1;
     s.tps = (int)((s.ntiles + target - 1) / target);
     if (s.tps < 1) s.tps = 1;
@@ -2221,7 +2285,7 @@ BwdWork bwd_work(const FlowGeom &g, int64_t n, void *work)
     b.imgH1 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
     b.imgH2 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
     b.imgG2 = (uint8_t *)take(s.ntiles * 2 * (int64_t)BLK);
-    b.imgD = (uint8_t *)take(s.ntiles * s.NB3 * (int64_t)BLK);
+    b.imgD = (uint8_t *)take(s.ntiles * s.ngr * s.NB3G * (int64_t)BLK);
     b.part = (float *)take((int64_t)s.nsplit * WGI_SPLIT_STRIDE(s.Mtot) * 4);
     b.partb = (float *)take((int64_t)s.nsplit * s.Mtot * 4);
     b.ld = (float *)take(n * 4);
@@ -2366,7 +2430,7 @@ static int flow_grad_umma(const FlowGeom &g, const vg_flow *fl, int64_t n, const
                           void *work, size_t work_bytes, cudaStream_t st, int *used)
 {
     *used = 0;
-    if (g_flow_force_legacy || (g.K != 32 && g.K != 16) || g.dBmax > 4 || g.dAmax > 8) return VG_OK;
+    if (g_flow_force_legacy || (g.K != 32 && g.K != 16) || g.dBmax > 8 || g.dAmax > 8) return VG_OK;
     const void *kb = g.K == 32 ? (const void *)flow_bwd_umma_kernel<32> : (const void *)flow_bwd_umma_kernel<16>;
     size_t stat = 0;
     cudaFuncAttributes fa;
@@ -2401,12 +2465,14 @@ static int flow_grad_umma(const FlowGeom &g, const vg_flow *fl, int64_t n, const
                 g, l, fl->theta, (const __nv_bfloat16 *)fl->mirror, n, s.ntiles, b.zl, gcur, w, gnext, b.imgH1,
                 b.imgH2, b.imgD, b.imgG2, fl->grad, fl->loss);
         VG_LAUNCH_CHECK();
-        const int nb3l = (y.NP + 63) / 64, nc3l = (y.NP + 127) / 128;
-        flow_wgrad_img_kernel<<<dim3((unsigned)s.nsplit, (unsigned)(1 + nc3l)), WGI_NT, wsm, st>>>(
-            b.imgH1, b.imgH2, b.imgD, b.imgG2, s.NB3, nb3l, s.ntiles, s.tps, s.Mtot, b.part, b.partb);
+        const int ngl = (y.dB + 3) / 4, njobs = 1 + ngl * s.NCg;
+        flow_wgrad_img_kernel<<<dim3((unsigned)s.nsplit, (unsigned)njobs), WGI_NT, wsm, st>>>(
+            b.imgH1, b.imgH2, b.imgD, b.imgG2, s.NB3G, ngl, s.NCg, y.dB, g.CH, s.ntiles, s.tps, s.Mtot, b.part,
+            b.partb);
         VG_LAUNCH_CHECK();
-        flow_wgrad_img_reduce_kernel<<<1024, 256, 0, st>>>(b.part, b.partb, s.nsplit, s.Mtot, FH * (1 + nc3l), y.oW2,
-                                                          y.ob2, y.oW3, y.ob3, y.dB, g.CH, 2 * g.K + 1, fl->grad);
+        flow_wgrad_img_reduce_kernel<<<1024, 256, 0, st>>>(b.part, b.partb, s.nsplit, s.Mtot, FH * njobs, s.NCg,
+                                                          y.oW2, y.ob2, y.oW3, y.ob3, y.dB, g.CH, 2 * g.K + 1,
+                                                          fl->grad);
         VG_LAUNCH_CHECK();
         float *tmp = gcur;
         gcur = gnext;

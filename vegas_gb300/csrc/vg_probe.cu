@@ -140,7 +140,8 @@ __global__ void __launch_bounds__(128) probe_umma_kernel(const __nv_bfloat16 *__
     umma::fence_after_sync();
     const uint32_t tmem = slot;
     if (tid == 0) {
-        umma::gemm_128xN_ex(tmem, umma::smem_u32(sa), a_mn, 128, umma::smem_u32(sb), b_mn, N, N, K, 0);
+        umma::gemm_128xN_ex(tmem, umma::smem_u32(sa), a_mn, a_mn ? 0 : 128, umma::smem_u32(sb), b_mn, b_mn ? 0 : N, N,
+                            K, 0);
         umma::mma_commit(umma::smem_u32(&bar));
     }
     const bool ok = umma::mbar_wait(umma::smem_u32(&bar), 0);

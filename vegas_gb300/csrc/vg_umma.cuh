@@ -124,10 +124,12 @@ __device__ __forceinline__ void gemm_128xN(uint32_t tmem_d, uint32_t a_saddr, ui
 }
 
 // General form with either operand K-major or MN-major.  An MN-major operand
-// X (MN x Kt) is the SW128 tile of its transpose: Kt rows of MN elements,
-// i.e. what sw128_offset(Kt, k, mn) addresses; its descriptor steps 64-element
-// MN blocks by LBO = Kt * 128 bytes and 8-row K groups by SBO = 1024 bytes,
-// and a K step of 16 advances the start by 16 rows (2048 bytes).
+// X (MN x Kt) is the SW128 tile of its transpose: R rows of MN elements (R >=
+// Kt, the first Kt used), i.e. what sw128_offset(R, k, mn) addresses; its
+// descriptor steps 64-element MN blocks by LBO = R * 128 bytes and 8-row K
+// groups by SBO = 1024 bytes, and a K step of 16 advances the start by 16
+// rows (2048 bytes).  a_rows / b_rows: the K-major tile's row count (the
+// stride of its 64-column blocks), or R of an MN-major tile (0: R = Kt).
 __device__ __forceinline__ uint64_t sdesc_sw128_lbo(uint32_t saddr, uint32_t lbo)
 {
     return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
@@ -141,9 +143,9 @@ __device__ __forceinline__ void gemm_128xN_ex(uint32_t tmem_d, uint32_t a_saddr,
     const uint32_t idesc = idesc_bf16(128, N) | ((uint32_t)(a_mn ? 1 : 0) << 15) | ((uint32_t)(b_mn ? 1 : 0) << 16);
     for (int k = 0; k < Kt; k += 16) {
         uint64_t ad, bd;
-        if (a_mn) ad = sdesc_sw128_lbo(a_saddr + (uint32_t)k * 128u, (uint32_t)Kt * 128u);
+        if (a_mn) ad = sdesc_sw128_lbo(a_saddr + (uint32_t)k * 128u, (uint32_t)(a_rows > 0 ? a_rows : Kt) * 128u);
         else ad = sdesc_sw128(a_saddr + (uint32_t)((k >> 6) * a_rows * 128 + ((k & 63) << 1)));
-        if (b_mn) bd = sdesc_sw128_lbo(b_saddr + (uint32_t)k * 128u, (uint32_t)Kt * 128u);
+        if (b_mn) bd = sdesc_sw128_lbo(b_saddr + (uint32_t)k * 128u, (uint32_t)(b_rows > 0 ? b_rows : Kt) * 128u);
         else bd = sdesc_sw128(b_saddr + (uint32_t)((k >> 6) * b_rows * 128 + ((k & 63) << 1)));
         mma_bf16(tmem_d, ad, bd, idesc, (k > 0 || accumulate) ? 1u : 0u);
     }
