@@ -24,8 +24,8 @@
 //   flow_mirror_kernel  BF16 copies of W2, W3 (and transposes) for the MMAs
 // These run the 128x128 hidden layer and the output layer as BF16
 // mma.sync.m16n8k16 with FP32 accumulation; they serve the configurations
-// the tcgen05 kernels do not fit (more than 4 transformed coordinates per
-// layer, K outside {16, 32}).  The 5th-generation tensor-core kernels:
+// the tcgen05 kernels do not fit (K outside {16, 32}) and are the tests'
+// comparison path.  The 5th-generation tensor-core kernels:
 //   flow_pass_umma_kernel   inference / training forward through all layers
 //   flow_bwd_umma_kernel    training backward of one layer: forward
 //                           recomputation, spline backward in registers,
