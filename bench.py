@@ -422,7 +422,7 @@ def _jsonable(o):
     raise TypeError(type(o).__name__)
 
 
-def lattice_flow_line(dev, nlam=8, neval=1 << 20):
+def lattice_flow_line(dev, nlam=8, neval=1 << 20, train_itn=100, train_steps=2):
     """The flow on the lattice couplings: for a subset of the 64 lambda of
     the scan, flow-augmented vegas+ (FlowIntegrator: 6 coupling layers,
     32-bin splines, 2x128 conditioners, as on the mixture) against plain
@@ -437,8 +437,9 @@ def lattice_flow_line(dev, nlam=8, neval=1 << 20):
     scan = np.exp(np.linspace(np.log(0.01), np.log(1.0), 64))
     lams = [float(v) for v in scan[np.linspace(0, 63, nlam).round().astype(int)]]
     out = {'workload': 'dim-16 periodic lattice action, a=0.5, x in [-5,5]^16, lambda in %s, %d evaluations '
-                       'per iteration; plain vegas+ 50 + 20 iterations; flow-augmented vegas+ 30 plain + 40 '
-                       'flow (trained) + 20 measured' % ([round(v, 4) for v in lams], neval), 'per_lambda': {}}
+                       'per iteration; plain vegas+ 50 + 20 iterations; flow-augmented vegas+ 30 plain + %d '
+                       'flow (trained, %d Adam steps each) + 20 measured'
+                       % ([round(v, 4) for v in lams], neval, train_itn, train_steps), 'per_lambda': {}}
     lim = 16 * [[-5.0, 5.0]]
     for lam in lams:
         f = vg.LatticeAction(0.5, float(lam))
@@ -450,9 +451,9 @@ def lattice_flow_line(dev, nlam=8, neval=1 << 20):
         r = I(f, nitn=20)
         torch.cuda.synchronize()
         tp = (time.perf_counter() - t0) / 20
-        fi = FlowIntegrator(lim, neval=neval, seed=3, device=dev, plain_itn=30, kl_itn=10, train_itn=40,
-                            grace=10, patience=3, train_steps=4, train_batch=1 << 15, lr=1e-3)
-        fi(f, nitn=70)
+        fi = FlowIntegrator(lim, neval=neval, seed=3, device=dev, plain_itn=30, kl_itn=10, train_itn=train_itn,
+                            grace=10, patience=3, train_steps=train_steps, train_batch=1 << 15, lr=1e-3)
+        fi(f, nitn=30 + train_itn)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rf = fi(f, nitn=20)
