@@ -68,12 +68,15 @@ class Flow(object):
         self.theta.copy_(torch.as_tensor(np.asarray(theta, np.float32)))
         self.refresh()
 
-    def sample(self, zhat):
-        """zhat [n, dim] (float32, unit cube) -> (z, logdet), log|dz/dzhat| = -logdet."""
+    def sample(self, zhat, z=None, ld=None):
+        """zhat [n, dim] (float32, unit cube) -> (z, logdet), log|dz/dzhat| = -logdet.
+        z, ld: optional output tensors ([n, dim] and [n] float32)."""
         zhat = zhat.to(self.device, torch.float32).contiguous()
         n = zhat.shape[0]
-        z = torch.empty_like(zhat)
-        ld = torch.empty(n, dtype=torch.float32, device=self.device)
+        if z is None:
+            z = torch.empty_like(zhat)
+        if ld is None:
+            ld = torch.empty(n, dtype=torch.float32, device=self.device)
         N.check(N.load().vg_flow_sample(ctypes.byref(self._struct()), n, N.ptr(zhat), N.ptr(z),
                                         N.ptr(ld), N.stream_ptr(self.device)))
         return z, ld

@@ -96,6 +96,7 @@ class FlowIntegrator(object):
         self.plain_scores = []
         self.losing = 0
         self.strat = None            # stratification integrator on [0,1]^d (flow phase)
+        self._bufs = {}              # per-iteration device buffers, reused
         self.map = None              # frozen AdaptiveMap (flow phase)
         self._nit = 0
         self._flow_nit = 0
@@ -151,6 +152,13 @@ class FlowIntegrator(object):
         f = f.contiguous()
         N.check(L.vg_weight_points(n, N.ptr(f), N.ptr(jac), N.ptr(ld), N.ptr(out), stream))
 
+    def _buf(self, name, *shape):
+        """A float32 device tensor of the given shape, kept for reuse."""
+        t = self._bufs.get(name)
+        if t is None or tuple(t.shape) != shape:
+            t = self._bufs[name] = torch.empty(shape, dtype=torch.float32, device=self.device)
+        return t
+
     def _flow_iteration(self, fcn, train):
         s = self.strat
         L = N.load()
@@ -160,13 +168,14 @@ class FlowIntegrator(object):
         n = int(s._read_stats().neval)
         s._itn += 1
         itn_word = s._itn & 0xffffffff
-        yv, _, wgt, hc = s._points(it, ncap, itn_word, None, want_hc=train)
+        # the iteration's device buffers are kept and reused (no allocator traffic per iteration)
+        yv, _, wgt, hc = s._points(it, ncap, itn_word, None, want_hc=train, bufs=self._bufs)
         yv = yv[:n]
-        yp, ld = self.flow.sample(yv)
-        x = torch.empty_like(yp)
-        jac = torch.empty(n, dtype=torch.float32, device=self.device)
+        yp, ld = self.flow.sample(yv, z=self._buf('yp', ncap, self.dim)[:n], ld=self._buf('ld', ncap)[:n])
+        x = self._buf('xm', ncap, self.dim)[:n]
+        jac = self._buf('jac', ncap)[:n]
         self.map.map(yp, x, jac)
-        f = torch.empty(ncap, dtype=torch.float32, device=self.device)
+        f = self._buf('f', ncap)
         self._feff(fcn, x, jac, ld, f)
         N.check(L.vg_reduce(ctypes.byref(it), itn_word, None, N.ptr(f), N.VG_F32, stream))
         if train and self.train_steps > 0:

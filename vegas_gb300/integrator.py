@@ -304,16 +304,27 @@ class Integrator(object):
         N.check(L.vg_allocate(ctypes.byref(it), N.stream_ptr(self.device)))
 
     # ------------------------------------------------------------- sampling
-    def _points(self, it, ncap, itn, u, want_y=False, want_hc=False, want_w=True, keep=None):
+    def _points(self, it, ncap, itn, u, want_y=False, want_hc=False, want_w=True, keep=None, bufs=None):
         """x (and y, weights, hypercubes) of the current allocation; with
         ``keep`` (a device buffer of vg_keep_bytes) the sampler also keeps
-        each sample's Jacobian and training bins for vg_reduce_kept."""
+        each sample's Jacobian and training bins for vg_reduce_kept.  With
+        ``bufs`` (a dict) the output tensors are kept there and reused by
+        the next call of the same size."""
         L = N.load()
         dt = torch.float64 if self.precision == 'fp64' else torch.float32
-        x = torch.empty((ncap, self.dim), dtype=dt, device=self.device)
-        y = torch.empty((ncap, self.dim), dtype=dt, device=self.device) if want_y else None
-        w = torch.empty(ncap, dtype=torch.float64, device=self.device) if want_w else None
-        hc = torch.empty(ncap, dtype=torch.int64, device=self.device) if want_hc else None
+
+        def out(name, shape, dtype):
+            if bufs is None:
+                return torch.empty(shape, dtype=dtype, device=self.device)
+            t = bufs.get(name)
+            if t is None or tuple(t.shape) != tuple(shape) or t.dtype != dtype:
+                t = bufs[name] = torch.empty(shape, dtype=dtype, device=self.device)
+            return t
+
+        x = out('x', (ncap, self.dim), dt)
+        y = out('y', (ncap, self.dim), dt) if want_y else None
+        w = out('w', (ncap,), torch.float64) if want_w else None
+        hc = out('hc', (ncap,), torch.int64) if want_hc else None
         if keep is None:
             N.check(L.vg_sample(ctypes.byref(it), itn, N.ptr(u), N.ptr(x), N.ptr(y), N.ptr(w),
                                 N.ptr(hc), ncap, N.stream_ptr(self.device)))
