@@ -37,9 +37,12 @@ def test_flow_beats_plain_vegas_on_mixture():
     plain(f, nitn=50)
     rp = plain(f, nitn=10)
     v_plain = np.median([r.sdev ** 2 for r in rp.itn_results]) * plain.last_neval
-    F = FlowIntegrator(8 * [[0, 1]], neval=neval, seed=11, plain_itn=10, kl_itn=10, train_itn=40,
-                       grace=1000, train_steps=6, train_batch=1 << 15)
-    F(f, nitn=50)                      # 10 plain + 40 training flow iterations
+    # the training schedule of the benchmark (30 of the 100 training
+    # iterations on the KL loss, 2 Adam steps each): the shorter 40 x 6-step
+    # schedule left the flow short of the 5x gain in about one run in four
+    F = FlowIntegrator(8 * [[0, 1]], neval=neval, seed=11, plain_itn=10, kl_itn=30, train_itn=100,
+                       grace=1000, train_steps=2, train_batch=1 << 15)
+    F(f, nitn=110)                     # 10 plain + 100 training flow iterations
     rf = F(f, nitn=20)                 # frozen flow
     assert F.flow_on
     # medians over 20 iterations each (a median of 10 variance estimates

@@ -1017,6 +1017,25 @@ __device__ __forceinline__ float spline_reg(float (&o)[2 * K + 1], float x, floa
 }
 
 
+// Output biases staged in shared memory: coordinate j's 2K+1 values at
+// j * bias_stride(K) floats (padded to a multiple of 4), added to the
+// logits with 16-byte loads.
+__host__ __device__ constexpr int bias_stride(int K) { return (2 * K + 1 + 3) / 4 * 4; }
+
+template <int K>
+__device__ __forceinline__ void add_bias(float (&o)[2 * K + 1], const float *bb)
+{
+    constexpr int NR = 2 * K + 1;
+#pragma unroll
+    for (int q = 0; q < NR; q += 4) {
+        const float4 b = *reinterpret_cast<const float4 *>(bb + q);
+        o[q] += b.x;
+        if (q + 1 < NR) o[q + 1] += b.y;
+        if (q + 2 < NR) o[q + 2] += b.z;
+        if (q + 3 < NR) o[q + 3] += b.w;
+    }
+}
+
 constexpr int UST_MAX = 16;      // 128-row sub-tiles per super-tile
 constexpr int WG_SPLIT = 64;     // split-K chunks of the weight-gradient GEMMs
 constexpr int UNT = 512;         // threads of the tcgen05 pass: 16 warps
@@ -1046,7 +1065,7 @@ __host__ __device__ inline UmmaPlan umma_plan(const FlowGeom &g, int ST)
     p.oW1 = o; o += sizeof(float) * FH * 8;
     p.ob1 = o; o += sizeof(float) * FH;
     p.ob2 = o; o += sizeof(float) * FH;
-    p.ob3 = o; o += sizeof(float) * 8 * (2 * g.K + 1);   // dB <= 8 coordinates of 2K + 1 outputs
+    p.ob3 = o; o += sizeof(float) * 8 * bias_stride(g.K);   // dB <= 8 coordinates of 2K + 1 outputs (padded)
     p.oZ = o;  o += sizeof(float) * (size_t)ST * FROWS * p.zst;
     p.oLD = o; o += sizeof(float) * UNH * (size_t)ST * FROWS;
     p.total = o + 1024;          // + alignment slack of the dynamic base
@@ -1140,7 +1159,7 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                 sb1[i] = theta[y.ob1 + i];
                 sb2[i] = theta[y.ob2 + i];
             }
-            for (int i = tid; i < y.dB * NR; i += UNT) sb3[i] = theta[y.ob3 + i];
+            for (int i = tid; i < y.dB * NR; i += UNT) sb3[(i / NR) * bias_stride(K) + i % NR] = theta[y.ob3 + i];
             // one thread waits on the mbarrier; the others park at the CTA barrier
             if (tid == 0 && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
             ph_w ^= 1;
@@ -1248,9 +1267,7 @@ __global__ void __launch_bounds__(UNT, 1) flow_pass_umma_kernel(FlowGeom g, cons
                     }
                     if (NR > 64) o[64] = umma::tmem_ld1(tmem + lane_base + col + 64u);
                 }
-                const float *bb = sb3 + j * NR;
-#pragma unroll
-                for (int q = 0; q < NR; q++) o[q] += bb[q];
+                add_bias<K>(o, sb3 + j * bias_stride(K));
                 const int cz = y.B[j];
                 const float xin = Zs[r * zst + cz];
                 float lp;
@@ -1547,8 +1564,7 @@ __device__ __noinline__ float2 spline_grad_row(uint32_t taddr, const float *bb, 
         }
         if (NR > 64) o[64] = umma::tmem_ld1(taddr + 64u);
     }
-#pragma unroll
-    for (int q = 0; q < NR; q++) o[q] += bb[q];
+    add_bias<K>(o, bb);
     float lp;
     const float gx = spline_grad_reg<K>(o, x, gC, gL, lp);
 #pragma unroll
@@ -1603,7 +1619,7 @@ __host__ __device__ inline BwdPlan bwd_plan(const FlowGeom &g)
     p.oW1 = o; o += sizeof(float) * FH * 8;
     p.ob1 = o; o += sizeof(float) * FH;
     p.ob2 = o; o += sizeof(float) * FH;
-    p.ob3 = o; o += sizeof(float) * g.dBmax * (2 * g.K + 1);
+    p.ob3 = o; o += sizeof(float) * g.dBmax * bias_stride(g.K);
     p.oZ = o;  o += sizeof(float) * FROWS * zst;
     p.oG = o;  o += sizeof(float) * FROWS * zst;
     p.oLW = o; o += sizeof(float) * FROWS;
@@ -1706,7 +1722,7 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
         sb1[i] = theta[y.ob1 + i];
         sb2[i] = theta[y.ob2 + i];
     }
-    for (int i = tid; i < dB * NR; i += BNT) sb3[i] = theta[y.ob3 + i];
+    for (int i = tid; i < dB * NR; i += BNT) sb3[(i / NR) * bias_stride(K) + i % NR] = theta[y.ob3 + i];
     if (tid == 0 && !umma::mbar_wait(bar_w, ph_w)) abort_flag = 1;
     ph_w ^= 1;
     __syncthreads();
@@ -1856,7 +1872,7 @@ __global__ void __launch_bounds__(BNT, 1) flow_bwd_umma_kernel(
                     const int j = 4 * gi + h;
                     const int cz = y.B[j];
                     const float gL = sLW[r];
-                    const float2 gl = spline_grad_row<K>(tmem + lane_base + (uint32_t)(FH + h * CHT), sb3 + j * NR,
+                    const float2 gl = spline_grad_row<K>(tmem + lane_base + (uint32_t)(FH + h * CHT), sb3 + j * bias_stride(K),
                                                          sZ[r * zst + cz], sG[r * zst + cz], gL, sD, r, h * CHT);
                     sG[r * zst + cz] = gl.x;   // dL/d(layer input) of a transformed coordinate
                     lterm = (r0 + r < n) ? gL * gl.y : 0.f;
