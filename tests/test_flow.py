@@ -11,8 +11,8 @@ rounding of activations and weights:
                                      <= 4u in every parameter block (W1,
                                      b1, W2, b2, W3, b3 of each layer),
                                      u = 2^-9 the BF16 unit roundoff
-(the backward rounds dL/dout, dL/dh2', dL/dh1' and the transposed
-activations to BF16 for the tensor-core weight-gradient GEMMs -- one BF16
+(the backward rounds dL/dout, dL/dh2', dL/dh1' and the activations to
+BF16 for the tensor-core weight-gradient GEMMs -- one BF16
 rounding of each operand, which the oracle does not emulate -- so each
 block carries a relative error of order u; measured: at most 3u per block
 and 1.3u overall on these cases).
