@@ -11,27 +11,27 @@
 // out[j(2K+1) + K + k] K+1 vertex logits.  Parameter layout, masks and spline
 // match oracle/flow_oracle.py (the FP64 checker).
 //
-// Kernels (CTA = 256 threads = 8 warps, 128 rows per tile):
-//   flow_pass_kernel    sampling or density pass through all layers (inference)
-//   flow_fwd_kernel     training forward: density pass storing each layer input
-//   flow_bwd_kernel     training backward of one layer: recompute activations,
-//                       spline backward, dOUT/dH2/dH1 through the MLP, write
-//                       the transposed activations/gradients the weight
-//                       gradients need
-//   flow_wgrad_kernel   weight gradients dW = dY^T X over the batch as split-K
-//                       GEMMs (K = batch rows) + flow_wgrad_reduce_kernel
-//   flow_adam_kernel    Adam update of the FP32 parameters
-//   flow_mirror_kernel  BF16 copies of W2, W3 (and transposes) for the MMAs
-// These run the 128x128 hidden layer and the output layer as BF16
-// mma.sync.m16n8k16 with FP32 accumulation; they serve the configurations
-// the tcgen05 kernels do not fit (K outside {16, 32}) and are the tests'
-// comparison path.  The 5th-generation tensor-core kernels:
-//   flow_pass_umma_kernel   inference / training forward through all layers
+// Kernels on the 5th-generation tensor cores (CTA = 512 threads = 16 warps,
+// one per SM, TMEM accumulators; K in {16, 32}):
+//   flow_pass_umma_kernel   inference (sampling / density) and the training
+//                           forward (storing each layer's input)
 //   flow_bwd_umma_kernel    training backward of one layer: forward
 //                           recomputation, spline backward in registers,
 //                           dH2, dH1 and dW1 with TMEM accumulators
 //   flow_wgrad_img_kernel   dW2, dW3 (and db2, db3) over the backward's
 //                           tile images + flow_wgrad_img_reduce_kernel
+// Kernels on mma.sync.m16n8k16 (BF16, FP32 accumulation; CTA = 256 threads,
+// 128 rows per tile), for K outside {16, 32} and as the tests' comparison
+// path:
+//   flow_pass_kernel        inference and training forward
+//   flow_bwd_kernel         training backward of one layer: recompute
+//                           activations, spline backward, dOUT/dH2/dH1
+//                           through the MLP, the transposed activations and
+//                           gradients for flow_wgrad_umma_kernel (split-K
+//                           weight gradients on tcgen05) + flow_wgrad_reduce_kernel
+// Shared by both: flow_adam_kernel (Adam on the FP32 parameters),
+// flow_mirror_kernel (BF16 copies and tcgen05 operand images of W2, W3),
+// train_gather_kernel / train_norm_kernel (the training batch).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
