@@ -2295,9 +2295,13 @@ BwdWork bwd_work(const FlowGeom &g, int64_t n, void *work)
 {
     const BwdSizes s = bwd_sizes(g, n);
     BwdWork b;
-    char *p = (char *)work;
+    char *p = (char *)work;   // nullptr: sizes only
     int64_t o = 0;
-    auto take = [&](int64_t bytes) { char *q = p + o; o += (bytes + 255) & ~255LL; return q; };
+    auto take = [&](int64_t bytes) {
+        char *q = p != nullptr ? p + o : nullptr;
+        o += (bytes + 255) & ~255LL;
+        return q;
+    };
     b.zl = (float *)take((int64_t)g.L * n * g.dim * 4);
     b.ga = (float *)take(n * g.dim * 4);
     b.gb = (float *)take(n * g.dim * 4);
