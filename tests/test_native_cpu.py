@@ -68,3 +68,22 @@ def test_strata_complex_power_quirk():
     import vegas_gb300 as vg
     assert list(vg.strata(1, 0, 10 ** 6, True, None)['nstrat']) == [124000]
     assert list(vg.strata(1, 0, 10 ** 5, True, None)['nstrat']) == [12000]
+
+
+@pytest.mark.parametrize('dim,K', [(8, 32), (16, 32), (4, 16)])
+def test_flow_train_workspace_sizes(dim, K):
+    """vg_flow_train_bytes (a host-side size query): positive, growing with
+    the batch, and at least the tile images of the tensor-core backward
+    (H1, H2, dH2' at 32 KB and dL/dout at up to 2 x 80 KB per 128-row tile)."""
+    L = N.load()
+    s = N.VgFlow()
+    s.dim, s.nlayers, s.K, s.hidden = dim, 6, K, 128
+    prev = 0
+    for n in (1, 128, 777, 1 << 15):
+        b = int(L.vg_flow_train_bytes(ctypes.byref(s), n))
+        assert b > prev
+        tiles = (n + 127) // 128
+        assert b >= tiles * 3 * 32768
+        prev = b
+    s.hidden = 64   # unsupported width: the query reports an error
+    assert int(L.vg_flow_train_bytes(ctypes.byref(s), 128)) < 0
